@@ -1,0 +1,318 @@
+#!/usr/bin/env python3
+"""Benchmark: first-hit voxel traversal throughput (Mrays/s) on one GB300.
+
+Workload (default ``shapes1024``): a 1024^3 u8 palette-index grid with 10,000 seeded boxes and
+spheres (radius 2-40), rendered at 1920x1080 with one primary ray per pixel plus one hard-shadow
+ray per lit hit toward a seeded directional light.  A step is one frame: one ``vt_render``
+launch over the whole image.  Rays counted = primary rays + shadow rays actually traced.
+
+  value        device time of the render kernel (CUDA events on the launching stream), grid
+               resident in HBM, L2 flushed (256 MiB write) between timed frames
+  e2e          the same frame through ``vt_render_host``: camera/light in, all hit records copied
+               back to pinned host memory every step, host wall clock
+  roofline     algorithmic bytes of the render kernel per launch (per ray: 4 B per brick
+               directory entry visited, 64 B per occupied-brick mask entered, 5 B payload and
+               palette per hit, 16 B hit record) / kernel time, against the measured HBM copy
+               bandwidth
+  cpu_baseline the CPU oracle (the reference traversal restated in C) on bands of rows of the same
+               frame, all host cores
+
+``--impl reference`` times that CPU restatement alone (rank 0 only).  Under torchrun (N > 1) each
+rank renders its own replica of the frame (replicas only: rays are independent and nothing is
+exchanged); value = all ranks' rays / max-over-ranks time.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s (1080p, 1024^3 grid)"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--config", choices=["shapes1024", "terrain256"], default="shapes1024")
+    p.add_argument("--cpu-seconds", type=float, default=2.0,
+                   help="wall-clock budget of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def build_workload(name):
+    from vtrace_gb300 import workloads
+    return workloads.shapes1024() if name == "shapes1024" else workloads.terrain256()
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        self.t0 = time.time()
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.remove(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_sample(w, seconds, threads=0):
+    """The CPU oracle on bands of 8 rows spread over the frame until `seconds` of wall time."""
+    from oracle import pyoracle as po
+    og = po.Grid(w["voxels"], w["palette"])
+    cam = po.make_camera(w["camera"].as_dict())
+    L = w["light"]
+    light = po.make_light(list(L.dir), L.ambient, bool(L.shadows))
+    threads = threads or po.hardware_threads()
+    H = cam.height
+    band = 8
+    order = np.random.default_rng(0).permutation(H // band)
+    rays = 0
+    rows = 0
+    t0 = time.perf_counter()
+    for b in order:
+        r0 = int(b) * band
+        _, st = po.render(og, cam, light, threads=threads, stats=True, rows=(r0, r0 + band))
+        rays += st["rays"]
+        rows += band
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": "%d of %d rows of the %dx%d frame in 8-row bands (%d rays incl. shadow "
+                      "rays), %.1f s wall" % (rows, H, cam.width, H, rays, dt)}
+
+
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import pyoracle as po
+    w = build_workload(args.config)
+    og = po.Grid(w["voxels"], w["palette"])
+    cam = po.make_camera(w["camera"].as_dict())
+    L = w["light"]
+    light = po.make_light(list(L.dir), L.ambient, bool(L.shadows))
+    threads = po.hardware_threads()
+    H = cam.height
+    # a step renders one contiguous band of rows at a seeded offset (bands cycle over the
+    # frame); the band is sized to ~0.25 s from a first 8-row sample and capped so the whole
+    # run stays within a few minutes
+    t0 = time.perf_counter()
+    po.render(og, cam, light, threads=threads, rows=(H // 2, H // 2 + 8))
+    per_row = (time.perf_counter() - t0) / 8
+    rows_per_step = max(1, min(H, int(0.25 / max(per_row, 1e-6))))
+    budget_rows = int(150.0 / max(per_row, 1e-6))
+    rows_per_step = max(1, min(rows_per_step, budget_rows // max(1, args.steps + args.warmup)))
+    offsets = np.random.default_rng(1).integers(0, H - rows_per_step + 1, args.steps + args.warmup)
+
+    def step(k):
+        r0 = int(offsets[k])
+        _, st = po.render(og, cam, light, threads=threads, stats=True,
+                          rows=(r0, r0 + rows_per_step))
+        return st["rays"]
+
+    for k in range(args.warmup):
+        step(k)
+    rays = 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        rays += step(args.warmup + k)
+    dt = time.perf_counter() - t0
+    value = rays / dt / 1e6
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "impl": "reference",
+        "config": {"workload": w["name"], "sample_rows_per_step": rows_per_step},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": "a band of %d contiguous rows of the frame per step at "
+                                   "seeded offsets, %d host threads" % (rows_per_step, threads)},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import vtrace_gb300 as vt
+
+    rank, local_rank, world = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    vt.init(dev)
+    w = build_workload(args.config)
+    cam, light = w["camera"], w["light"]
+    grid = vt.Grid.from_u8(w["voxels"], w["palette"])
+    npx = cam.width * cam.height
+    d_hits = torch.empty(npx * 16, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    # counters of one frame (counting kernel, not timed): rays traced and algorithmic bytes
+    stats = vt.render_stats(grid, cam, light, d_hits)
+    rays_per_frame = stats["rays"]
+    algo_bytes = (4 * stats["bricks_entered"] + 64 * stats["nonempty_bricks_entered"] +
+                  5 * stats["hits"] + 16 * npx)
+
+    for _ in range(args.warmup):
+        vt.render(grid, cam, light, d_hits, stream)
+    torch.cuda.synchronize()
+    shadow_rays = int(((d_hits.view(-1, 16)[:, 7] & vt.FLAG_SHADOW_RAY) != 0).sum().item())
+    assert shadow_rays + npx == rays_per_frame, (shadow_rays, npx, rays_per_frame)
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    sampler = ClockSampler(dev) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)  # 256 MiB write: evicts the 129 MB L2 between frames
+        starts[k].record(stream)
+        vt.render(grid, cam, light, d_hits, stream)
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop() if sampler else None
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * rays_per_frame / (ms * 1e-3) / 1e6
+
+    # end to end through the C ABI with a pinned host output buffer
+    host_out = torch.empty(npx * 16, dtype=torch.uint8, pin_memory=True)
+    for _ in range(2):
+        vt.render_host(grid, cam, light, out=host_out)
+    e2e_times = []
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vt.render_host(grid, cam, light, out=host_out)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_times) / len(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * rays_per_frame / e2e_s / 1e6, "unit": "Mrays/s",
+           "h2d_bytes_per_step": 76, "d2h_bytes_per_step": npx * 16,
+           "path": "vt_render_host (C ABI), pinned host output"}
+
+    peak, peak_kind = measured_peak()
+    achieved = algo_bytes / (ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generators, no dataset)",
+        "config": {"workload": w["name"], "grid": list(w["voxels"].shape[::-1]),
+                   "image": [cam.width, cam.height], "spp": 1, "shadow_rays": shadow_rays,
+                   "rays_per_frame": rays_per_frame, "l2": "flushed (256 MiB write) between "
+                   "timed frames", "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": e2e,
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": None, "algorithmic_bytes_per_launch": algo_bytes,
+                     "kernel": "vt::render_kernel<false>"},
+        "clocks": clocks,
+        "grid_info": grid.info(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample(w, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    grid.destroy()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

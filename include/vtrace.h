@@ -1,0 +1,263 @@
+/*
+ * vtrace.h — C ABI of libvtrace, a GB300 (sm_103a) voxel ray-traversal engine.
+ *
+ * Two groups of entry points live here:
+ *
+ *  1. The seven symbols vtrace's Rust host binds over FFI (src/render.rs:110-128), with the same
+ *     names, argument meaning and error convention, but headless: there is no window, no Vulkan and
+ *     no swapchain; a frame is one CUDA launch into a device framebuffer.
+ *
+ *  2. New vt_* calls for the traversal hot path: grid creation (brick re-layout), ray-buffer
+ *     tracing, per-pixel rendering with shading and hard shadows, batched multi-view rendering in
+ *     one persistent kernel replayed from a CUDA graph, and a continuous-batching serving loop.
+ *
+ * Conventions
+ *  - vt_* calls return int32 status codes (VT_OK == 0, negative on error); vt_last_error() gives a
+ *    message for the calling thread's most recent failure.
+ *  - Grids are identified by int32 ids >= 0 (like the texture ids add_texture returns).
+ *  - Pointers documented as "device" are CUDA device pointers; "host" pointers are ordinary host
+ *    memory (pinned memory makes the copies asynchronous and faster, but is not required).
+ *  - `stream` parameters are cudaStream_t values passed as void*; NULL selects the library's own
+ *    stream. Calls that take a stream are asynchronous with respect to the host unless stated.
+ *  - Voxel grids are x-fastest: index = x + nx * (y + ny * z), the layout the reference uploads
+ *    with bufferRowLength = 0 (lib/memory.c:353-366).
+ */
+#ifndef VTRACE_H
+#define VTRACE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define VT_OK 0
+#define VT_EINVAL (-1)     /* bad argument (null pointer, zero or oversized dimension, bad id) */
+#define VT_ENOMEM (-2)     /* device or host allocation failed, or an HBM budget is exhausted */
+#define VT_ECUDA (-3)      /* a CUDA runtime call failed; vt_last_error() names it */
+#define VT_ENOTFOUND (-4)  /* unknown grid / batch / request id */
+#define VT_ETIMEDOUT (-5)  /* a bounded wait ran out */
+#define VT_EBUSY (-6)      /* resource still referenced by in-flight work */
+#define VT_ECANCELED (-7)  /* request cancelled or service stopped */
+#define VT_ENOTREADY (-8)  /* request accepted but not finished yet */
+#define VT_ELIMIT (-9)     /* a fixed capacity of this library was exceeded */
+
+/* ---------------------------------------------------------------- records */
+
+/* One traced ray's first hit, 16 bytes (one 128-bit store on the device).
+ *  x, y, z        hit voxel (0xFFFF on a miss)
+ *  palette_index  voxel value of the hit (u8 grids); 0 for RGBA8 grids and misses
+ *  face           bits 0-2: entered face as its outward normal, VT_FACE_*; 0 when the ray starts
+ *                 inside the hit voxel or misses.  Bits 3-7: VT_HIT_FLAG_*.
+ *  t              ray parameter of the entered face plane, (plane - origin[a]) / dir[a]; 0 when the
+ *                 origin lies in the hit voxel; +inf on a miss
+ *  rgba           colour, little-endian R | G<<8 | B<<16 | A<<24: the voxel colour for
+ *                 vt_trace_rays, the shaded colour for vt_render, VT_SKY_RGBA on a render miss */
+typedef struct vt_hit {
+    uint16_t x, y, z;
+    uint8_t palette_index;
+    uint8_t face;
+    float t;
+    uint32_t rgba;
+} vt_hit;
+
+#define VT_FACE_NONE 0
+#define VT_FACE_POS_X 1
+#define VT_FACE_NEG_X 2
+#define VT_FACE_POS_Y 3
+#define VT_FACE_NEG_Y 4
+#define VT_FACE_POS_Z 5
+#define VT_FACE_NEG_Z 6
+#define VT_FACE_MASK 0x07u
+
+#define VT_HIT_FLAG_SHADOW_RAY 0x08u /* a shadow ray was traced for this hit */
+#define VT_HIT_FLAG_INVALID 0x10u    /* non-finite origin or direction: reported as a miss */
+#define VT_HIT_FLAG_SHADOWED 0x20u   /* the shadow ray found an occupied voxel */
+#define VT_HIT_FLAG_TIE 0x40u        /* a DDA step advanced two or three axes at once (edge/corner) */
+#define VT_HIT_FLAG_HIT 0x80u        /* an occupied voxel was found */
+
+/* sRGB encoding of the reference's clear colour (0.53, 0.81, 0.92, 1) (lib/command.c:57-60). */
+#define VT_SKY_RGBA 0xFFF6E8C0u
+
+/* A ray in grid (voxel) coordinates: the grid occupies [0,nx] x [0,ny] x [0,nz]. 24 bytes. */
+typedef struct vt_ray {
+    float origin[3];
+    float dir[3];
+} vt_ray;
+
+/* Pinhole camera in grid coordinates.  For pixel (px, py) with sub-pixel offset (jx, jy) in [0,1)
+ * (0.5 without jitter) the primary ray is origin + t * normalize(forward + sx*right + sy*up) with
+ * sx = (px + jx) * (2/width) - 1 and sy = 1 - (py + jy) * (2/height), evaluated in IEEE binary32
+ * round-to-nearest in exactly that order.  `right` and `up` carry the tan(fov/2) and aspect
+ * scaling; vt_camera_look_at fills them. */
+typedef struct vt_camera {
+    float origin[3];
+    float forward[3];
+    float right[3];
+    float up[3];
+    uint32_t width, height;
+} vt_camera;
+
+/* Directional light for vt_render.  `dir` points from the surface towards the light (unit length).
+ * Shading: k = ambient + (1 - ambient) * max(n.L, 0) * visible, colour = floor(base * k + 0.5). */
+typedef struct vt_light {
+    float dir[3];
+    float ambient;
+    uint32_t shadows; /* nonzero: trace one hard-shadow ray per lit hit */
+} vt_light;
+
+typedef struct vt_grid_info {
+    uint32_t nx, ny, nz;
+    uint32_t bricks_x, bricks_y, bricks_z;
+    uint64_t bricks_total;
+    uint64_t bricks_nonempty;
+    uint64_t voxels_occupied;
+    uint64_t device_bytes; /* directory + masks + payloads + palette */
+    uint32_t payload_format; /* VT_PAYLOAD_* */
+    uint32_t reserved;
+} vt_grid_info;
+
+#define VT_PAYLOAD_U8 1    /* palette index per voxel + 256-entry RGBA8 palette */
+#define VT_PAYLOAD_RGBA8 2 /* RGBA8 texel per voxel (the reference's add_texture format) */
+
+/* Per-launch traversal counters gathered by the counting variant of the kernels. */
+typedef struct vt_trace_stats {
+    uint64_t rays;                /* primary + shadow rays traced */
+    uint64_t shadow_rays;
+    uint64_t hits;                /* primary rays that found an occupied voxel */
+    uint64_t steps;               /* DDA loop iterations over all rays */
+    uint64_t bricks_entered;      /* brick visits (directory lookups) over all rays */
+    uint64_t nonempty_bricks_entered;
+    uint64_t voxels_tested;       /* occupancy-bit tests inside non-empty bricks */
+    uint64_t ties;                /* rays with VT_HIT_FLAG_TIE */
+} vt_trace_stats;
+
+/* ---------------------------------------------------------------- library state */
+
+/* Select the CUDA device and create the library's stream.  Optional: every other call initialises
+ * the library on device 0 when needed.  Returns VT_OK or VT_ECUDA. */
+int32_t vt_init(int32_t device);
+/* Free every grid, batch and buffer and destroy the library's stream. */
+void vt_shutdown(void);
+/* Message for the calling thread's most recent failed call ("" if none). */
+const char* vt_last_error(void);
+/* ABI version: (major << 16) | minor. */
+uint32_t vt_version(void);
+/* Device the library runs on and its SM count; for sizing persistent launches. */
+int32_t vt_device_info(int32_t* device, int32_t* sm_count, uint64_t* free_bytes, uint64_t* total_bytes);
+
+/* ---------------------------------------------------------------- grids */
+
+/* Build a brick grid (8^3 bricks, 512-bit occupancy masks, dense payloads for occupied bricks)
+ * from an x-fastest u8 palette-index grid and a 256-entry RGBA8 palette (both host memory).
+ * A voxel is occupied iff its palette entry's alpha byte is nonzero, the reference's
+ * `texture(...).w > 0.0` rule (shaders/trace.frag:78).  Returns a grid id >= 0 or an error. */
+int32_t vt_grid_create_u8(const uint8_t* voxels, const uint32_t* palette,
+                          uint32_t nx, uint32_t ny, uint32_t nz);
+/* Same, with the voxel array already in device memory (x-fastest, nx*ny*nz bytes); the palette is
+ * host memory.  The build runs on `stream`; the call returns after the build has finished. */
+int32_t vt_grid_create_u8_device(const uint8_t* d_voxels, const uint32_t* palette,
+                                 uint32_t nx, uint32_t ny, uint32_t nz, void* stream);
+/* Build a brick grid from an x-fastest RGBA8 texel array (host), the format of the reference's
+ * add_texture (lib/memory.c:286-385).  Occupied iff alpha > 0. */
+int32_t vt_grid_create_rgba8(const uint8_t* rgba, uint32_t nx, uint32_t ny, uint32_t nz);
+int32_t vt_grid_destroy(int32_t grid);
+int32_t vt_grid_get_info(int32_t grid, vt_grid_info* info);
+/* Copy the grid's brick directory (bricks_total u32, 0xFFFFFFFF = empty brick, else the brick's
+ * slot) and occupancy masks (bricks_nonempty * 64 bytes) to host memory; either may be NULL. */
+int32_t vt_grid_download_bricks(int32_t grid, uint32_t* directory, uint64_t* masks);
+
+/* ---------------------------------------------------------------- tracing */
+
+/* Trace n rays (device array) against a grid; writes n vt_hit records (device).  Hit colour is the
+ * voxel's unshaded RGBA8, miss colour 0.  Asynchronous on `stream`. */
+int32_t vt_trace_rays(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_hit* d_hits, void* stream);
+/* Same through host buffers: copies rays in, traces, copies hits out, and returns when done. */
+int32_t vt_trace_rays_host(int32_t grid, const vt_ray* rays, uint64_t n, vt_hit* hits);
+
+/* Render one image: one primary ray per pixel (pixel centres), first hit, face-normal Lambert
+ * shading and, when light->shadows is set, one hard-shadow ray per lit hit.  light may be NULL
+ * (unshaded voxel colour, no shadow rays).  Writes width*height records, row-major from the top
+ * row (device).  Asynchronous on `stream`. */
+int32_t vt_render(int32_t grid, const vt_camera* camera, const vt_light* light,
+                  vt_hit* d_hits, void* stream);
+/* Same through a host output buffer; returns when the records are in `hits`. */
+int32_t vt_render_host(int32_t grid, const vt_camera* camera, const vt_light* light, vt_hit* hits);
+/* Counting variant of vt_render / vt_trace_rays: same records, plus traversal counters (a slower
+ * kernel build; for roofline accounting, not for timing).  rays == NULL selects the render form. */
+int32_t vt_render_stats(int32_t grid, const vt_camera* camera, const vt_light* light,
+                        vt_hit* d_hits, vt_trace_stats* stats);
+int32_t vt_trace_rays_stats(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_hit* d_hits,
+                            vt_trace_stats* stats);
+
+/* Fill a vt_camera that looks from `eye` at `target` with world-up `up`, vertical field of view
+ * `vfov_degrees`, and the given image size (computed in double, stored as float). */
+int32_t vt_camera_look_at(const float eye[3], const float target[3], const float up[3],
+                          float vfov_degrees, uint32_t width, uint32_t height, vt_camera* out);
+
+/* ---------------------------------------------------------------- scene generators (host) */
+
+/* Seeded synthetic content, deterministic across platforms (integer hashing and IEEE binary32
+ * arithmetic without contraction).  All write x-fastest u8 palette indices (0 = empty). */
+int32_t vt_gen_palette(uint32_t seed, uint32_t* palette256);
+/* fBm-noise heightfield terrain, y up, `octaves` octaves, scaled to `occupancy` (0..1). */
+int32_t vt_gen_terrain(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t seed, uint32_t octaves,
+                       float occupancy, uint8_t* voxels);
+/* `count` random axis-aligned boxes and spheres with radius in [rmin, rmax]. */
+int32_t vt_gen_shapes(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t seed, uint32_t count,
+                      float rmin, float rmax, uint8_t* voxels);
+/* 3D gradient-noise cave: voxel solid where noise > threshold chosen for `occupancy`. */
+int32_t vt_gen_cave(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t seed, float occupancy,
+                    uint8_t* voxels);
+/* n rays with origins uniform inside [0,nx]x[0,ny]x[0,nz] and directions uniform on the sphere. */
+int32_t vt_gen_rays_uniform(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t seed, uint64_t n,
+                            vt_ray* rays);
+
+/* ---------------------------------------------------------------- reference-compatible ABI */
+
+/* render_tick_info of lib/common.h:89-92: pointers to column-major float[16] matrices. */
+typedef struct render_tick_info {
+    void* perspective;
+    void* camera;
+} render_tick_info;
+
+/* user_input of lib/common.h:145-151. */
+typedef struct user_input {
+    uint8_t keys[6];
+    double mouse_x;
+    double mouse_y;
+    double last_mouse_x;
+    double last_mouse_y;
+} user_input;
+
+/* lib/entry.c:54-57.  Initialise the headless renderer: CUDA device, stream and a 1000x1000
+ * RGBA8 framebuffer (VTRACE_WIDTH / VTRACE_HEIGHT override the size).  Returns
+ * ((uint64_t)cudaError << 32) | custom; 0 on success. */
+uint64_t entry(void);
+/* lib/entry.c:150-248.  Render every instance into the framebuffer with the given projection and
+ * camera matrices and write the framebuffer size back.  Returns 0, or -1 on error. */
+int32_t render_tick(int32_t* window_width, int32_t* window_height, const render_tick_info* info);
+/* lib/entry.c:146-148.  There is no window: returns a zeroed, library-owned struct. */
+user_input* get_input_data_pointer(void);
+/* lib/memory.c:286-385.  Upload a width x height x depth RGBA8 texture (x-fastest, caller keeps
+ * ownership) as a brick grid.  Returns the texture id >= 0, or -1. At most 65536 textures. */
+int32_t add_texture(const uint8_t* data, uint32_t width, uint32_t height, uint32_t depth);
+/* lib/memory.c:235-248.  Returns a host buffer for instance_count column-major mat4 instances
+ * (64 B each, texture id stored as the bit pattern of element [3][3]); NULL on failure.
+ * instance_count == 0 is treated as 1. */
+float* start_update_instances(uint32_t instance_count);
+/* lib/memory.c:250-267.  Publish the instances written since start_update_instances; they are
+ * copied to the device at the next render_tick.  Returns 0, or -1. */
+int32_t end_update_instances(uint32_t instance_count);
+/* lib/entry.c:100-144.  Free everything entry() and later calls created. */
+void cleanup(void);
+/* Headless framebuffer readback (no counterpart in the reference, which presents to a window):
+ * copies width*height RGBA8 pixels, row-major from the top row, into `rgba`. */
+int32_t vt_framebuffer_download(uint8_t* rgba, uint64_t capacity_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VTRACE_H */

@@ -1,0 +1,588 @@
+/*
+ * vt_oracle.c — CPU restatement of vtrace's voxel traversal (TEST INFRASTRUCTURE ONLY; see
+ * vt_oracle.h for the semantics and the reference lines each part follows).
+ *
+ * Build with -ffp-contract=off: every float expression below is one IEEE binary32 operation per
+ * operator, evaluated in source order.
+ */
+#define _GNU_SOURCE
+#include "vt_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <unistd.h>
+
+/* GLSL min(x, y) is defined as (y < x) ? y : x (GLSL 4.60 §8.3). */
+static inline float glsl_min(float x, float y) { return (y < x) ? y : x; }
+static inline double glsl_min64(double x, double y) { return (y < x) ? y : x; }
+/* GLSL sign(): 1.0, 0.0 or -1.0. */
+static inline float glsl_sign(float x) { return x > 0.0f ? 1.0f : (x < 0.0f ? -1.0f : 0.0f); }
+
+static inline uint32_t voxel_rgba(const vto_grid* g, int32_t x, int32_t y, int32_t z) {
+    uint64_t i = (uint64_t)x + (uint64_t)g->nx * ((uint64_t)y + (uint64_t)g->ny * (uint64_t)z);
+    if (g->texels) return g->texels[i];
+    return g->palette[g->voxels[i]];
+}
+static inline uint8_t voxel_index(const vto_grid* g, int32_t x, int32_t y, int32_t z) {
+    if (!g->voxels) return 0;
+    uint64_t i = (uint64_t)x + (uint64_t)g->nx * ((uint64_t)y + (uint64_t)g->ny * (uint64_t)z);
+    return g->voxels[i];
+}
+/* shaders/trace.frag:78: texSample.w > 0.0; the alpha byte a gives a/255 > 0 iff a != 0. */
+static inline int voxel_occupied(const vto_grid* g, int32_t x, int32_t y, int32_t z) {
+    return (voxel_rgba(g, x, y, z) >> 24) != 0u;
+}
+
+int vto_grid_prepare(vto_grid* g) {
+    int32_t bx = (g->nx + 7) / 8, by = (g->ny + 7) / 8, bz = (g->nz + 7) / 8;
+    g->brick_nonempty = (uint8_t*)calloc((size_t)bx * by * bz, 1);
+    if (!g->brick_nonempty) return -1;
+    for (int32_t z = 0; z < g->nz; ++z)
+        for (int32_t y = 0; y < g->ny; ++y)
+            for (int32_t x = 0; x < g->nx; ++x)
+                if (voxel_occupied(g, x, y, z))
+                    g->brick_nonempty[(x >> 3) + bx * ((y >> 3) + by * (z >> 3))] = 1;
+    return 0;
+}
+
+void vto_grid_release(vto_grid* g) {
+    free(g->brick_nonempty);
+    g->brick_nonempty = NULL;
+}
+
+/* shaders/trace.frag:68-87, with the brick visit counters of the brick-grid layout. */
+void vto_dda_f32(const vto_grid* g, const float pos[3], const float d[3], vto_dda_out* out,
+                 vto_stats* stats) {
+    const int32_t isize[3] = {g->nx, g->ny, g->nz};
+    const float size[3] = {(float)g->nx, (float)g->ny, (float)g->nz};
+    /* length(): sqrt((x*x + y*y) + z*z) */
+    const float len = sqrtf((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+    int32_t v[3], st[3];
+    float delta[3], side[3];
+    for (int a = 0; a < 3; ++a) {
+        /* trace.frag:68 ivec3(floor(min(model_ray_pos, model_size - 1.0))) */
+        float m = glsl_min(pos[a], size[a] - 1.0f);
+        v[a] = (int32_t)floorf(m);
+        /* trace.frag:69-71 */
+        float sg = glsl_sign(d[a]);
+        st[a] = (int32_t)sg;
+        delta[a] = fabsf(len / d[a]);
+        side[a] = ((sg * ((float)v[a] - pos[a]) + sg * 0.5f) + 0.5f) * delta[a];
+    }
+    const int32_t bxn = (g->nx + 7) / 8, byn = (g->ny + 7) / 8;
+    const uint32_t max_steps = (uint32_t)(g->nx + g->ny + g->nz); /* trace.frag:74 */
+    uint32_t steps = 0;
+    int32_t last = 0, tie = 0, hit = 0;
+    int64_t prev_brick = -1;
+    while (steps < max_steps && v[0] >= 0 && v[1] >= 0 && v[2] >= 0 && v[0] < isize[0] &&
+           v[1] < isize[1] && v[2] < isize[2]) { /* trace.frag:75 */
+        int64_t brick = (int64_t)(v[0] >> 3) + bxn * ((int64_t)(v[1] >> 3) + (int64_t)byn * (v[2] >> 3));
+        int nonempty = g->brick_nonempty ? g->brick_nonempty[brick] : 1;
+        if (stats) {
+            if (brick != prev_brick) {
+                stats->bricks_entered++;
+                if (nonempty) stats->nonempty_bricks_entered++;
+            }
+            if (nonempty) stats->voxels_tested++;
+        }
+        prev_brick = brick;
+        if (nonempty && voxel_occupied(g, v[0], v[1], v[2])) { /* trace.frag:76-80 */
+            hit = 1;
+            break;
+        }
+        /* trace.frag:83-86 */
+        float mnx = glsl_min(side[1], side[2]);
+        float mny = glsl_min(side[2], side[0]);
+        float mnz = glsl_min(side[0], side[1]);
+        int bx = side[0] <= mnx, by = side[1] <= mny, bz = side[2] <= mnz;
+        if (bx) side[0] = side[0] + delta[0];
+        if (by) side[1] = side[1] + delta[1];
+        if (bz) side[2] = side[2] + delta[2];
+        if (bx) v[0] += st[0];
+        if (by) v[1] += st[1];
+        if (bz) v[2] += st[2];
+        last = bx | (by << 1) | (bz << 2);
+        if (bx + by + bz > 1) tie = 1;
+        ++steps;
+    }
+    if (stats) stats->steps += steps;
+    for (int a = 0; a < 3; ++a) {
+        out->v[a] = v[a];
+        out->step[a] = st[a];
+    }
+    out->hit = hit;
+    out->steps = steps;
+    out->last_mask = last;
+    out->tie = tie;
+}
+
+int vto_slab_entry(const vto_grid* g, const float o[3], const float d[3], float pos[3],
+                   float* t_entry, int* entry_axis) {
+    const float size[3] = {(float)g->nx, (float)g->ny, (float)g->nz};
+    float tn = -INFINITY, tf = INFINITY;
+    int ax = -1;
+    for (int a = 0; a < 3; ++a) {
+        if (d[a] == 0.0f) {
+            if (o[a] < 0.0f || o[a] > size[a]) return 0;
+            continue;
+        }
+        float ta = (0.0f - o[a]) / d[a];
+        float tb = (size[a] - o[a]) / d[a];
+        float lo = ta < tb ? ta : tb;
+        float hi = ta < tb ? tb : ta;
+        if (lo > tn) {
+            tn = lo;
+            ax = a;
+        }
+        if (hi < tf) tf = hi;
+    }
+    if (tn > tf || tf < 0.0f) return 0;
+    if (tn <= 0.0f) {
+        pos[0] = o[0];
+        pos[1] = o[1];
+        pos[2] = o[2];
+        *t_entry = 0.0f;
+        *entry_axis = -1;
+        return 2;
+    }
+    for (int b = 0; b < 3; ++b) {
+        float p = o[b] + tn * d[b];
+        p = p < 0.0f ? 0.0f : p;
+        p = p > size[b] ? size[b] : p;
+        pos[b] = p;
+    }
+    pos[ax] = d[ax] > 0.0f ? 0.0f : size[ax];
+    *t_entry = tn;
+    *entry_axis = ax;
+    return 1;
+}
+
+static inline uint8_t face_code(int axis, int normal_positive) {
+    return (uint8_t)(1 + 2 * axis + (normal_positive ? 0 : 1));
+}
+
+static void miss_record(vto_hit* out, uint8_t flags) {
+    out->x = out->y = out->z = 0xFFFF;
+    out->palette_index = 0;
+    out->face = flags;
+    out->t = INFINITY;
+    out->rgba = 0;
+}
+
+static inline int finite3(const float a[3]) {
+    return isfinite(a[0]) && isfinite(a[1]) && isfinite(a[2]);
+}
+
+void vto_trace_ray_f32(const vto_grid* g, const float o[3], const float d[3], vto_hit* out,
+                       vto_stats* stats) {
+    if (stats) stats->rays++;
+    if (!finite3(o) || !finite3(d)) {
+        miss_record(out, VTO_FLAG_INVALID);
+        return;
+    }
+    float pos[3], t_entry;
+    int entry_axis;
+    int kind = vto_slab_entry(g, o, d, pos, &t_entry, &entry_axis);
+    if (kind == 0) {
+        miss_record(out, 0);
+        return;
+    }
+    vto_dda_out r;
+    vto_dda_f32(g, pos, d, &r, stats);
+    uint8_t flags = r.tie ? VTO_FLAG_TIE : 0;
+    if (stats && r.tie) stats->ties++;
+    if (!r.hit) {
+        miss_record(out, flags);
+        return;
+    }
+    uint8_t face = 0;
+    float t = 0.0f;
+    if (r.steps > 0) {
+        int a = (r.last_mask & 1) ? 0 : ((r.last_mask & 2) ? 1 : 2);
+        float plane = (float)(r.step[a] > 0 ? r.v[a] : r.v[a] + 1);
+        t = (plane - o[a]) / d[a];
+        face = face_code(a, r.step[a] < 0);
+    } else if (kind == 1) {
+        int a = entry_axis;
+        t = t_entry;
+        face = face_code(a, d[a] < 0.0f);
+    }
+    out->x = (uint16_t)r.v[0];
+    out->y = (uint16_t)r.v[1];
+    out->z = (uint16_t)r.v[2];
+    out->palette_index = voxel_index(g, r.v[0], r.v[1], r.v[2]);
+    out->face = (uint8_t)(face | flags | VTO_FLAG_HIT);
+    out->t = t;
+    out->rgba = voxel_rgba(g, r.v[0], r.v[1], r.v[2]);
+}
+
+/* The same traversal with the DDA state in binary64; the entry point comes from the binary32 slab
+ * test so that only the recurrence differs. */
+void vto_trace_ray_f64(const vto_grid* g, const float o[3], const float d[3], vto_hit64* out) {
+    memset(out, 0, sizeof(*out));
+    out->t = INFINITY;
+    if (!finite3(o) || !finite3(d)) return;
+    float pos32[3], t_entry;
+    int entry_axis;
+    int kind = vto_slab_entry(g, o, d, pos32, &t_entry, &entry_axis);
+    if (kind == 0) return;
+    const int32_t isize[3] = {g->nx, g->ny, g->nz};
+    const double size[3] = {(double)g->nx, (double)g->ny, (double)g->nz};
+    double dd[3] = {d[0], d[1], d[2]}, pos[3] = {pos32[0], pos32[1], pos32[2]};
+    double len = sqrt((dd[0] * dd[0] + dd[1] * dd[1]) + dd[2] * dd[2]);
+    int32_t v[3], st[3];
+    double delta[3], side[3];
+    for (int a = 0; a < 3; ++a) {
+        double m = glsl_min64(pos[a], size[a] - 1.0);
+        v[a] = (int32_t)floor(m);
+        double sg = dd[a] > 0.0 ? 1.0 : (dd[a] < 0.0 ? -1.0 : 0.0);
+        st[a] = (int32_t)sg;
+        delta[a] = fabs(len / dd[a]);
+        side[a] = ((sg * ((double)v[a] - pos[a]) + sg * 0.5) + 0.5) * delta[a];
+    }
+    uint32_t max_steps = (uint32_t)(g->nx + g->ny + g->nz), steps = 0;
+    int last = 0, tie = 0, hit = 0;
+    while (steps < max_steps && v[0] >= 0 && v[1] >= 0 && v[2] >= 0 && v[0] < isize[0] &&
+           v[1] < isize[1] && v[2] < isize[2]) {
+        if (voxel_occupied(g, v[0], v[1], v[2])) {
+            hit = 1;
+            break;
+        }
+        double mnx = glsl_min64(side[1], side[2]);
+        double mny = glsl_min64(side[2], side[0]);
+        double mnz = glsl_min64(side[0], side[1]);
+        int bx = side[0] <= mnx, by = side[1] <= mny, bz = side[2] <= mnz;
+        if (bx) side[0] = side[0] + delta[0];
+        if (by) side[1] = side[1] + delta[1];
+        if (bz) side[2] = side[2] + delta[2];
+        if (bx) v[0] += st[0];
+        if (by) v[1] += st[1];
+        if (bz) v[2] += st[2];
+        last = bx | (by << 1) | (bz << 2);
+        if (bx + by + bz > 1) tie = 1;
+        ++steps;
+    }
+    out->tie = tie;
+    if (!hit) return;
+    out->hit = 1;
+    out->v[0] = v[0];
+    out->v[1] = v[1];
+    out->v[2] = v[2];
+    if (steps > 0) {
+        int a = (last & 1) ? 0 : ((last & 2) ? 1 : 2);
+        double plane = (double)(st[a] > 0 ? v[a] : v[a] + 1);
+        out->t = (plane - (double)o[a]) / dd[a];
+        out->face = face_code(a, st[a] < 0);
+    } else if (kind == 1) {
+        int a = entry_axis;
+        double plane = d[a] > 0.0f ? 0.0 : size[a];
+        out->t = (plane - (double)o[a]) / dd[a];
+        out->face = face_code(a, d[a] < 0.0f);
+    } else {
+        out->t = 0.0;
+        out->face = 0;
+    }
+}
+
+void vto_trace_entry_points(const vto_grid* g, uint64_t n, const float* mp, const float* s,
+                            int32_t* out) {
+    const float size[3] = {(float)g->nx, (float)g->ny, (float)g->nz};
+    for (uint64_t i = 0; i < n; ++i) {
+        const float* v = s + 3 * i;
+        const float len = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+        float d[3], pos[3];
+        for (int a = 0; a < 3; ++a) {
+            d[a] = v[a] / len;
+            pos[a] = (mp[3 * i + a] + 0.5f) * size[a];
+        }
+        vto_dda_out r;
+        vto_dda_f32(g, pos, d, &r, NULL);
+        int32_t* o = out + 5 * i;
+        o[0] = r.hit;
+        o[1] = r.v[0];
+        o[2] = r.v[1];
+        o[3] = r.v[2];
+        o[4] = (int32_t)(r.steps + (r.hit ? 1u : 0u));
+    }
+}
+
+void vto_raygen(const vto_camera* c, uint32_t px, uint32_t py, float jx, float jy, float o[3],
+                float d[3]) {
+    const float inv_w2 = 2.0f / (float)c->width;
+    const float inv_h2 = 2.0f / (float)c->height;
+    const float fx = (float)px + jx;
+    const float fy = (float)py + jy;
+    const float sx = fx * inv_w2 - 1.0f;
+    const float sy = 1.0f - fy * inv_h2;
+    float r[3];
+    for (int a = 0; a < 3; ++a) r[a] = (c->forward[a] + sx * c->right[a]) + sy * c->up[a];
+    const float len = sqrtf((r[0] * r[0] + r[1] * r[1]) + r[2] * r[2]);
+    for (int a = 0; a < 3; ++a) {
+        d[a] = r[a] / len;
+        o[a] = c->origin[a];
+    }
+}
+
+static inline void mulhilo32(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo) {
+    uint64_t p = (uint64_t)a * (uint64_t)b;
+    *hi = (uint32_t)(p >> 32);
+    *lo = (uint32_t)p;
+}
+
+void vto_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0, lo0, hi1, lo1;
+        mulhilo32(0xD2511F53u, c0, &hi0, &lo0);
+        mulhilo32(0xCD9E8D57u, c2, &hi1, &lo1);
+        uint32_t n0 = hi1 ^ c1 ^ k0, n1 = lo1, n2 = hi0 ^ c3 ^ k1, n3 = lo0;
+        c0 = n0;
+        c1 = n1;
+        c2 = n2;
+        c3 = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+void vto_jitter(uint32_t seed, uint32_t view, uint32_t px, uint32_t py, uint32_t s, float* jx,
+                float* jy) {
+    const uint32_t ctr[4] = {px, py, s, view};
+    const uint32_t key[2] = {seed, 0x56544752u};
+    uint32_t r[4];
+    vto_philox4x32_10(ctr, key, r);
+    *jx = (float)(r[0] >> 8) * 0x1p-24f;
+    *jy = (float)(r[1] >> 8) * 0x1p-24f;
+}
+
+static void shade_from_ray(const vto_grid* g, const vto_light* light, const float o[3],
+                           const float d[3], vto_hit* out, vto_stats* stats) {
+    vto_trace_ray_f32(g, o, d, out, stats);
+    if (!(out->face & VTO_FLAG_HIT)) {
+        out->rgba = VTO_SKY_RGBA;
+        return;
+    }
+    if (stats) stats->hits++;
+    if (!light) return;
+    const int face = out->face & 7;
+    if (face == 0) return; /* origin inside the hit voxel: no normal, colour unshaded */
+    const int a = (face - 1) / 2;
+    const int npos = (face & 1) != 0;
+    const float ndl = npos ? light->dir[a] : -light->dir[a];
+    float vis = 1.0f;
+    if (ndl > 0.0f && light->shadows) {
+        const int32_t hv[3] = {out->x, out->y, out->z};
+        const float plane = (float)(npos ? hv[a] + 1 : hv[a]);
+        float so[3];
+        for (int b = 0; b < 3; ++b) so[b] = o[b] + out->t * d[b];
+        so[a] = npos ? plane + 0.015625f : plane - 0.015625f;
+        vto_hit sh;
+        vto_trace_ray_f32(g, so, light->dir, &sh, stats);
+        if (stats) stats->shadow_rays++;
+        out->face |= VTO_FLAG_SHADOW_RAY;
+        if (sh.face & VTO_FLAG_HIT) {
+            vis = 0.0f;
+            out->face |= VTO_FLAG_SHADOWED;
+        }
+    }
+    const float lam = ndl > 0.0f ? ndl : 0.0f;
+    const float k = light->ambient + (1.0f - light->ambient) * (lam * vis);
+    uint32_t base = out->rgba, res = base & 0xFF000000u;
+    for (int c = 0; c < 3; ++c) {
+        float v = (float)((base >> (8 * c)) & 0xFFu) * k + 0.5f;
+        uint32_t q = v >= 255.0f ? 255u : (v <= 0.0f ? 0u : (uint32_t)v);
+        res |= q << (8 * c);
+    }
+    out->rgba = res;
+}
+
+void vto_shade_sample(const vto_grid* g, const vto_camera* cam, const vto_light* light,
+                      uint32_t px, uint32_t py, float jx, float jy, vto_hit* out,
+                      vto_stats* stats) {
+    float o[3], d[3];
+    vto_raygen(cam, px, py, jx, jy, o, d);
+    shade_from_ray(g, light, o, d, out, stats);
+}
+
+/* ------------------------------------------------------------------ threading */
+
+int vto_hardware_threads(void) {
+    long n = sysconf(_SC_NPROCESSORS_ONLN);
+    return n > 0 ? (int)n : 1;
+}
+
+typedef struct job {
+    int kind; /* 0 render rows, 1 rays f32, 2 rays f64, 3 view */
+    const vto_grid* g;
+    const vto_camera* cam;
+    const vto_light* light;
+    const float* rays;
+    vto_hit* hits;
+    vto_hit64* hits64;
+    uint32_t spp, seed, view;
+    uint64_t begin, end; /* pixels (kind 0/3) or rays */
+    uint32_t row_offset;
+    vto_stats stats;
+    int want_stats;
+} job;
+
+static void* run_job(void* arg) {
+    job* j = (job*)arg;
+    vto_stats* st = j->want_stats ? &j->stats : NULL;
+    if (j->kind == 0) { /* begin/end: pixel indices y * width + x */
+        const uint32_t w = j->cam->width;
+        for (uint64_t p = j->begin; p < j->end; ++p) {
+            const uint32_t y = (uint32_t)(p / w), x = (uint32_t)(p % w);
+            vto_shade_sample(j->g, j->cam, j->light, x, y, 0.5f, 0.5f,
+                             &j->hits[p - (uint64_t)j->row_offset * w], st);
+        }
+    } else if (j->kind == 1) {
+        for (uint64_t i = j->begin; i < j->end; ++i) {
+            const float* r = j->rays + 6 * i;
+            vto_trace_ray_f32(j->g, r, r + 3, &j->hits[i], st);
+        }
+    } else if (j->kind == 2) {
+        for (uint64_t i = j->begin; i < j->end; ++i) {
+            const float* r = j->rays + 6 * i;
+            vto_trace_ray_f64(j->g, r, r + 3, &j->hits64[i]);
+        }
+    } else { /* begin/end: pixel indices */
+        const uint32_t w = j->cam->width;
+        for (uint64_t p = j->begin; p < j->end; ++p) {
+            const uint32_t y = (uint32_t)(p / w), x = (uint32_t)(p % w);
+            for (uint32_t s = 0; s < j->spp; ++s) {
+                float jx, jy;
+                vto_jitter(j->seed, j->view, x, y, s, &jx, &jy);
+                vto_shade_sample(j->g, j->cam, j->light, x, y, jx, jy, &j->hits[p * j->spp + s],
+                                 st);
+            }
+        }
+    }
+    return NULL;
+}
+
+typedef struct lane {
+    job* jobs;
+    uint64_t n, first, stride;
+} lane;
+
+static void* lane_main(void* arg) {
+    lane* l = (lane*)arg;
+    for (uint64_t c = l->first; c < l->n; c += l->stride) run_job(&l->jobs[c]);
+    return NULL;
+}
+
+/* Splits [begin, end) into chunks of ~1/16 of a thread's share, handed out round-robin. */
+static void run_parallel(job* proto, uint64_t begin, uint64_t end, int threads, vto_stats* stats) {
+    if (end <= begin) return;
+    if (threads <= 0) threads = vto_hardware_threads();
+    if ((uint64_t)threads > end - begin) threads = (int)(end - begin);
+    if (threads < 1) threads = 1;
+    const uint64_t total = end - begin;
+    uint64_t chunk = total / ((uint64_t)threads * 16);
+    if (chunk == 0) chunk = 1;
+    const uint64_t nchunks = (total + chunk - 1) / chunk;
+    job* jobs = (job*)calloc((size_t)nchunks, sizeof(job));
+    pthread_t* tids = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
+    lane* lanes = (lane*)calloc((size_t)threads, sizeof(lane));
+    for (uint64_t c = 0; c < nchunks; ++c) {
+        jobs[c] = *proto;
+        memset(&jobs[c].stats, 0, sizeof(vto_stats));
+        jobs[c].begin = begin + c * chunk;
+        jobs[c].end = jobs[c].begin + chunk < end ? jobs[c].begin + chunk : end;
+    }
+    for (int t = 0; t < threads; ++t) {
+        lanes[t].jobs = jobs;
+        lanes[t].n = nchunks;
+        lanes[t].first = (uint64_t)t;
+        lanes[t].stride = (uint64_t)threads;
+    }
+    if (threads == 1) {
+        lane_main(&lanes[0]);
+    } else {
+        for (int t = 0; t < threads; ++t) pthread_create(&tids[t], NULL, lane_main, &lanes[t]);
+        for (int t = 0; t < threads; ++t) pthread_join(tids[t], NULL);
+    }
+    if (stats) {
+        for (uint64_t c = 0; c < nchunks; ++c) {
+            const vto_stats* s = &jobs[c].stats;
+            stats->rays += s->rays;
+            stats->shadow_rays += s->shadow_rays;
+            stats->hits += s->hits;
+            stats->steps += s->steps;
+            stats->bricks_entered += s->bricks_entered;
+            stats->nonempty_bricks_entered += s->nonempty_bricks_entered;
+            stats->voxels_tested += s->voxels_tested;
+            stats->ties += s->ties;
+        }
+    }
+    free(lanes);
+    free(tids);
+    free(jobs);
+}
+
+void vto_render_rows(const vto_grid* g, const vto_camera* cam, const vto_light* light,
+                     uint32_t row0, uint32_t row1, vto_hit* hits, int threads, vto_stats* stats) {
+    job p;
+    memset(&p, 0, sizeof(p));
+    p.kind = 0;
+    p.g = g;
+    p.cam = cam;
+    p.light = light;
+    p.hits = hits;
+    p.row_offset = row0;
+    p.want_stats = stats != NULL;
+    run_parallel(&p, (uint64_t)row0 * cam->width, (uint64_t)row1 * cam->width, threads, stats);
+}
+
+void vto_render(const vto_grid* g, const vto_camera* cam, const vto_light* light, vto_hit* hits,
+                int threads, vto_stats* stats) {
+    vto_render_rows(g, cam, light, 0, cam->height, hits, threads, stats);
+}
+
+void vto_render_view(const vto_grid* g, const vto_camera* cam, const vto_light* light,
+                     uint32_t spp, uint32_t seed, uint32_t view, vto_hit* hits, int threads,
+                     vto_stats* stats) {
+    job p;
+    memset(&p, 0, sizeof(p));
+    p.kind = 3;
+    p.g = g;
+    p.cam = cam;
+    p.light = light;
+    p.hits = hits;
+    p.spp = spp;
+    p.seed = seed;
+    p.view = view;
+    p.want_stats = stats != NULL;
+    run_parallel(&p, 0, (uint64_t)cam->height * cam->width, threads, stats);
+}
+
+void vto_trace_rays(const vto_grid* g, const float* rays, uint64_t n, vto_hit* hits, int threads,
+                    vto_stats* stats) {
+    job p;
+    memset(&p, 0, sizeof(p));
+    p.kind = 1;
+    p.g = g;
+    p.rays = rays;
+    p.hits = hits;
+    p.want_stats = stats != NULL;
+    run_parallel(&p, 0, n, threads, stats);
+}
+
+void vto_trace_rays_f64(const vto_grid* g, const float* rays, uint64_t n, vto_hit64* hits,
+                        int threads) {
+    job p;
+    memset(&p, 0, sizeof(p));
+    p.kind = 2;
+    p.g = g;
+    p.rays = rays;
+    p.hits64 = hits;
+    run_parallel(&p, 0, n, threads, NULL);
+}

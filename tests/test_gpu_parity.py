@@ -1,0 +1,274 @@
+"""GPU parity: libvtrace's CUDA kernels against the CPU oracle, bit-exact on every field of the
+hit records (voxel, palette index, face, flags, t, colour), through the C ABI."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import vtrace_gb300 as vt
+from vtrace_gb300 import workloads
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    assert t.cuda.is_available()
+    vt.init(0)
+    return t
+
+
+def to_dev(torch, arr):
+    a = np.ascontiguousarray(arr)
+    return torch.from_numpy(a.view(np.uint8).reshape(-1)).cuda()
+
+
+def hits_from_dev(buf):
+    return buf.cpu().numpy().view(vt.HIT_DTYPE)
+
+
+def assert_hits_equal(got, want, what=""):
+    g = np.ascontiguousarray(got).view(np.uint8).reshape(-1, 16)
+    w = np.ascontiguousarray(want).view(np.uint8).reshape(-1, 16)
+    bad = np.nonzero((g != w).any(1))[0]
+    if len(bad):
+        i = bad[0]
+        raise AssertionError("%s: %d of %d records differ; first at %d: got %r want %r" % (
+            what, len(bad), len(g), i, got.reshape(-1)[i], want.reshape(-1)[i]))
+
+
+def oracle_camera(cam):
+    return po.make_camera(cam.as_dict())
+
+
+def oracle_light(L):
+    return None if L is None else po.make_light(list(L.dir), L.ambient, bool(L.shadows))
+
+
+def device_trace(torch, grid, rays):
+    n = rays.shape[0]
+    d_rays = to_dev(torch, rays.astype(np.float32))
+    d_hits = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    vt.trace_rays(grid, d_rays, n, d_hits)
+    torch.cuda.synchronize()
+    vt.check(vt.lib().vt_init(0))
+    return hits_from_dev(d_hits), d_rays, d_hits
+
+
+def device_render(torch, grid, cam, light):
+    d_hits = torch.empty(cam.width * cam.height * 16, dtype=torch.uint8, device="cuda")
+    vt.render(grid, cam, light, d_hits, torch.cuda.current_stream())
+    torch.cuda.synchronize()
+    return hits_from_dev(d_hits).reshape(cam.height, cam.width), d_hits
+
+
+# ------------------------------------------------------------------ golden fixtures
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_golden_fixtures(torch, path):
+    z = np.load(path)
+    g = vt.Grid.from_u8(z["voxels"], z["palette"])
+    try:
+        hits, _, _ = device_trace(torch, g, z["rays"])
+        want = z["ray_hits"].reshape(-1).view(vt.HIT_DTYPE)
+        assert_hits_equal(hits, want, "ray-buffer form")
+        cam = vt.Camera()
+        cam.origin[:] = z["cam_origin"].tolist()
+        cam.forward[:] = z["cam_forward"].tolist()
+        cam.right[:] = z["cam_right"].tolist()
+        cam.up[:] = z["cam_up"].tolist()
+        cam.width, cam.height = (int(v) for v in z["cam_size"])
+        L = z["light"]
+        light = vt.Light()
+        light.dir[:] = L[:3].tolist()
+        light.ambient, light.shadows = float(L[3]), int(L[4])
+        img, _ = device_render(torch, g, cam, light)
+        assert_hits_equal(img, z["render_hits"].reshape(-1).view(vt.HIT_DTYPE), "render form")
+    finally:
+        g.destroy()
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_rgba8_grid_matches_oracle(torch, path):
+    z = np.load(path)
+    texels = z["palette"][z["voxels"]]
+    g = vt.Grid.from_rgba8(texels)
+    try:
+        hits, _, _ = device_trace(torch, g, z["rays"])
+        want = po.trace_rays(po.Grid(texels=texels), z["rays"], threads=4)
+        assert_hits_equal(hits, want, "rgba8 grid")
+    finally:
+        g.destroy()
+
+
+def expected_bricks(vox, pal):
+    nz, ny, nx = vox.shape
+    occ = (pal[vox] >> 24) != 0
+    bx, by, bz = (nx + 7) // 8, (ny + 7) // 8, (nz + 7) // 8
+    pad = np.zeros((bz * 8, by * 8, bx * 8), bool)
+    pad[:nz, :ny, :nx] = occ
+    # [bz, lz, by, ly, bx, lx] -> [bz, by, bx, lz, ly, lx]
+    b = pad.reshape(bz, 8, by, 8, bx, 8).transpose(0, 2, 4, 1, 3, 5)
+    bits = b.reshape(bz * by * bx, 8, 64)
+    words = (bits.astype(np.uint64) << np.arange(64, dtype=np.uint64)).sum(axis=2, dtype=np.uint64)
+    nonempty = bits.any(axis=(1, 2))
+    slots = np.cumsum(nonempty) - 1
+    directory = np.where(nonempty, slots, 0xFFFFFFFF).astype(np.uint32)
+    return directory, words[nonempty], int(occ.sum())
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 16), (13, 21, 9), (64, 8, 40)])
+def test_brick_layout(torch, shape):
+    rng = np.random.default_rng(sum(shape))
+    nz, ny, nx = shape[2], shape[1], shape[0]
+    vox = np.where(rng.random((nz, ny, nx)) < 0.02, rng.integers(1, 256, (nz, ny, nx)), 0).astype(np.uint8)
+    pal = vt.gen_palette(4)
+    pal[5] &= 0x00FFFFFF
+    g = vt.Grid.from_u8(vox, pal)
+    try:
+        d, m = g.bricks()
+        wd, wm, occ = expected_bricks(vox, pal)
+        np.testing.assert_array_equal(d, wd)
+        np.testing.assert_array_equal(m, wm)
+        info = g.info()
+        assert info["voxels_occupied"] == occ
+        assert info["bricks_nonempty"] == len(wm)
+    finally:
+        g.destroy()
+
+
+# ------------------------------------------------------------------ benchmark configurations
+
+def test_terrain256_full_frame_and_counters(torch):
+    w = workloads.terrain256()
+    g = vt.Grid.from_u8(w["voxels"], w["palette"])
+    try:
+        cam, light = w["camera"], w["light"]
+        img, d_hits = device_render(torch, g, cam, light)
+        og = po.Grid(w["voxels"], w["palette"])
+        want, ostats = po.render(og, oracle_camera(cam), oracle_light(light), stats=True)
+        assert_hits_equal(img, want, "terrain256 640x480")
+        assert (img["face"] & vt.FLAG_HIT).astype(bool).mean() > 0.5
+        gstats = vt.render_stats(g, cam, light, d_hits)
+        assert gstats == ostats
+        img2 = hits_from_dev(d_hits).reshape(cam.height, cam.width)
+        assert_hits_equal(img2, want, "counting kernel output")
+        # the host-buffer form returns the same image
+        assert_hits_equal(vt.render_host(g, cam, light), want, "vt_render_host")
+        # unshaded form
+        img3, _ = device_render(torch, g, cam, None)
+        assert_hits_equal(img3, po.render(og, oracle_camera(cam), None), "unlit render")
+    finally:
+        g.destroy()
+
+
+@pytest.fixture(scope="module")
+def shapes(torch):
+    w = workloads.shapes1024()
+    g = vt.Grid.from_u8(w["voxels"], w["palette"])
+    yield w, g
+    g.destroy()
+
+
+def test_shapes1024_1080p_band_parity(torch, shapes):
+    w, g = shapes
+    cam, light = w["camera"], w["light"]
+    img, _ = device_render(torch, g, cam, light)
+    og = po.Grid(w["voxels"], w["palette"])
+    r0, r1 = 516, 564
+    want = po.render(og, oracle_camera(cam), oracle_light(light), rows=(r0, r1))
+    assert_hits_equal(img[r0:r1], want, "shapes1024 rows %d-%d" % (r0, r1))
+    # every hit voxel of the full frame is occupied in the dense grid
+    hit = (img["face"] & vt.FLAG_HIT) != 0
+    v = w["voxels"][img["z"][hit], img["y"][hit], img["x"][hit]]
+    assert (v != 0).all() and ((w["palette"][v] >> 24) != 0).all()
+    assert hit.mean() > 0.3
+    shadow = (img["face"] & vt.FLAG_SHADOW_RAY) != 0
+    assert shadow.sum() > 0 and not (shadow & ~hit).any()
+
+
+def test_shapes1024_trace_rays_sample_with_t_accuracy(torch, shapes):
+    w, g = shapes
+    n = 1 << 20
+    rays = vt.gen_rays_uniform(1024, 77, n)
+    hits, d_rays, d_hits = device_trace(torch, g, rays)
+    og = po.Grid(w["voxels"], w["palette"])
+    want = po.trace_rays(og, rays)
+    assert_hits_equal(hits, want, "shapes1024 1M rays")
+    # t against the binary64 DDA: within 1e-5 relative where both find the same voxel and face
+    h64 = po.trace_rays_f64(og, rays)
+    hit32 = (hits["face"] & vt.FLAG_HIT) != 0
+    same = hit32 & (h64["hit"] == 1) & (hits["x"] == h64["v"][:, 0]) & \
+        (hits["y"] == h64["v"][:, 1]) & (hits["z"] == h64["v"][:, 2]) & \
+        ((hits["face"] & 7) == h64["face"])
+    t32 = hits["t"][same].astype(np.float64)
+    t64 = h64["t"][same]
+    rel = np.abs(t32 - t64) / np.maximum(np.abs(t64), 1e-30)
+    assert rel.max() <= 1e-5, rel.max()
+    diverged = (hit32 != (h64["hit"] == 1)) | (hit32 & ~same)
+    # divergent rays are the binary32 recurrence resolving a near-tie differently
+    assert diverged.mean() < 1e-2
+
+
+def test_cave512_trace_rays_parity(torch):
+    w = workloads.cave512(rays=1 << 20)
+    g = vt.Grid.from_u8(w["voxels"], w["palette"])
+    try:
+        hits, d_rays, d_hits = device_trace(torch, g, w["rays"])
+        og = po.Grid(w["voxels"], w["palette"])
+        want, ostats = po.trace_rays(og, w["rays"], stats=True)
+        assert_hits_equal(hits, want, "cave512 1M rays")
+        gstats = vt.trace_rays_stats(g, d_rays, w["rays"].shape[0], d_hits)
+        assert gstats == ostats
+        assert_hits_equal(vt.trace_rays_host(g, w["rays"][:4096]), want[:4096], "host form")
+    finally:
+        g.destroy()
+
+
+def test_device_grid_upload_matches_host_upload(torch):
+    w = workloads.terrain256(n=128, width=64, height=48)
+    d_vox = to_dev(torch, w["voxels"])
+    g1 = vt.Grid.from_u8_device(d_vox, (128, 128, 128), w["palette"],
+                                torch.cuda.current_stream())
+    g2 = vt.Grid.from_u8(w["voxels"], w["palette"])
+    try:
+        a, b = g1.bricks(), g2.bricks()
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[1], b[1])
+        assert g1.info() == g2.info()
+    finally:
+        g1.destroy()
+        g2.destroy()
+
+
+def test_repeat_launches_are_identical(torch):
+    w = workloads.terrain256(n=128, width=160, height=120)
+    g = vt.Grid.from_u8(w["voxels"], w["palette"])
+    try:
+        a, _ = device_render(torch, g, w["camera"], w["light"])
+        b, _ = device_render(torch, g, w["camera"], w["light"])
+        assert_hits_equal(a, b, "repeat")
+    finally:
+        g.destroy()
+
+
+def test_errors_are_reported_not_fatal(torch):
+    with pytest.raises(vt.VtError) as e:
+        vt.render(vt.Grid(999999), workloads.terrain256(n=16, width=4, height=4)["camera"],
+                  None, 0)
+    assert e.value.code == -4
+    g = vt.Grid.from_u8(np.zeros((8, 8, 8), np.uint8), vt.gen_palette(1))
+    try:
+        buf = torch.empty(64, dtype=torch.uint8, device="cuda")
+        with pytest.raises(vt.VtError):
+            vt.trace_rays(g, buf.data_ptr() + 4, 1, buf)  # misaligned rays
+        # an empty grid: everything misses
+        hits = vt.trace_rays_host(g, np.array([[4, 4, -5, 0, 0, 1]], np.float32))
+        assert not hits["face"][0] & vt.FLAG_HIT
+    finally:
+        g.destroy()

@@ -1,0 +1,343 @@
+"""vtrace_gb300 — GB300-native voxel ray traversal behind vtrace's C ABI.
+
+Python host-side mirror of ``include/vtrace.h``: thin ctypes bindings over ``libvtrace.so``
+(CUDA kernels for sm_103a).  There is no CPU fallback: every call goes to the CUDA library, and
+loading fails loudly when the library is missing or cannot be built.
+
+Device buffers are passed as raw pointers (ints) or objects with ``data_ptr()`` (e.g. torch CUDA
+tensors); streams as raw ``cudaStream_t`` values (ints, e.g. ``torch.cuda.current_stream()
+.cuda_stream``) or None for the library's own stream.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+HIT_DTYPE = np.dtype([("x", "<u2"), ("y", "<u2"), ("z", "<u2"), ("palette_index", "u1"),
+                      ("face", "u1"), ("t", "<f4"), ("rgba", "<u4")])
+RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("dir", "<f4", 3)])
+
+VT_OK = 0
+ERRORS = {-1: "EINVAL", -2: "ENOMEM", -3: "ECUDA", -4: "ENOTFOUND", -5: "ETIMEDOUT",
+          -6: "EBUSY", -7: "ECANCELED", -8: "ENOTREADY", -9: "ELIMIT"}
+FACE_MASK = 0x07
+FLAG_SHADOW_RAY = 0x08
+FLAG_INVALID = 0x10
+FLAG_SHADOWED = 0x20
+FLAG_TIE = 0x40
+FLAG_HIT = 0x80
+SKY_RGBA = 0xFFF6E8C0
+PAYLOAD_U8 = 1
+PAYLOAD_RGBA8 = 2
+
+
+class VtError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "ERROR"), code, message))
+        self.code = code
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_float * 3), ("forward", ctypes.c_float * 3),
+                ("right", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {"origin": list(self.origin), "forward": list(self.forward),
+                "right": list(self.right), "up": list(self.up), "width": self.width,
+                "height": self.height}
+
+
+class Light(ctypes.Structure):
+    _fields_ = [("dir", ctypes.c_float * 3), ("ambient", ctypes.c_float),
+                ("shadows", ctypes.c_uint32)]
+
+
+class GridInfo(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_uint32), ("ny", ctypes.c_uint32), ("nz", ctypes.c_uint32),
+                ("bricks_x", ctypes.c_uint32), ("bricks_y", ctypes.c_uint32),
+                ("bricks_z", ctypes.c_uint32), ("bricks_total", ctypes.c_uint64),
+                ("bricks_nonempty", ctypes.c_uint64), ("voxels_occupied", ctypes.c_uint64),
+                ("device_bytes", ctypes.c_uint64), ("payload_format", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+class TraceStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "rays", "shadow_rays", "hits", "steps", "bricks_entered", "nonempty_bricks_entered",
+        "voxels_tested", "ties")]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+class RenderTickInfo(ctypes.Structure):
+    _fields_ = [("perspective", ctypes.c_void_p), ("camera", ctypes.c_void_p)]
+
+
+class UserInput(ctypes.Structure):
+    _fields_ = [("keys", ctypes.c_uint8 * 6), ("mouse_x", ctypes.c_double),
+                ("mouse_y", ctypes.c_double), ("last_mouse_x", ctypes.c_double),
+                ("last_mouse_y", ctypes.c_double)]
+
+
+_lib = None
+
+# (name, restype, argtypes) of every symbol include/vtrace.h declares
+_vp, _i32, _u32, _u64, _f32 = (ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint32, ctypes.c_uint64,
+                               ctypes.c_float)
+SIGNATURES = [
+    ("vt_init", _i32, [_i32]),
+    ("vt_shutdown", None, []),
+    ("vt_last_error", ctypes.c_char_p, []),
+    ("vt_version", _u32, []),
+    ("vt_device_info", _i32, [_vp, _vp, _vp, _vp]),
+    ("vt_grid_create_u8", _i32, [_vp, _vp, _u32, _u32, _u32]),
+    ("vt_grid_create_u8_device", _i32, [_vp, _vp, _u32, _u32, _u32, _vp]),
+    ("vt_grid_create_rgba8", _i32, [_vp, _u32, _u32, _u32]),
+    ("vt_grid_destroy", _i32, [_i32]),
+    ("vt_grid_get_info", _i32, [_i32, ctypes.POINTER(GridInfo)]),
+    ("vt_grid_download_bricks", _i32, [_i32, _vp, _vp]),
+    ("vt_trace_rays", _i32, [_i32, _vp, _u64, _vp, _vp]),
+    ("vt_trace_rays_host", _i32, [_i32, _vp, _u64, _vp]),
+    ("vt_render", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp, _vp]),
+    ("vt_render_host", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp]),
+    ("vt_render_stats", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp,
+                               ctypes.POINTER(TraceStats)]),
+    ("vt_trace_rays_stats", _i32, [_i32, _vp, _u64, _vp, ctypes.POINTER(TraceStats)]),
+    ("vt_camera_look_at", _i32, [_vp, _vp, _vp, _f32, _u32, _u32, ctypes.POINTER(Camera)]),
+    ("vt_gen_palette", _i32, [_u32, _vp]),
+    ("vt_gen_terrain", _i32, [_u32, _u32, _u32, _u32, _u32, _f32, _vp]),
+    ("vt_gen_shapes", _i32, [_u32, _u32, _u32, _u32, _u32, _f32, _f32, _vp]),
+    ("vt_gen_cave", _i32, [_u32, _u32, _u32, _u32, _f32, _vp]),
+    ("vt_gen_rays_uniform", _i32, [_u32, _u32, _u32, _u32, _u64, _vp]),
+    ("entry", _u64, []),
+    ("render_tick", _i32, [_vp, _vp, ctypes.POINTER(RenderTickInfo)]),
+    ("get_input_data_pointer", ctypes.POINTER(UserInput), []),
+    ("add_texture", _i32, [_vp, _u32, _u32, _u32]),
+    ("start_update_instances", ctypes.POINTER(ctypes.c_float), [_u32]),
+    ("end_update_instances", _i32, [_u32]),
+    ("cleanup", None, []),
+    ("vt_framebuffer_download", _i32, [_vp, _u64]),
+]
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib():
+    """The loaded libvtrace.so, built in-tree first if needed.  Raises if it cannot be had."""
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError("libvtrace.so was not built")
+        L = ctypes.CDLL(path)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error():
+    return lib().vt_last_error().decode()
+
+
+def check(rc):
+    if rc < 0:
+        raise VtError(rc, last_error())
+    return rc
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    raise TypeError("expected a pointer, an ndarray or a tensor, got %r" % type(x))
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return s.cuda_stream
+
+
+def init(device=0):
+    check(lib().vt_init(device))
+
+
+def device_info():
+    d, sm = ctypes.c_int32(), ctypes.c_int32()
+    f, t = ctypes.c_uint64(), ctypes.c_uint64()
+    check(lib().vt_device_info(ctypes.byref(d), ctypes.byref(sm), ctypes.byref(f),
+                               ctypes.byref(t)))
+    return {"device": d.value, "sm_count": sm.value, "free_bytes": f.value,
+            "total_bytes": t.value}
+
+
+# ---------------------------------------------------------------- content
+
+def gen_palette(seed):
+    pal = np.zeros(256, np.uint32)
+    check(lib().vt_gen_palette(seed, pal.ctypes.data))
+    return pal
+
+
+def gen_terrain(n, seed, octaves=5, occupancy=0.3):
+    nx, ny, nz = (n, n, n) if isinstance(n, int) else n
+    v = np.empty((nz, ny, nx), np.uint8)
+    check(lib().vt_gen_terrain(nx, ny, nz, seed, octaves, occupancy, v.ctypes.data))
+    return v
+
+
+def gen_shapes(n, seed, count=10000, rmin=2.0, rmax=40.0):
+    nx, ny, nz = (n, n, n) if isinstance(n, int) else n
+    v = np.empty((nz, ny, nx), np.uint8)
+    check(lib().vt_gen_shapes(nx, ny, nz, seed, count, rmin, rmax, v.ctypes.data))
+    return v
+
+
+def gen_cave(n, seed, occupancy=0.45):
+    nx, ny, nz = (n, n, n) if isinstance(n, int) else n
+    v = np.empty((nz, ny, nx), np.uint8)
+    check(lib().vt_gen_cave(nx, ny, nz, seed, occupancy, v.ctypes.data))
+    return v
+
+
+def gen_rays_uniform(n_grid, seed, count):
+    nx, ny, nz = (n_grid, n_grid, n_grid) if isinstance(n_grid, int) else n_grid
+    r = np.empty((count, 6), np.float32)
+    check(lib().vt_gen_rays_uniform(nx, ny, nz, seed, count, r.ctypes.data))
+    return r
+
+
+def camera_look_at(eye, target, up=(0.0, 1.0, 0.0), vfov_degrees=60.0, width=640,
+                   height=480):
+    c = Camera()
+    e = (ctypes.c_float * 3)(*eye)
+    t = (ctypes.c_float * 3)(*target)
+    u = (ctypes.c_float * 3)(*up)
+    check(lib().vt_camera_look_at(e, t, u, vfov_degrees, width, height, ctypes.byref(c)))
+    return c
+
+
+def make_light(direction, ambient=0.25, shadows=True):
+    d = np.asarray(direction, np.float64)
+    d = d / np.linalg.norm(d)
+    L = Light()
+    L.dir[:] = [float(np.float32(x)) for x in d]
+    L.ambient = ambient
+    L.shadows = 1 if shadows else 0
+    return L
+
+
+# ---------------------------------------------------------------- grids
+
+class Grid:
+    """A brick grid resident on the device (ids are the library's grid ids)."""
+
+    def __init__(self, gid):
+        self.id = gid
+
+    @classmethod
+    def from_u8(cls, voxels, palette):
+        voxels = np.ascontiguousarray(voxels, np.uint8)
+        palette = np.ascontiguousarray(palette, np.uint32)
+        if palette.shape != (256,):
+            raise ValueError("palette must hold 256 RGBA8 entries")
+        nz, ny, nx = voxels.shape
+        return cls(check(lib().vt_grid_create_u8(voxels.ctypes.data, palette.ctypes.data,
+                                                 nx, ny, nz)))
+
+    @classmethod
+    def from_u8_device(cls, d_voxels, dims, palette, stream=None):
+        nx, ny, nz = dims
+        palette = np.ascontiguousarray(palette, np.uint32)
+        return cls(check(lib().vt_grid_create_u8_device(_ptr(d_voxels), palette.ctypes.data,
+                                                        nx, ny, nz, _stream(stream))))
+
+    @classmethod
+    def from_rgba8(cls, rgba):
+        """rgba: uint8 [z, y, x, 4] or uint32 [z, y, x] texels."""
+        a = np.ascontiguousarray(rgba)
+        if a.dtype == np.uint32:
+            nz, ny, nx = a.shape
+        else:
+            a = a.astype(np.uint8, copy=False)
+            nz, ny, nx, _ = a.shape
+        return cls(check(lib().vt_grid_create_rgba8(a.ctypes.data, nx, ny, nz)))
+
+    def info(self):
+        gi = GridInfo()
+        check(lib().vt_grid_get_info(self.id, ctypes.byref(gi)))
+        return gi.as_dict()
+
+    def bricks(self):
+        inf = self.info()
+        d = np.zeros(inf["bricks_total"], np.uint32)
+        m = np.zeros(max(1, inf["bricks_nonempty"]) * 8, np.uint64)
+        check(lib().vt_grid_download_bricks(self.id, d.ctypes.data, m.ctypes.data))
+        return d, m[: inf["bricks_nonempty"] * 8].reshape(-1, 8)
+
+    def destroy(self):
+        if self.id is not None and self.id >= 0:
+            check(lib().vt_grid_destroy(self.id))
+            self.id = None
+
+
+# ---------------------------------------------------------------- tracing
+
+def trace_rays(grid, d_rays, n, d_hits, stream=None):
+    """Asynchronous: n rays (device, 24 B each) -> n hit records (device, 16 B each)."""
+    check(lib().vt_trace_rays(grid.id, _ptr(d_rays), n, _ptr(d_hits), _stream(stream)))
+
+
+def trace_rays_host(grid, rays):
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    hits = np.zeros(rays.shape[0], HIT_DTYPE)
+    check(lib().vt_trace_rays_host(grid.id, rays.ctypes.data, rays.shape[0], hits.ctypes.data))
+    return hits
+
+
+def trace_rays_stats(grid, d_rays, n, d_hits):
+    st = TraceStats()
+    check(lib().vt_trace_rays_stats(grid.id, _ptr(d_rays), n, _ptr(d_hits), ctypes.byref(st)))
+    return st.as_dict()
+
+
+def render(grid, camera, light, d_hits, stream=None):
+    """Asynchronous: camera.width*camera.height records into d_hits (device)."""
+    check(lib().vt_render(grid.id, ctypes.byref(camera),
+                          ctypes.byref(light) if light is not None else None, _ptr(d_hits),
+                          _stream(stream)))
+
+
+def render_host(grid, camera, light=None, out=None):
+    hits = out if out is not None else np.zeros(camera.height * camera.width, HIT_DTYPE)
+    check(lib().vt_render_host(grid.id, ctypes.byref(camera),
+                               ctypes.byref(light) if light is not None else None,
+                               _ptr(hits)))
+    return hits.reshape(camera.height, camera.width) if out is None else hits
+
+
+def render_stats(grid, camera, light, d_hits):
+    st = TraceStats()
+    check(lib().vt_render_stats(grid.id, ctypes.byref(camera),
+                                ctypes.byref(light) if light is not None else None,
+                                _ptr(d_hits), ctypes.byref(st)))
+    return st.as_dict()

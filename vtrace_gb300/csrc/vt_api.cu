@@ -1,0 +1,507 @@
+// vt_api.cu — C ABI of libvtrace: library state, grid table, tracing and rendering calls.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "vt_api_internal.h"
+#include "vt_device.cuh"
+#include "vt_internal.h"
+#include "vt_kernels.h"
+
+namespace vt {
+
+static thread_local std::string g_last_error;
+
+int32_t fail(int32_t code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+void clear_error() { g_last_error.clear(); }
+
+int32_t cuda_fail(cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fail(VT_ECUDA, m);
+}
+
+State& state() {
+    static State s;
+    return s;
+}
+
+int32_t ensure_init_locked(int32_t device) {
+    State& s = state();
+    if (s.inited) return VT_OK;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+    e = cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+    s.device = device;
+    s.inited = true;
+    return VT_OK;
+}
+
+int32_t ensure_init() {
+    State& s = state();
+    std::lock_guard<std::mutex> lk(s.mu);
+    return ensure_init_locked(0);
+}
+
+cudaStream_t pick_stream(void* stream) {
+    return stream ? (cudaStream_t)stream : state().stream;
+}
+
+GridView Grid::view() const {
+    GridView v;
+    v.dir = dir;
+    v.masks = masks;
+    v.payload8 = format == VT_PAYLOAD_U8 ? (const uint8_t*)payload : nullptr;
+    v.payload32 = format == VT_PAYLOAD_RGBA8 ? (const uint32_t*)payload : nullptr;
+    v.palette = palette;
+    v.nx = (int32_t)nx;
+    v.ny = (int32_t)ny;
+    v.nz = (int32_t)nz;
+    v.bx = (int32_t)bx;
+    v.by = (int32_t)by;
+    v.bz = (int32_t)bz;
+    v.max_steps = nx + ny + nz;
+    v.format = format;
+    return v;
+}
+
+void Grid::release() {
+    cudaFree(dir);
+    cudaFree(masks);
+    cudaFree(payload);
+    cudaFree(palette);
+    dir = nullptr;
+    masks = nullptr;
+    payload = nullptr;
+    palette = nullptr;
+}
+
+int32_t check_dims(uint32_t nx, uint32_t ny, uint32_t nz) {
+    if (nx == 0 || ny == 0 || nz == 0)
+        return fail(VT_EINVAL, "grid dimensions must be nonzero");
+    if (nx > kMaxDim || ny > kMaxDim || nz > kMaxDim)
+        return fail(VT_EINVAL, "grid dimension above 65535 (hit records hold 16-bit coordinates)");
+    const uint64_t bricks = (uint64_t)((nx + 7) / 8) * ((ny + 7) / 8) * ((nz + 7) / 8);
+    if (bricks > 0xFFFFFFF0ull) return fail(VT_EINVAL, "grid has more than 2^32 bricks");
+    return VT_OK;
+}
+
+// Builds the brick layout of a dense device grid on `stream` and waits for it.
+int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_host,
+                   uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,
+                   std::unique_ptr<Grid>& out) {
+    std::unique_ptr<Grid> g(new Grid());
+    g->nx = nx;
+    g->ny = ny;
+    g->nz = nz;
+    g->bx = (nx + 7) / 8;
+    g->by = (ny + 7) / 8;
+    g->bz = (nz + 7) / 8;
+    g->bricks = (uint64_t)g->bx * g->by * g->bz;
+    g->format = format;
+    cudaError_t e;
+    if (format == VT_PAYLOAD_U8) {
+        e = cudaMalloc(&g->palette, 256 * sizeof(uint32_t));
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(palette)");
+        e = cudaMemcpyAsync(g->palette, palette_host, 256 * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, stream);
+        if (e != cudaSuccess) {
+            g->release();
+            return cuda_fail(e, "cudaMemcpy(palette)");
+        }
+    }
+    void* scratch = nullptr;
+    const size_t sbytes = build_scratch_bytes(g->bricks);
+    e = cudaMalloc(&scratch, sbytes);
+    if (e != cudaSuccess) {
+        g->release();
+        cudaGetLastError();
+        return fail(VT_ENOMEM, "cudaMalloc(brick build scratch) failed");
+    }
+    BuildScratch s = carve_build_scratch(scratch, g->bricks);
+    int32_t rc = VT_OK;
+    uint32_t last_off = 0, last_flag = 0;
+    unsigned long long occ = 0;
+    do {
+        e = launch_brick_words(d_src, format, g->palette, (int32_t)nx, (int32_t)ny, (int32_t)nz, s,
+                               stream);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "brick words kernel"); break; }
+        e = launch_brick_scan(s, g->bricks, stream);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "brick scan kernel"); break; }
+        e = cudaMemcpyAsync(&last_off, s.offsets + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&last_flag, s.flags + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&occ, s.occupied, 8, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "brick count readback"); break; }
+        g->nonempty = (uint64_t)last_off + last_flag;
+        g->occupied = occ;
+        const uint64_t slots = g->nonempty ? g->nonempty : 1;
+        const size_t psize = format == VT_PAYLOAD_U8 ? 512 : 2048;
+        if (cudaMalloc(&g->dir, g->bricks * 4) != cudaSuccess ||
+            cudaMalloc(&g->masks, slots * 64) != cudaSuccess ||
+            cudaMalloc(&g->payload, slots * psize) != cudaSuccess) {
+            cudaGetLastError();
+            rc = fail(VT_ENOMEM, "cudaMalloc(brick grid) failed");
+            break;
+        }
+        e = launch_brick_compact(d_src, format, (int32_t)nx, (int32_t)ny, (int32_t)nz, s, g->dir,
+                                 g->masks, g->payload, stream);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "brick compact kernel"); break; }
+        e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "brick build"); break; }
+        g->bytes = g->bricks * 4 + slots * 64 + slots * psize + (g->palette ? 1024 : 0);
+    } while (0);
+    cudaFree(scratch);
+    if (rc != VT_OK) {
+        g->release();
+        return rc;
+    }
+    out = std::move(g);
+    return VT_OK;
+}
+
+int32_t register_grid(std::unique_ptr<Grid> g) {
+    State& s = state();
+    std::lock_guard<std::mutex> lk(s.mu);
+    for (size_t i = 0; i < s.grids.size(); ++i)
+        if (!s.grids[i]) {
+            s.grids[i] = std::move(g);
+            return (int32_t)i;
+        }
+    if (s.grids.size() >= kMaxGrids) {
+        g->release();
+        return fail(VT_ELIMIT, "too many grids");
+    }
+    s.grids.push_back(std::move(g));
+    return (int32_t)(s.grids.size() - 1);
+}
+
+Grid* lookup_grid(int32_t id) {
+    State& s = state();
+    std::lock_guard<std::mutex> lk(s.mu);
+    if (id < 0 || (size_t)id >= s.grids.size() || !s.grids[id]) return nullptr;
+    return s.grids[id].get();
+}
+
+LightView light_view(const vt_light* light) {
+    LightView L;
+    memset(&L, 0, sizeof(L));
+    if (light) {
+        L.dx = light->dir[0];
+        L.dy = light->dir[1];
+        L.dz = light->dir[2];
+        L.ambient = light->ambient;
+        L.enabled = 1;
+        L.shadows = light->shadows ? 1u : 0u;
+    }
+    return L;
+}
+
+int32_t check_camera(const vt_camera* cam) {
+    if (!cam) return fail(VT_EINVAL, "null camera");
+    if (cam->width == 0 || cam->height == 0 || cam->width > 65536 || cam->height > 65536)
+        return fail(VT_EINVAL, "camera size must be in 1..65536");
+    return VT_OK;
+}
+
+// Device staging for the *_host calls (grown on demand, guarded by State::host_mu).
+int32_t staging(size_t bytes, void** out) {
+    State& s = state();
+    if (s.staging_bytes < bytes) {
+        cudaFree(s.staging);
+        s.staging = nullptr;
+        s.staging_bytes = 0;
+        if (cudaMalloc(&s.staging, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(VT_ENOMEM, "cudaMalloc(staging) failed");
+        }
+        s.staging_bytes = bytes;
+    }
+    *out = s.staging;
+    return VT_OK;
+}
+
+static void stats_from(const Counters& c, vt_trace_stats* st) {
+    st->rays = c.rays;
+    st->shadow_rays = c.shadow_rays;
+    st->hits = c.hits;
+    st->steps = c.steps;
+    st->bricks_entered = c.bricks;
+    st->nonempty_bricks_entered = c.nonempty;
+    st->voxels_tested = c.tested;
+    st->ties = c.ties;
+}
+
+}  // namespace vt
+
+using namespace vt;
+
+extern "C" {
+
+int32_t vt_init(int32_t device) {
+    State& s = state();
+    std::lock_guard<std::mutex> lk(s.mu);
+    if (s.inited) {
+        if (s.device != device) return fail(VT_EINVAL, "vt_init: already initialised on another device");
+        return VT_OK;
+    }
+    return ensure_init_locked(device);
+}
+
+void vt_shutdown(void) {
+    vt_compat_release();
+    vt_batch_release_all();
+    State& s = state();
+    std::lock_guard<std::mutex> lk(s.mu);
+    if (!s.inited) return;
+    cudaStreamSynchronize(s.stream);
+    for (auto& g : s.grids)
+        if (g) g->release();
+    s.grids.clear();
+    cudaFree(s.staging);
+    s.staging = nullptr;
+    s.staging_bytes = 0;
+    cudaStreamDestroy(s.stream);
+    s.stream = nullptr;
+    s.inited = false;
+}
+
+const char* vt_last_error(void) { return g_last_error.c_str(); }
+
+uint32_t vt_version(void) { return (1u << 16) | 0u; }
+
+int32_t vt_device_info(int32_t* device, int32_t* sm_count, uint64_t* free_bytes,
+                       uint64_t* total_bytes) {
+    int32_t rc = ensure_init();
+    if (rc) return rc;
+    State& s = state();
+    if (device) *device = s.device;
+    if (sm_count) *sm_count = s.sm_count;
+    size_t f = 0, t = 0;
+    cudaError_t e = cudaMemGetInfo(&f, &t);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemGetInfo");
+    if (free_bytes) *free_bytes = f;
+    if (total_bytes) *total_bytes = t;
+    return VT_OK;
+}
+
+int32_t vt_grid_create_u8_device(const uint8_t* d_voxels, const uint32_t* palette, uint32_t nx,
+                                 uint32_t ny, uint32_t nz, void* stream) {
+    if (!d_voxels || !palette) return fail(VT_EINVAL, "vt_grid_create_u8_device: null pointer");
+    int32_t rc = check_dims(nx, ny, nz);
+    if (rc) return rc;
+    if ((rc = ensure_init())) return rc;
+    std::unique_ptr<Grid> g;
+    rc = build_grid(d_voxels, VT_PAYLOAD_U8, palette, nx, ny, nz, pick_stream(stream), g);
+    if (rc) return rc;
+    return register_grid(std::move(g));
+}
+
+static int32_t create_from_host(const void* data, size_t elem, uint32_t format,
+                                const uint32_t* palette, uint32_t nx, uint32_t ny, uint32_t nz) {
+    int32_t rc = check_dims(nx, ny, nz);
+    if (rc) return rc;
+    if ((rc = ensure_init())) return rc;
+    const size_t bytes = (size_t)nx * ny * nz * elem;
+    void* d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(VT_ENOMEM, "cudaMalloc(dense grid upload) failed");
+    }
+    cudaStream_t st = state().stream;
+    cudaError_t e = cudaMemcpyAsync(d, data, bytes, cudaMemcpyHostToDevice, st);
+    std::unique_ptr<Grid> g;
+    if (e != cudaSuccess)
+        rc = cuda_fail(e, "cudaMemcpy(dense grid)");
+    else
+        rc = build_grid(d, format, palette, nx, ny, nz, st, g);
+    cudaStreamSynchronize(st);
+    cudaFree(d);
+    if (rc) return rc;
+    return register_grid(std::move(g));
+}
+
+int32_t vt_grid_create_u8(const uint8_t* voxels, const uint32_t* palette, uint32_t nx,
+                          uint32_t ny, uint32_t nz) {
+    if (!voxels || !palette) return fail(VT_EINVAL, "vt_grid_create_u8: null pointer");
+    return create_from_host(voxels, 1, VT_PAYLOAD_U8, palette, nx, ny, nz);
+}
+
+int32_t vt_grid_create_rgba8(const uint8_t* rgba, uint32_t nx, uint32_t ny, uint32_t nz) {
+    if (!rgba) return fail(VT_EINVAL, "vt_grid_create_rgba8: null pointer");
+    return create_from_host(rgba, 4, VT_PAYLOAD_RGBA8, nullptr, nx, ny, nz);
+}
+
+int32_t vt_grid_destroy(int32_t grid) {
+    State& s = state();
+    std::lock_guard<std::mutex> lk(s.mu);
+    if (grid < 0 || (size_t)grid >= s.grids.size() || !s.grids[grid])
+        return fail(VT_ENOTFOUND, "vt_grid_destroy: unknown grid");
+    if (s.grids[grid]->refs.load() > 0) return fail(VT_EBUSY, "vt_grid_destroy: grid in use");
+    cudaStreamSynchronize(s.stream);
+    s.grids[grid]->release();
+    s.grids[grid].reset();
+    return VT_OK;
+}
+
+int32_t vt_grid_get_info(int32_t grid, vt_grid_info* info) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_grid_get_info: unknown grid");
+    if (!info) return fail(VT_EINVAL, "vt_grid_get_info: null info");
+    info->nx = g->nx;
+    info->ny = g->ny;
+    info->nz = g->nz;
+    info->bricks_x = g->bx;
+    info->bricks_y = g->by;
+    info->bricks_z = g->bz;
+    info->bricks_total = g->bricks;
+    info->bricks_nonempty = g->nonempty;
+    info->voxels_occupied = g->occupied;
+    info->device_bytes = g->bytes;
+    info->payload_format = g->format;
+    info->reserved = 0;
+    return VT_OK;
+}
+
+int32_t vt_grid_download_bricks(int32_t grid, uint32_t* directory, uint64_t* masks) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_grid_download_bricks: unknown grid");
+    cudaStream_t st = state().stream;
+    cudaError_t e = cudaSuccess;
+    if (directory) e = cudaMemcpyAsync(directory, g->dir, g->bricks * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && masks && g->nonempty)
+        e = cudaMemcpyAsync(masks, g->masks, g->nonempty * 64, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_grid_download_bricks");
+    return VT_OK;
+}
+
+int32_t vt_trace_rays(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_hit* d_hits,
+                      void* stream) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_trace_rays: unknown grid");
+    if (n && (!d_rays || !d_hits)) return fail(VT_EINVAL, "vt_trace_rays: null buffer");
+    if (((uintptr_t)d_rays & 7u) || ((uintptr_t)d_hits & 15u))
+        return fail(VT_EINVAL, "vt_trace_rays: rays must be 8-byte and hits 16-byte aligned");
+    cudaError_t e = launch_trace_rays(g->view(), d_rays, n, (uint4*)d_hits, nullptr, pick_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "vt_trace_rays launch");
+    return VT_OK;
+}
+
+int32_t vt_trace_rays_stats(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_hit* d_hits,
+                            vt_trace_stats* stats) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_trace_rays_stats: unknown grid");
+    if (!stats || (n && (!d_rays || !d_hits))) return fail(VT_EINVAL, "vt_trace_rays_stats: null pointer");
+    if (((uintptr_t)d_rays & 7u) || ((uintptr_t)d_hits & 15u))
+        return fail(VT_EINVAL, "vt_trace_rays_stats: misaligned buffer");
+    Counters* dc = nullptr;
+    cudaStream_t st = state().stream;
+    if (cudaMalloc(&dc, sizeof(Counters)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(VT_ENOMEM, "cudaMalloc(counters)");
+    }
+    Counters hc;
+    cudaError_t e = cudaMemsetAsync(dc, 0, sizeof(Counters), st);
+    if (e == cudaSuccess) e = launch_trace_rays(g->view(), d_rays, n, (uint4*)d_hits, dc, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dc);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_trace_rays_stats");
+    stats_from(hc, stats);
+    return VT_OK;
+}
+
+int32_t vt_trace_rays_host(int32_t grid, const vt_ray* rays, uint64_t n, vt_hit* hits) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_trace_rays_host: unknown grid");
+    if (n == 0) return VT_OK;
+    if (!rays || !hits) return fail(VT_EINVAL, "vt_trace_rays_host: null buffer");
+    State& s = state();
+    std::lock_guard<std::mutex> lk(s.host_mu);
+    const size_t rb = (size_t)n * sizeof(vt_ray), hb = (size_t)n * sizeof(vt_hit);
+    const size_t roff = (hb + 255) / 256 * 256;
+    void* buf;
+    int32_t rc = staging(roff + rb, &buf);
+    if (rc) return rc;
+    vt_hit* dh = (vt_hit*)buf;
+    vt_ray* dr = (vt_ray*)((char*)buf + roff);
+    cudaStream_t st = s.stream;
+    cudaError_t e = cudaMemcpyAsync(dr, rays, rb, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_trace_rays(g->view(), dr, n, (uint4*)dh, nullptr, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hits, dh, hb, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_trace_rays_host");
+    return VT_OK;
+}
+
+int32_t vt_render(int32_t grid, const vt_camera* camera, const vt_light* light, vt_hit* d_hits,
+                  void* stream) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_render: unknown grid");
+    int32_t rc = check_camera(camera);
+    if (rc) return rc;
+    if (!d_hits || ((uintptr_t)d_hits & 15u)) return fail(VT_EINVAL, "vt_render: hits must be 16-byte aligned");
+    cudaError_t e = launch_render(g->view(), *camera, light_view(light), (uint4*)d_hits, nullptr,
+                                  pick_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "vt_render launch");
+    return VT_OK;
+}
+
+int32_t vt_render_stats(int32_t grid, const vt_camera* camera, const vt_light* light,
+                        vt_hit* d_hits, vt_trace_stats* stats) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_render_stats: unknown grid");
+    int32_t rc = check_camera(camera);
+    if (rc) return rc;
+    if (!stats || !d_hits || ((uintptr_t)d_hits & 15u)) return fail(VT_EINVAL, "vt_render_stats: bad buffer");
+    Counters* dc = nullptr;
+    cudaStream_t st = state().stream;
+    if (cudaMalloc(&dc, sizeof(Counters)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(VT_ENOMEM, "cudaMalloc(counters)");
+    }
+    Counters hc;
+    cudaError_t e = cudaMemsetAsync(dc, 0, sizeof(Counters), st);
+    if (e == cudaSuccess) e = launch_render(g->view(), *camera, light_view(light), (uint4*)d_hits, dc, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dc);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_render_stats");
+    stats_from(hc, stats);
+    return VT_OK;
+}
+
+int32_t vt_render_host(int32_t grid, const vt_camera* camera, const vt_light* light,
+                       vt_hit* hits) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_render_host: unknown grid");
+    int32_t rc = check_camera(camera);
+    if (rc) return rc;
+    if (!hits) return fail(VT_EINVAL, "vt_render_host: null output");
+    State& s = state();
+    std::lock_guard<std::mutex> lk(s.host_mu);
+    const size_t hb = (size_t)camera->width * camera->height * sizeof(vt_hit);
+    void* buf;
+    if ((rc = staging(hb, &buf))) return rc;
+    cudaStream_t st = s.stream;
+    cudaError_t e = launch_render(g->view(), *camera, light_view(light), (uint4*)buf, nullptr, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hits, buf, hb, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_render_host");
+    return VT_OK;
+}
+
+}  // extern "C"

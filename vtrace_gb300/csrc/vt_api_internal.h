@@ -1,0 +1,67 @@
+// vt_api_internal.h — library state shared by the C ABI translation units (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "vtrace.h"
+
+namespace vt {
+
+struct GridView;
+struct LightView;
+
+constexpr uint32_t kMaxDim = 65535;
+constexpr size_t kMaxGrids = 1u << 20;
+
+// A brick grid resident in device memory.
+struct Grid {
+    uint32_t nx = 0, ny = 0, nz = 0, bx = 0, by = 0, bz = 0;
+    uint64_t bricks = 0, nonempty = 0, occupied = 0;
+    uint32_t format = VT_PAYLOAD_U8;
+    uint32_t* dir = nullptr;
+    uint64_t* masks = nullptr;
+    void* payload = nullptr;
+    uint32_t* palette = nullptr;
+    size_t bytes = 0;
+    std::atomic<int32_t> refs{0};  // in-flight batches / serving requests using the grid
+    GridView view() const;
+    void release();
+};
+
+struct State {
+    std::mutex mu;       // grid table and initialisation
+    std::mutex host_mu;  // staging buffer of the *_host calls
+    bool inited = false;
+    int32_t device = 0;
+    int32_t sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<std::unique_ptr<Grid>> grids;
+    void* staging = nullptr;
+    size_t staging_bytes = 0;
+};
+
+State& state();
+int32_t ensure_init();
+int32_t cuda_fail(cudaError_t e, const char* what);
+cudaStream_t pick_stream(void* stream);
+Grid* lookup_grid(int32_t id);
+int32_t register_grid(std::unique_ptr<Grid> g);
+int32_t check_dims(uint32_t nx, uint32_t ny, uint32_t nz);
+int32_t check_camera(const vt_camera* cam);
+LightView light_view(const vt_light* light);
+int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_host,
+                   uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,
+                   std::unique_ptr<Grid>& out);
+
+}  // namespace vt
+
+// Release hooks of the other subsystems, called by vt_shutdown.
+void vt_compat_release();
+void vt_batch_release_all();

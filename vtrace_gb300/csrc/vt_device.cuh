@@ -1,0 +1,485 @@
+// vt_device.cuh — device-side traversal of libvtrace (sm_103a).
+//
+// The arithmetic restates vtrace's fragment shader (shaders/trace.frag:68-87) operation for
+// operation in IEEE binary32 round-to-nearest, written with explicit __f*_rn intrinsics so that no
+// multiply-add is ever contracted.  The grid is read through the brick layout built by
+// vt_grid.cu:
+//   dir[brick]            u32 slot of an occupied 8^3 brick, kEmptyBrick otherwise
+//                         (brick = bx + BX * (by + BY * bz), x fastest)
+//   masks[slot * 8 + lz]  u64 occupancy of z-slice lz, bit (ly * 8 + lx)
+//   payload[slot*512+li]  voxel value at li = lx + 8 * (ly + 8 * lz) (u8 index or RGBA8)
+// A voxel is occupied iff its colour's alpha byte is nonzero (trace.frag:78).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <limits.h>
+#include <stdint.h>
+
+#include "vtrace.h"
+
+namespace vt {
+
+constexpr uint32_t kEmptyBrick = 0xFFFFFFFFu;
+
+struct GridView {
+    const uint32_t* dir;
+    const uint64_t* masks;
+    const uint8_t* payload8;    // VT_PAYLOAD_U8
+    const uint32_t* payload32;  // VT_PAYLOAD_RGBA8
+    const uint32_t* palette;    // 256 entries (VT_PAYLOAD_U8)
+    int32_t nx, ny, nz;
+    int32_t bx, by, bz;
+    uint32_t max_steps;  // nx + ny + nz (trace.frag:74)
+    uint32_t format;
+};
+
+struct LightView {
+    float dx, dy, dz;
+    float ambient;
+    uint32_t enabled;
+    uint32_t shadows;
+};
+
+// Traversal counters of the counting kernels (vt_trace_stats).
+struct Counters {
+    unsigned long long rays, shadow_rays, hits, steps, bricks, nonempty, tested, ties;
+};
+
+template <bool STATS>
+struct Tally {
+    __device__ __forceinline__ void rays() {}
+    __device__ __forceinline__ void shadow() {}
+    __device__ __forceinline__ void hit() {}
+    __device__ __forceinline__ void steps(uint32_t) {}
+    __device__ __forceinline__ void brick() {}
+    __device__ __forceinline__ void nonempty() {}
+    __device__ __forceinline__ void tested() {}
+    __device__ __forceinline__ void tie() {}
+    __device__ __forceinline__ void flush(Counters*) {}
+};
+
+template <>
+struct Tally<true> {
+    Counters c = {0, 0, 0, 0, 0, 0, 0, 0};
+    __device__ __forceinline__ void rays() { c.rays++; }
+    __device__ __forceinline__ void shadow() { c.shadow_rays++; }
+    __device__ __forceinline__ void hit() { c.hits++; }
+    __device__ __forceinline__ void steps(uint32_t n) { c.steps += n; }
+    __device__ __forceinline__ void brick() { c.bricks++; }
+    __device__ __forceinline__ void nonempty() { c.nonempty++; }
+    __device__ __forceinline__ void tested() { c.tested++; }
+    __device__ __forceinline__ void tie() { c.ties++; }
+    __device__ __forceinline__ void flush(Counters* g) {
+        atomicAdd(&g->rays, c.rays);
+        atomicAdd(&g->shadow_rays, c.shadow_rays);
+        atomicAdd(&g->hits, c.hits);
+        atomicAdd(&g->steps, c.steps);
+        atomicAdd(&g->bricks, c.bricks);
+        atomicAdd(&g->nonempty, c.nonempty);
+        atomicAdd(&g->tested, c.tested);
+        atomicAdd(&g->ties, c.ties);
+    }
+};
+
+// GLSL min(x, y) := (y < x) ? y : x (GLSL 4.60 section 8.3).
+__device__ __forceinline__ float glsl_min(float x, float y) { return (y < x) ? y : x; }
+__device__ __forceinline__ float glsl_sign(float x) {
+    return x > 0.f ? 1.f : (x < 0.f ? -1.f : 0.f);
+}
+
+// trace.frag:68-71 for one axis.
+__device__ __forceinline__ void dda_setup_axis(float p, float d, int32_t n, float len, int32_t& v,
+                                               int32_t& st, float& delta, float& side) {
+    const float m = glsl_min(p, __fsub_rn(__int2float_rn(n), 1.0f));
+    v = (int32_t)floorf(m);
+    const float sg = glsl_sign(d);
+    st = (int32_t)sg;
+    delta = fabsf(__fdiv_rn(len, d));
+    side = __fmul_rn(
+        __fadd_rn(__fadd_rn(__fmul_rn(sg, __fsub_rn(__int2float_rn(v), p)), __fmul_rn(sg, 0.5f)),
+                  0.5f),
+        delta);
+}
+
+struct DDAResult {
+    int32_t vx, vy, vz;
+    uint32_t steps;
+    uint32_t slot;  // brick slot of the final voxel when hit
+    int32_t last;   // axes stepped on the final iteration (bit 0 = x)
+    bool hit;
+    bool tie;
+};
+
+__device__ __forceinline__ bool grid_inside(const GridView& g, int32_t x, int32_t y, int32_t z) {
+    return (uint32_t)x < (uint32_t)g.nx && (uint32_t)y < (uint32_t)g.ny &&
+           (uint32_t)z < (uint32_t)g.nz;
+}
+
+// The literal loop of trace.frag:73-87, used when a side distance is NaN (degenerate
+// directions: zero length, or a component so small that len/d overflows while the side term is
+// zero).  GLSL min semantics are kept exactly; the step counter bounds the loop.
+template <bool STATS>
+__device__ __forceinline__ void dda_literal(const GridView& g, int32_t vx, int32_t vy, int32_t vz,
+                                         int32_t stx, int32_t sty, int32_t stz, float dlx,
+                                         float dly, float dlz, float sx, float sy, float sz,
+                                         DDAResult& r, Tally<STATS>& tl) {
+    uint32_t steps = 0, slot = kEmptyBrick;
+    int32_t last = 0;
+    bool tie = false, hit = false;
+    long long prev = -1;
+    while (steps < g.max_steps && grid_inside(g, vx, vy, vz)) {
+        const long long brick =
+            (long long)(vx >> 3) + (long long)g.bx * ((vy >> 3) + (long long)g.by * (vz >> 3));
+        slot = __ldg(g.dir + brick);
+        if (brick != prev) {
+            tl.brick();
+            if (slot != kEmptyBrick) tl.nonempty();
+        }
+        prev = brick;
+        if (slot != kEmptyBrick) {
+            tl.tested();
+            const uint64_t w = __ldg(g.masks + (size_t)slot * 8 + (vz & 7));
+            if ((w >> (((vy & 7) << 3) | (vx & 7))) & 1ull) {
+                hit = true;
+                break;
+            }
+        }
+        const float mnx = glsl_min(sy, sz), mny = glsl_min(sz, sx), mnz = glsl_min(sx, sy);
+        const bool mx = sx <= mnx, my = sy <= mny, mz = sz <= mnz;
+        if (mx) sx = __fadd_rn(sx, dlx);
+        if (my) sy = __fadd_rn(sy, dly);
+        if (mz) sz = __fadd_rn(sz, dlz);
+        if (mx) vx += stx;
+        if (my) vy += sty;
+        if (mz) vz += stz;
+        last = (mx ? 1 : 0) | (my ? 2 : 0) | (mz ? 4 : 0);
+        if ((int)mx + (int)my + (int)mz > 1) tie = true;
+        ++steps;
+    }
+    tl.steps(steps);
+    r.vx = vx;
+    r.vy = vy;
+    r.vz = vz;
+    r.steps = steps;
+    r.slot = slot;
+    r.last = last;
+    r.hit = hit;
+    r.tie = tie;
+}
+
+// The reference DDA (trace.frag:68-87) from grid-space point (px,py,pz) along (dx,dy,dz).
+//
+// Same voxel sequence, step count and hit as the literal loop; the work is organised by brick:
+// one directory load per brick visited, no memory access at all while crossing an empty brick,
+// and one 64-bit mask-word load (L1-resident) per voxel inside an occupied brick.  When no side
+// distance is NaN every iteration advances at least one axis, so each axis leaves its brick
+// within 8 steps; the trace.frag:74 step bound is still checked on every iteration.
+template <bool STATS>
+__device__ __forceinline__ void dda(const GridView& g, float px, float py, float pz, float dx,
+                                    float dy, float dz, DDAResult& r, Tally<STATS>& tl) {
+    const float len = __fsqrt_rn(
+        __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+    int32_t vx, vy, vz, stx, sty, stz;
+    float dlx, dly, dlz, sx, sy, sz;
+    dda_setup_axis(px, dx, g.nx, len, vx, stx, dlx, sx);
+    dda_setup_axis(py, dy, g.ny, len, vy, sty, dly, sy);
+    dda_setup_axis(pz, dz, g.nz, len, vz, stz, dlz, sz);
+    if (isnan(sx) || isnan(sy) || isnan(sz)) {
+        dda_literal<STATS>(g, vx, vy, vz, stx, sty, stz, dlx, dly, dlz, sx, sy, sz, r, tl);
+        return;
+    }
+    const int32_t vx0 = vx, vy0 = vy, vz0 = vz;
+    const uint32_t max_steps = g.max_steps;
+    uint32_t steps = 0, slot = kEmptyBrick;
+    bool mx = false, my = false, mz = false, hit = false;
+
+#define VT_DDA_STEP                                                          \
+    {                                                                        \
+        const float mnx = fminf(sy, sz), mny = fminf(sz, sx), mnz = fminf(sx, sy); \
+        mx = sx <= mnx;                                                      \
+        my = sy <= mny;                                                      \
+        mz = sz <= mnz;                                                      \
+        if (mx) sx = __fadd_rn(sx, dlx);                                     \
+        if (my) sy = __fadd_rn(sy, dly);                                     \
+        if (mz) sz = __fadd_rn(sz, dlz);                                     \
+        if (mx) vx += stx;                                                   \
+        if (my) vy += sty;                                                   \
+        if (mz) vz += stz;                                                   \
+        ++steps;                                                             \
+    }
+
+    if (grid_inside(g, vx, vy, vz)) {
+        for (;;) {
+            const int32_t bxi = vx >> 3, byi = vy >> 3, bzi = vz >> 3;
+            slot = __ldg(g.dir + ((size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi)));
+            // first coordinate outside this brick (or the grid) along each stepping direction
+            const int32_t ex = stx > 0 ? min((bxi << 3) + 8, g.nx) : (stx < 0 ? (bxi << 3) - 1 : INT_MIN);
+            const int32_t ey = sty > 0 ? min((byi << 3) + 8, g.ny) : (sty < 0 ? (byi << 3) - 1 : INT_MIN);
+            const int32_t ez = stz > 0 ? min((bzi << 3) + 8, g.nz) : (stz < 0 ? (bzi << 3) - 1 : INT_MIN);
+            tl.brick();
+            if (slot == kEmptyBrick) {
+                do VT_DDA_STEP while (vx != ex && vy != ey && vz != ez && steps < max_steps);
+            } else {
+                tl.nonempty();
+                const uint64_t* mk = g.masks + (size_t)slot * 8;
+                for (;;) {
+                    tl.tested();
+                    const uint64_t w = __ldg(mk + (vz & 7));
+                    if ((w >> (((vy & 7) << 3) | (vx & 7))) & 1ull) {
+                        hit = true;
+                        break;
+                    }
+                    VT_DDA_STEP
+                    if (vx == ex || vy == ey || vz == ez || steps >= max_steps) break;
+                }
+                if (hit) break;
+            }
+            if (steps >= max_steps || !grid_inside(g, vx, vy, vz)) break;
+        }
+    }
+#undef VT_DDA_STEP
+    tl.steps(steps);
+    r.vx = vx;
+    r.vy = vy;
+    r.vz = vz;
+    r.steps = steps;
+    r.slot = slot;
+    r.last = (mx ? 1 : 0) | (my ? 2 : 0) | (mz ? 4 : 0);
+    r.hit = hit;
+    // every iteration advanced at least one axis by one voxel, monotonically: some iteration
+    // advanced two or more iff the voxel moves outnumber the iterations
+    r.tie = (uint32_t)(abs(vx - vx0) + abs(vy - vy0) + abs(vz - vz0)) != steps;
+}
+
+// Ray/box entry against [0,nx]x[0,ny]x[0,nz]: 0 = miss, 1 = enters from outside, 2 = origin
+// inside.  Same operation order as the oracle's slab test.
+__device__ __forceinline__ int slab_entry(const GridView& g, const float o[3], const float d[3],
+                                          float pos[3], float& t_entry, int& axis) {
+    const float size[3] = {__int2float_rn(g.nx), __int2float_rn(g.ny), __int2float_rn(g.nz)};
+    float tn = -INFINITY, tf = INFINITY;
+    int ax = -1;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (d[a] == 0.0f) {
+            if (o[a] < 0.0f || o[a] > size[a]) return 0;
+            continue;
+        }
+        const float ta = __fdiv_rn(__fsub_rn(0.0f, o[a]), d[a]);
+        const float tb = __fdiv_rn(__fsub_rn(size[a], o[a]), d[a]);
+        const float lo = ta < tb ? ta : tb;
+        const float hi = ta < tb ? tb : ta;
+        if (lo > tn) {
+            tn = lo;
+            ax = a;
+        }
+        if (hi < tf) tf = hi;
+    }
+    if (tn > tf || tf < 0.0f) return 0;
+    if (tn <= 0.0f) {
+        pos[0] = o[0];
+        pos[1] = o[1];
+        pos[2] = o[2];
+        t_entry = 0.0f;
+        axis = -1;
+        return 2;
+    }
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        float p = __fadd_rn(o[b], __fmul_rn(tn, d[b]));
+        p = p < 0.0f ? 0.0f : p;
+        p = p > size[b] ? size[b] : p;
+        pos[b] = p;
+    }
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+        if (b == ax) pos[b] = d[b] > 0.0f ? 0.0f : size[b];
+    t_entry = tn;
+    axis = ax;
+    return 1;
+}
+
+__device__ __forceinline__ uint32_t face_code(int axis, bool normal_positive) {
+    return (uint32_t)(1 + 2 * axis + (normal_positive ? 0 : 1));
+}
+
+// Packed vt_hit: {x | y<<16, z | index<<16 | face<<24, t bits, rgba}.
+struct HitRec {
+    uint32_t w0, w1, w2, w3;
+};
+
+__device__ __forceinline__ HitRec miss_rec(uint32_t flags, uint32_t rgba) {
+    HitRec h;
+    h.w0 = 0xFFFFFFFFu;
+    h.w1 = 0xFFFFu | (flags << 24);
+    h.w2 = __float_as_uint(INFINITY);
+    h.w3 = rgba;
+    return h;
+}
+
+__device__ __forceinline__ bool finite3(const float a[3]) {
+    return isfinite(a[0]) && isfinite(a[1]) && isfinite(a[2]);
+}
+
+__device__ __forceinline__ uint32_t voxel_value(const GridView& g, uint32_t slot, int32_t x,
+                                                int32_t y, int32_t z, uint32_t& index) {
+    const uint32_t li = (uint32_t)(x & 7) | ((uint32_t)(y & 7) << 3) | ((uint32_t)(z & 7) << 6);
+    if (g.format == VT_PAYLOAD_U8) {
+        index = __ldg(g.payload8 + (size_t)slot * 512 + li);
+        return __ldg(g.palette + index);
+    }
+    index = 0;
+    return __ldg(g.payload32 + (size_t)slot * 512 + li);
+}
+
+// One ray: validity, slab entry, DDA, face, t, unshaded colour.  Mirrors vto_trace_ray_f32.
+// Returns the hit record; `o`/`d` are the ray, `hitv` receives the hit voxel for shading.
+template <bool STATS>
+__device__ __forceinline__ HitRec trace_ray(const GridView& g, const float o[3], const float d[3],
+                                            Tally<STATS>& tl) {
+    tl.rays();
+    if (!finite3(o) || !finite3(d)) return miss_rec(VT_HIT_FLAG_INVALID, 0u);
+    float pos[3], t_entry;
+    int entry_axis;
+    const int kind = slab_entry(g, o, d, pos, t_entry, entry_axis);
+    if (kind == 0) return miss_rec(0u, 0u);
+    DDAResult r;
+    dda<STATS>(g, pos[0], pos[1], pos[2], d[0], d[1], d[2], r, tl);
+    const uint32_t flags = r.tie ? VT_HIT_FLAG_TIE : 0u;
+    if (r.tie) tl.tie();
+    if (!r.hit) return miss_rec(flags, 0u);
+    uint32_t face = 0;
+    float t = 0.0f;
+    if (r.steps > 0) {
+        const int a = (r.last & 1) ? 0 : ((r.last & 2) ? 1 : 2);
+        const int32_t va = a == 0 ? r.vx : (a == 1 ? r.vy : r.vz);
+        const float da = a == 0 ? d[0] : (a == 1 ? d[1] : d[2]);
+        const float oa = a == 0 ? o[0] : (a == 1 ? o[1] : o[2]);
+        const float plane = __int2float_rn(da > 0.0f ? va : va + 1);
+        t = __fdiv_rn(__fsub_rn(plane, oa), da);
+        face = face_code(a, da < 0.0f);
+    } else if (kind == 1) {
+        const int a = entry_axis;
+        const float da = a == 0 ? d[0] : (a == 1 ? d[1] : d[2]);
+        t = t_entry;
+        face = face_code(a, da < 0.0f);
+    }
+    uint32_t index;
+    const uint32_t rgba = voxel_value(g, r.slot, r.vx, r.vy, r.vz, index);
+    HitRec h;
+    h.w0 = (uint32_t)r.vx | ((uint32_t)r.vy << 16);
+    h.w1 = (uint32_t)r.vz | (index << 16) | ((face | flags | VT_HIT_FLAG_HIT) << 24);
+    h.w2 = __float_as_uint(t);
+    h.w3 = rgba;
+    return h;
+}
+
+// Primary ray for pixel (px, py) + sub-pixel offset (jx, jy).  Mirrors vto_raygen.
+__device__ __forceinline__ void raygen(const vt_camera& c, uint32_t px, uint32_t py, float jx,
+                                       float jy, float o[3], float d[3]) {
+    const float inv_w2 = __fdiv_rn(2.0f, __uint2float_rn(c.width));
+    const float inv_h2 = __fdiv_rn(2.0f, __uint2float_rn(c.height));
+    const float fx = __fadd_rn(__uint2float_rn(px), jx);
+    const float fy = __fadd_rn(__uint2float_rn(py), jy);
+    const float sx = __fsub_rn(__fmul_rn(fx, inv_w2), 1.0f);
+    const float sy = __fsub_rn(1.0f, __fmul_rn(fy, inv_h2));
+    float r[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        r[a] = __fadd_rn(__fadd_rn(c.forward[a], __fmul_rn(sx, c.right[a])), __fmul_rn(sy, c.up[a]));
+    const float len = __fsqrt_rn(
+        __fadd_rn(__fadd_rn(__fmul_rn(r[0], r[0]), __fmul_rn(r[1], r[1])), __fmul_rn(r[2], r[2])));
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        d[a] = __fdiv_rn(r[a], len);
+        o[a] = c.origin[a];
+    }
+}
+
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), the published counter-based generator.
+__device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                              uint32_t k0, uint32_t k1, uint32_t out[4]) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+        const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+__device__ __forceinline__ void jitter(uint32_t seed, uint32_t view, uint32_t px, uint32_t py,
+                                       uint32_t s, float& jx, float& jy) {
+    uint32_t r[4];
+    philox4x32_10(px, py, s, view, seed, 0x56544752u, r);
+    jx = __fmul_rn(__uint2float_rn(r[0] >> 8), 0x1p-24f);
+    jy = __fmul_rn(__uint2float_rn(r[1] >> 8), 0x1p-24f);
+}
+
+// Primary hit + Lambert shading + optional hard shadow.  Mirrors the oracle's shade_from_ray.
+template <bool STATS>
+__device__ __forceinline__ HitRec shade_ray(const GridView& g, const LightView& L,
+                                            const float o[3], const float d[3],
+                                            Tally<STATS>& tl) {
+    HitRec h = trace_ray<STATS>(g, o, d, tl);
+    const uint32_t flags = h.w1 >> 24;
+    if (!(flags & VT_HIT_FLAG_HIT)) {
+        h.w3 = VT_SKY_RGBA;
+        return h;
+    }
+    tl.hit();
+    if (!L.enabled) return h;
+    const uint32_t face = flags & VT_FACE_MASK;
+    if (face == 0) return h;
+    const int a = (int)(face - 1) / 2;
+    const bool npos = (face & 1u) != 0u;
+    const float la = a == 0 ? L.dx : (a == 1 ? L.dy : L.dz);
+    const float ndl = npos ? la : -la;
+    float vis = 1.0f;
+    uint32_t extra = 0;
+    if (ndl > 0.0f && L.shadows) {
+        const int32_t hv[3] = {(int32_t)(h.w0 & 0xFFFFu), (int32_t)(h.w0 >> 16),
+                               (int32_t)(h.w1 & 0xFFFFu)};
+        const float t = __uint_as_float(h.w2);
+        float so[3];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) so[b] = __fadd_rn(o[b], __fmul_rn(t, d[b]));
+        const int32_t ha = a == 0 ? hv[0] : (a == 1 ? hv[1] : hv[2]);
+        const float plane = __int2float_rn(npos ? ha + 1 : ha);
+        const float sa = npos ? __fadd_rn(plane, 0.015625f) : __fsub_rn(plane, 0.015625f);
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+            if (b == a) so[b] = sa;
+        const float ld[3] = {L.dx, L.dy, L.dz};
+        const HitRec s = trace_ray<STATS>(g, so, ld, tl);
+        tl.shadow();
+        extra |= VT_HIT_FLAG_SHADOW_RAY;
+        if ((s.w1 >> 24) & VT_HIT_FLAG_HIT) {
+            vis = 0.0f;
+            extra |= VT_HIT_FLAG_SHADOWED;
+        }
+    }
+    const float lam = ndl > 0.0f ? ndl : 0.0f;
+    const float k = __fadd_rn(L.ambient, __fmul_rn(__fsub_rn(1.0f, L.ambient), __fmul_rn(lam, vis)));
+    const uint32_t base = h.w3;
+    uint32_t res = base & 0xFF000000u;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float v = __fadd_rn(__fmul_rn(__uint2float_rn((base >> (8 * c)) & 0xFFu), k), 0.5f);
+        const uint32_t q = v >= 255.0f ? 255u : (v <= 0.0f ? 0u : (uint32_t)v);
+        res |= q << (8 * c);
+    }
+    h.w3 = res;
+    h.w1 |= extra << 24;
+    return h;
+}
+
+}  // namespace vt

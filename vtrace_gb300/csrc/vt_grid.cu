@@ -1,0 +1,299 @@
+// vt_grid.cu — brick re-layout of a dense voxel grid (the ingest side of vtrace's add_texture,
+// lib/memory.c:286-385): x-fastest u8 palette indices or RGBA8 texels in device memory become
+// an 8^3-brick directory, 512-bit occupancy masks and dense payloads of occupied bricks only.
+//
+// Three passes, all coalesced along x:
+//   words   one thread per (brick, z-slice): reads 8 rows of 8 voxels, builds the 64-bit
+//           occupancy word; the 8 lanes of a brick OR their words into the brick's flag
+//   scan    exclusive prefix sum of the flags = each occupied brick's slot
+//   compact one thread per (brick, z-slice) of occupied bricks: copies the word and the slice's
+//           64 voxels into the slot; writes the directory
+// Lanes are assigned slice-fastest, so a warp covers 4 consecutive bricks along x: its reads are
+// 8 z-planes x 32 contiguous bytes per row and its word writes are 256 contiguous bytes.
+#include <cuda_runtime.h>
+
+#include "vt_device.cuh"
+#include "vt_kernels.h"
+
+namespace vt {
+
+constexpr int kScanThreads = 1024, kScanItems = 4;
+constexpr uint64_t kScanBlock = (uint64_t)kScanThreads * kScanItems;
+
+static inline uint64_t align_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
+
+static uint64_t scan_partials(uint64_t n) {
+    // partial sums of every recursion level of the scan
+    uint64_t total = 0;
+    while (n > kScanBlock) {
+        n = (n + kScanBlock - 1) / kScanBlock;
+        total += align_up(n, 64);
+    }
+    return total + 64;
+}
+
+size_t build_scratch_bytes(uint64_t bricks) {
+    return (size_t)(align_up(bricks * 64, 256) + align_up(bricks * 4, 256) * 2 +
+                    align_up(scan_partials(bricks) * 4, 256) + 256);
+}
+
+BuildScratch carve_build_scratch(void* base, uint64_t bricks) {
+    char* p = (char*)base;
+    BuildScratch s;
+    s.words = (uint64_t*)p;
+    p += align_up(bricks * 64, 256);
+    s.flags = (uint32_t*)p;
+    p += align_up(bricks * 4, 256);
+    s.offsets = (uint32_t*)p;
+    p += align_up(bricks * 4, 256);
+    s.block_sums = (uint32_t*)p;
+    p += align_up(scan_partials(bricks) * 4, 256);
+    s.occupied = (unsigned long long*)p;
+    return s;
+}
+
+struct BrickCoord {
+    int32_t bxi, byi, bzi;
+};
+
+__device__ __forceinline__ BrickCoord brick_coord(uint64_t brick, int32_t bx, int32_t by) {
+    BrickCoord c;
+    c.bxi = (int32_t)(brick % (uint64_t)bx);
+    const uint64_t r = brick / (uint64_t)bx;
+    c.byi = (int32_t)(r % (uint64_t)by);
+    c.bzi = (int32_t)(r / (uint64_t)by);
+    return c;
+}
+
+// Occupancy bits of one 8-voxel row: bit lx set iff voxel x0+lx is inside the grid and occupied.
+template <uint32_t FMT>
+__device__ __forceinline__ uint32_t row_bits(const void* src, const uint8_t* lut, size_t row_base,
+                                             int32_t x0, int32_t nx) {
+    uint32_t bits = 0;
+    if (FMT == VT_PAYLOAD_U8) {
+        const uint8_t* row = (const uint8_t*)src + row_base + x0;
+        if (x0 + 8 <= nx && (((uintptr_t)row) & 7u) == 0) {
+            const uint2 v = __ldg((const uint2*)row);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) bits |= (uint32_t)lut[(v.x >> (8 * k)) & 0xFFu] << k;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) bits |= (uint32_t)lut[(v.y >> (8 * k)) & 0xFFu] << (k + 4);
+        } else {
+            for (int k = 0; k < 8 && x0 + k < nx; ++k) bits |= (uint32_t)lut[__ldg(row + k)] << k;
+        }
+    } else {
+        const uint32_t* row = (const uint32_t*)src + row_base + x0;
+        if (x0 + 8 <= nx && (((uintptr_t)row) & 15u) == 0) {
+            const uint4 a = __ldg((const uint4*)row), b = __ldg((const uint4*)row + 1);
+            const uint32_t t[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int k = 0; k < 8; ++k) bits |= (uint32_t)((t[k] >> 24) != 0u) << k;
+        } else {
+            for (int k = 0; k < 8 && x0 + k < nx; ++k)
+                bits |= (uint32_t)((__ldg(row + k) >> 24) != 0u) << k;
+        }
+    }
+    return bits;
+}
+
+template <uint32_t FMT>
+__global__ void __launch_bounds__(256) brick_words_kernel(const void* __restrict__ src,
+                                                          const uint32_t* __restrict__ palette,
+                                                          int32_t nx, int32_t ny, int32_t nz,
+                                                          int32_t bx, int32_t by, uint64_t bricks,
+                                                          uint64_t* __restrict__ words,
+                                                          uint32_t* __restrict__ flags,
+                                                          unsigned long long* occupied) {
+    __shared__ uint8_t lut[256];
+    if (FMT == VT_PAYLOAD_U8) {
+        for (int i = threadIdx.x; i < 256; i += blockDim.x)
+            lut[i] = (uint8_t)((__ldg(palette + i) >> 24) != 0u);
+        __syncthreads();
+    }
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lz = (uint32_t)(t & 7u);
+    const uint64_t brick = t >> 3;
+    const bool valid = brick < bricks;
+    uint64_t w = 0;
+    if (valid) {
+        const BrickCoord c = brick_coord(brick, bx, by);
+        const int32_t z = c.bzi * 8 + (int32_t)lz, x0 = c.bxi * 8;
+        if (z < nz) {
+            for (int ly = 0; ly < 8; ++ly) {
+                const int32_t y = c.byi * 8 + ly;
+                if (y >= ny) break;
+                const size_t row_base = (size_t)nx * ((size_t)y + (size_t)ny * (size_t)z);
+                w |= (uint64_t)row_bits<FMT>(src, lut, row_base, x0, nx) << (8 * ly);
+            }
+        }
+    }
+    uint64_t any = w;
+    any |= __shfl_xor_sync(0xFFFFFFFFu, any, 1);
+    any |= __shfl_xor_sync(0xFFFFFFFFu, any, 2);
+    any |= __shfl_xor_sync(0xFFFFFFFFu, any, 4);
+    if (valid) {
+        words[brick * 8 + lz] = w;
+        if (lz == 0) flags[brick] = any != 0 ? 1u : 0u;
+    }
+    unsigned long long pc = (unsigned long long)__popcll(w);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) pc += __shfl_xor_sync(0xFFFFFFFFu, pc, off);
+    if ((threadIdx.x & 31) == 0 && pc) atomicAdd(occupied, pc);
+}
+
+// Exclusive scan of up to kScanBlock items per block; block totals go to `sums`.
+__global__ void __launch_bounds__(kScanThreads) scan_block_kernel(const uint32_t* __restrict__ in,
+                                                                  uint32_t* __restrict__ out,
+                                                                  uint64_t n,
+                                                                  uint32_t* __restrict__ sums) {
+    __shared__ uint32_t warp_tot[kScanThreads / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * kScanBlock + (uint64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], local = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < n ? in[base + k] : 0u;
+        local += v[k];
+    }
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = local;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+        if (lane >= (uint32_t)off) incl += y;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t wt = warp_tot[lane], wi = wt;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, off);
+            if (lane >= (uint32_t)off) wi += y;
+        }
+        warp_tot[lane] = wi - wt;  // exclusive prefix of warp totals
+        if (lane == 31) sums[blockIdx.x] = wi;
+    }
+    __syncthreads();
+    uint32_t run = warp_tot[warp] + incl - local;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void scan_add_kernel(uint32_t* __restrict__ out, uint64_t n,
+                                const uint32_t* __restrict__ block_offsets) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += block_offsets[i / kScanBlock];
+}
+
+static cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* partial,
+                                  cudaStream_t stream) {
+    const uint64_t blocks = (n + kScanBlock - 1) / kScanBlock;
+    scan_block_kernel<<<(unsigned)blocks, kScanThreads, 0, stream>>>(in, out, n, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || blocks == 1) return e;
+    // scan the block totals in place one level up, then add them back
+    uint32_t* next = partial + align_up(blocks, 64);
+    e = scan_exclusive(partial, partial, blocks, next, stream);
+    if (e != cudaSuccess) return e;
+    scan_add_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(out, n, partial);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_brick_scan(const BuildScratch& s, uint64_t bricks, cudaStream_t stream) {
+    return scan_exclusive(s.flags, s.offsets, bricks, s.block_sums, stream);
+}
+
+cudaError_t launch_brick_words(const void* src, uint32_t format, const uint32_t* d_palette,
+                               int32_t nx, int32_t ny, int32_t nz, const BuildScratch& s,
+                               cudaStream_t stream) {
+    const int32_t bx = (nx + 7) / 8, by = (ny + 7) / 8, bz = (nz + 7) / 8;
+    const uint64_t bricks = (uint64_t)bx * by * bz;
+    const uint64_t threads = bricks * 8;
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    cudaError_t e = cudaMemsetAsync(s.occupied, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    if (format == VT_PAYLOAD_U8)
+        brick_words_kernel<VT_PAYLOAD_U8><<<blocks, 256, 0, stream>>>(
+            src, d_palette, nx, ny, nz, bx, by, bricks, s.words, s.flags, s.occupied);
+    else
+        brick_words_kernel<VT_PAYLOAD_RGBA8><<<blocks, 256, 0, stream>>>(
+            src, nullptr, nx, ny, nz, bx, by, bricks, s.words, s.flags, s.occupied);
+    return cudaGetLastError();
+}
+
+template <uint32_t FMT>
+__global__ void __launch_bounds__(256) brick_compact_kernel(
+    const void* __restrict__ src, int32_t nx, int32_t ny, int32_t nz, int32_t bx, int32_t by,
+    uint64_t bricks, const uint64_t* __restrict__ words, const uint32_t* __restrict__ flags,
+    const uint32_t* __restrict__ offsets, uint32_t* __restrict__ dir, uint64_t* __restrict__ masks,
+    void* __restrict__ payload) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lz = (uint32_t)(t & 7u);
+    const uint64_t brick = t >> 3;
+    if (brick >= bricks) return;
+    const uint32_t f = __ldg(flags + brick);
+    const uint32_t slot = __ldg(offsets + brick);
+    if (lz == 0) dir[brick] = f ? slot : kEmptyBrick;
+    if (!f) return;
+    masks[(size_t)slot * 8 + lz] = __ldg(words + brick * 8 + lz);
+    const BrickCoord c = brick_coord(brick, bx, by);
+    const int32_t z = c.bzi * 8 + (int32_t)lz, x0 = c.bxi * 8;
+    for (int ly = 0; ly < 8; ++ly) {
+        const int32_t y = c.byi * 8 + ly;
+        const bool row_in = z < nz && y < ny;
+        const size_t row_base = (size_t)nx * ((size_t)y + (size_t)ny * (size_t)z);
+        const size_t dst = (size_t)slot * 512 + lz * 64 + ly * 8;
+        if (FMT == VT_PAYLOAD_U8) {
+            const uint8_t* row = (const uint8_t*)src + row_base + x0;
+            uint2 v = make_uint2(0u, 0u);
+            if (row_in) {
+                if (x0 + 8 <= nx && (((uintptr_t)row) & 7u) == 0) {
+                    v = __ldg((const uint2*)row);
+                } else {
+                    uint32_t b[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    for (int k = 0; k < 8 && x0 + k < nx; ++k) b[k] = __ldg(row + k);
+                    v.x = b[0] | (b[1] << 8) | (b[2] << 16) | (b[3] << 24);
+                    v.y = b[4] | (b[5] << 8) | (b[6] << 16) | (b[7] << 24);
+                }
+            }
+            *(uint2*)((uint8_t*)payload + dst) = v;
+        } else {
+            const uint32_t* row = (const uint32_t*)src + row_base + x0;
+            uint4 a = make_uint4(0u, 0u, 0u, 0u), b = a;
+            if (row_in) {
+                if (x0 + 8 <= nx && (((uintptr_t)row) & 15u) == 0) {
+                    a = __ldg((const uint4*)row);
+                    b = __ldg((const uint4*)row + 1);
+                } else {
+                    uint32_t q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    for (int k = 0; k < 8 && x0 + k < nx; ++k) q[k] = __ldg(row + k);
+                    a = make_uint4(q[0], q[1], q[2], q[3]);
+                    b = make_uint4(q[4], q[5], q[6], q[7]);
+                }
+            }
+            uint4* p = (uint4*)((uint32_t*)payload + dst);
+            p[0] = a;
+            p[1] = b;
+        }
+    }
+}
+
+cudaError_t launch_brick_compact(const void* src, uint32_t format, int32_t nx, int32_t ny,
+                                 int32_t nz, const BuildScratch& s, uint32_t* dir,
+                                 uint64_t* masks, void* payload, cudaStream_t stream) {
+    const int32_t bx = (nx + 7) / 8, by = (ny + 7) / 8, bz = (nz + 7) / 8;
+    const uint64_t bricks = (uint64_t)bx * by * bz;
+    const unsigned blocks = (unsigned)((bricks * 8 + 255) / 256);
+    if (format == VT_PAYLOAD_U8)
+        brick_compact_kernel<VT_PAYLOAD_U8><<<blocks, 256, 0, stream>>>(
+            src, nx, ny, nz, bx, by, bricks, s.words, s.flags, s.offsets, dir, masks, payload);
+    else
+        brick_compact_kernel<VT_PAYLOAD_RGBA8><<<blocks, 256, 0, stream>>>(
+            src, nx, ny, nz, bx, by, bricks, s.words, s.flags, s.offsets, dir, masks, payload);
+    return cudaGetLastError();
+}
+
+}  // namespace vt

@@ -1,0 +1,42 @@
+// vt_kernels.h — host-callable launchers of libvtrace's CUDA kernels (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vtrace.h"
+
+namespace vt {
+
+struct GridView;
+struct LightView;
+struct Counters;
+
+cudaError_t launch_render(const GridView& g, const vt_camera& cam, const LightView& light,
+                          uint4* out, Counters* counters, cudaStream_t stream);
+cudaError_t launch_trace_rays(const GridView& g, const vt_ray* rays, uint64_t n, uint4* out,
+                              Counters* counters, cudaStream_t stream);
+
+// Scratch of one brick build, sized for `bricks` bricks.
+struct BuildScratch {
+    uint64_t* words = nullptr;      // bricks * 8 occupancy words
+    uint32_t* flags = nullptr;      // bricks: 1 if the brick holds an occupied voxel
+    uint32_t* offsets = nullptr;    // bricks: exclusive prefix sum of flags (the slot)
+    uint32_t* block_sums = nullptr; // scan partials
+    unsigned long long* occupied = nullptr;
+};
+size_t build_scratch_bytes(uint64_t bricks);
+// Carves BuildScratch out of one buffer of build_scratch_bytes(bricks) bytes.
+BuildScratch carve_build_scratch(void* base, uint64_t bricks);
+
+// Phase 1: occupancy words, brick flags and the occupied-voxel count; phase 2: slots.
+cudaError_t launch_brick_words(const void* src, uint32_t format, const uint32_t* d_palette,
+                               int32_t nx, int32_t ny, int32_t nz, const BuildScratch& s,
+                               cudaStream_t stream);
+cudaError_t launch_brick_scan(const BuildScratch& s, uint64_t bricks, cudaStream_t stream);
+// Phase 3: directory, compacted masks and payloads.
+cudaError_t launch_brick_compact(const void* src, uint32_t format, int32_t nx, int32_t ny,
+                                 int32_t nz, const BuildScratch& s, uint32_t* dir,
+                                 uint64_t* masks, void* payload, cudaStream_t stream);
+
+}  // namespace vt
