@@ -219,7 +219,8 @@ def run_ours(args):
     npx = cam.width * cam.height
     d_hits = torch.empty(npx * 16, dtype=torch.uint8, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # the render and its events share this stream
+    torch.cuda.set_stream(stream)
 
     # counters of one frame (counting kernel, not timed): rays traced and algorithmic bytes
     stats = vt.render_stats(grid, cam, light, d_hits)

@@ -18,7 +18,9 @@
  *  - Pointers documented as "device" are CUDA device pointers; "host" pointers are ordinary host
  *    memory (pinned memory makes the copies asynchronous and faster, but is not required).
  *  - `stream` parameters are cudaStream_t values passed as void*; NULL selects the library's own
- *    stream. Calls that take a stream are asynchronous with respect to the host unless stated.
+ *    (non-blocking) stream, so a caller that wants the legacy default stream passes
+ *    cudaStreamLegacy.  Calls that take a stream are asynchronous with respect to the host unless
+ *    stated.
  *  - Voxel grids are x-fastest: index = x + nx * (y + ny * z), the layout the reference uploads
  *    with bufferRowLength = 0 (lib/memory.c:353-366).
  */
@@ -49,7 +51,8 @@ extern "C" {
  *  x, y, z        hit voxel (0xFFFF on a miss)
  *  palette_index  voxel value of the hit (u8 grids); 0 for RGBA8 grids and misses
  *  face           bits 0-2: entered face as its outward normal, VT_FACE_*; 0 when the ray starts
- *                 inside the hit voxel or misses.  Bits 3-7: VT_HIT_FLAG_*.
+ *                 inside the hit voxel or misses.  Bits 3-7: VT_HIT_FLAG_* (bit 6 is reserved
+ *                 and always 0; multi-axis ties are counted in vt_trace_stats.ties).
  *  t              ray parameter of the entered face plane, (plane - origin[a]) / dir[a]; 0 when the
  *                 origin lies in the hit voxel; +inf on a miss
  *  rgba           colour, little-endian R | G<<8 | B<<16 | A<<24: the voxel colour for
@@ -74,7 +77,6 @@ typedef struct vt_hit {
 #define VT_HIT_FLAG_SHADOW_RAY 0x08u /* a shadow ray was traced for this hit */
 #define VT_HIT_FLAG_INVALID 0x10u    /* non-finite origin or direction: reported as a miss */
 #define VT_HIT_FLAG_SHADOWED 0x20u   /* the shadow ray found an occupied voxel */
-#define VT_HIT_FLAG_TIE 0x40u        /* a DDA step advanced two or three axes at once (edge/corner) */
 #define VT_HIT_FLAG_HIT 0x80u        /* an occupied voxel was found */
 
 /* sRGB encoding of the reference's clear colour (0.53, 0.81, 0.92, 1) (lib/command.c:57-60). */
@@ -130,7 +132,8 @@ typedef struct vt_trace_stats {
     uint64_t bricks_entered;      /* brick visits (directory lookups) over all rays */
     uint64_t nonempty_bricks_entered;
     uint64_t voxels_tested;       /* occupancy-bit tests inside non-empty bricks */
-    uint64_t ties;                /* rays with VT_HIT_FLAG_TIE */
+    uint64_t ties;                /* rays with an iteration that advanced two or three axes at
+                                     once (an exact tie on a voxel edge or corner) */
 } vt_trace_stats;
 
 /* ---------------------------------------------------------------- library state */
@@ -164,8 +167,11 @@ int32_t vt_grid_create_u8_device(const uint8_t* d_voxels, const uint32_t* palett
 int32_t vt_grid_create_rgba8(const uint8_t* rgba, uint32_t nx, uint32_t ny, uint32_t nz);
 int32_t vt_grid_destroy(int32_t grid);
 int32_t vt_grid_get_info(int32_t grid, vt_grid_info* info);
-/* Copy the grid's brick directory (bricks_total u32, 0xFFFFFFFF = empty brick, else the brick's
- * slot) and occupancy masks (bricks_nonempty * 64 bytes) to host memory; either may be NULL. */
+/* Copy the grid's brick directory and occupancy masks to host memory; either may be NULL.
+ * directory: bricks_total u32, x-fastest over bricks; an occupied brick's entry is its slot
+ * (bit 31 clear); an empty brick's entry is 0x80000000 | d, d = Chebyshev distance in bricks to
+ * the nearest occupied brick (1..31, saturating).  masks: bricks_nonempty * 8 u64 by slot, word
+ * lz holding bit (ly * 8 + lx) of z-slice lz. */
 int32_t vt_grid_download_bricks(int32_t grid, uint32_t* directory, uint64_t* masks);
 
 /* ---------------------------------------------------------------- tracing */

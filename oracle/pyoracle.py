@@ -18,7 +18,6 @@ assert HIT_DTYPE.itemsize == 16
 FLAG_SHADOW_RAY = 0x08
 FLAG_INVALID = 0x10
 FLAG_SHADOWED = 0x20
-FLAG_TIE = 0x40
 FLAG_HIT = 0x80
 SKY_RGBA = 0xFFF6E8C0
 
@@ -254,3 +253,24 @@ def ref_trace(grid, mp, s, variant="select", colours=False):
     L.vtref_trace(_ptr(rgba), grid.nx, grid.ny, grid.nz, mp.shape[0], _ptr(mp), _ptr(s),
                   _ptr(out), _ptr(col))
     return (out, col) if colours else out
+
+
+def compat_render(grids, instances, P, C, width, height, threads=0):
+    """The reference's multi-instance frame (see vto_compat_render): RGBA8 [height, width, 4]."""
+    L = lib()
+    arr = (_Grid * max(1, len(grids)))()
+    for i, g in enumerate(grids):
+        arr[i] = g._g
+    inst = np.ascontiguousarray(instances, dtype=np.float32).reshape(-1, 16)
+    P = np.ascontiguousarray(P, dtype=np.float32).reshape(16)
+    C = np.ascontiguousarray(C, dtype=np.float32).reshape(16)
+    out = np.zeros((height, width, 4), np.uint8)
+    L.vto_compat_render.argtypes = [ctypes.POINTER(_Grid), ctypes.c_uint32, ctypes.c_void_p,
+                                    ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                    ctypes.c_int]
+    rc = L.vto_compat_render(arr, len(grids), _ptr(inst), inst.shape[0], _ptr(P), _ptr(C),
+                             width, height, _ptr(out), threads)
+    if rc != 0:
+        raise ValueError("singular projection or camera matrix")
+    return out

@@ -191,7 +191,7 @@ void vto_trace_ray_f32(const vto_grid* g, const float o[3], const float d[3], vt
     }
     vto_dda_out r;
     vto_dda_f32(g, pos, d, &r, stats);
-    uint8_t flags = r.tie ? VTO_FLAG_TIE : 0;
+    const uint8_t flags = 0; /* ties are counted in the statistics, not flagged per record */
     if (stats && r.tie) stats->ties++;
     if (!r.hit) {
         miss_record(out, flags);
@@ -199,7 +199,7 @@ void vto_trace_ray_f32(const vto_grid* g, const float o[3], const float d[3], vt
     }
     uint8_t face = 0;
     float t = 0.0f;
-    if (r.steps > 0) {
+    if (r.last_mask != 0) { /* the ray moved: face of the final iteration's step */
         int a = (r.last_mask & 1) ? 0 : ((r.last_mask & 2) ? 1 : 2);
         float plane = (float)(r.step[a] > 0 ? r.v[a] : r.v[a] + 1);
         t = (plane - o[a]) / d[a];
@@ -585,4 +585,211 @@ void vto_trace_rays_f64(const vto_grid* g, const float* rays, uint64_t n, vto_hi
     p.rays = rays;
     p.hits64 = hits;
     run_parallel(&p, 0, n, threads, NULL);
+}
+
+/* ------------------------------------------------------------------ reference-compatible frame
+ *
+ * Restates libvtrace's headless render_tick: the reference rasterises one cube per instance and
+ * marches from each front-face fragment (trace.frag:41-90), depth-tests LESS on the cube face
+ * (lib/pipeline.c:146-152) and blends SRC_ALPHA / ONE_MINUS_SRC_ALPHA into an sRGB target
+ * cleared to (0.53, 0.81, 0.92, 1) (lib/command.c:57-60, lib/pipeline.c:129-137).  Per pixel, in
+ * draw order: slab entry into [-0.5,0.5]^3 along inverse(model) * view ray (skipped when the
+ * camera is inside), DDA from (entry + 0.5) * size, blend on a hit nearer than the depth so far.
+ * Matrix preparation is in binary64 with the same cofactor expansion as the library. */
+
+static double srgb_to_linear_d(double c) {
+    return c <= 0.04045 ? c / 12.92 : pow((c + 0.055) / 1.055, 2.4);
+}
+
+static int invert4d(const double* a, double* inv) {
+    double r[16];
+    r[0] = a[5] * a[10] * a[15] - a[5] * a[11] * a[14] - a[9] * a[6] * a[15] + a[9] * a[7] * a[14] + a[13] * a[6] * a[11] - a[13] * a[7] * a[10];
+    r[4] = -a[4] * a[10] * a[15] + a[4] * a[11] * a[14] + a[8] * a[6] * a[15] - a[8] * a[7] * a[14] - a[12] * a[6] * a[11] + a[12] * a[7] * a[10];
+    r[8] = a[4] * a[9] * a[15] - a[4] * a[11] * a[13] - a[8] * a[5] * a[15] + a[8] * a[7] * a[13] + a[12] * a[5] * a[11] - a[12] * a[7] * a[9];
+    r[12] = -a[4] * a[9] * a[14] + a[4] * a[10] * a[13] + a[8] * a[5] * a[14] - a[8] * a[6] * a[13] - a[12] * a[5] * a[10] + a[12] * a[6] * a[9];
+    r[1] = -a[1] * a[10] * a[15] + a[1] * a[11] * a[14] + a[9] * a[2] * a[15] - a[9] * a[3] * a[14] - a[13] * a[2] * a[11] + a[13] * a[3] * a[10];
+    r[5] = a[0] * a[10] * a[15] - a[0] * a[11] * a[14] - a[8] * a[2] * a[15] + a[8] * a[3] * a[14] + a[12] * a[2] * a[11] - a[12] * a[3] * a[10];
+    r[9] = -a[0] * a[9] * a[15] + a[0] * a[11] * a[13] + a[8] * a[1] * a[15] - a[8] * a[3] * a[13] - a[12] * a[1] * a[11] + a[12] * a[3] * a[9];
+    r[13] = a[0] * a[9] * a[14] - a[0] * a[10] * a[13] - a[8] * a[1] * a[14] + a[8] * a[2] * a[13] + a[12] * a[1] * a[10] - a[12] * a[2] * a[9];
+    r[2] = a[1] * a[6] * a[15] - a[1] * a[7] * a[14] - a[5] * a[2] * a[15] + a[5] * a[3] * a[14] + a[13] * a[2] * a[7] - a[13] * a[3] * a[6];
+    r[6] = -a[0] * a[6] * a[15] + a[0] * a[7] * a[14] + a[4] * a[2] * a[15] - a[4] * a[3] * a[14] - a[12] * a[2] * a[7] + a[12] * a[3] * a[6];
+    r[10] = a[0] * a[5] * a[15] - a[0] * a[7] * a[13] - a[4] * a[1] * a[15] + a[4] * a[3] * a[13] + a[12] * a[1] * a[7] - a[12] * a[3] * a[5];
+    r[14] = -a[0] * a[5] * a[14] + a[0] * a[6] * a[13] + a[4] * a[1] * a[14] - a[4] * a[2] * a[13] - a[12] * a[1] * a[6] + a[12] * a[2] * a[5];
+    r[3] = -a[1] * a[6] * a[11] + a[1] * a[7] * a[10] + a[5] * a[2] * a[11] - a[5] * a[3] * a[10] - a[9] * a[2] * a[7] + a[9] * a[3] * a[6];
+    r[7] = a[0] * a[6] * a[11] - a[0] * a[7] * a[10] - a[4] * a[2] * a[11] + a[4] * a[3] * a[10] + a[8] * a[2] * a[7] - a[8] * a[3] * a[6];
+    r[11] = -a[0] * a[5] * a[11] + a[0] * a[7] * a[9] + a[4] * a[1] * a[11] - a[4] * a[3] * a[9] - a[8] * a[1] * a[7] + a[8] * a[3] * a[5];
+    r[15] = a[0] * a[5] * a[10] - a[0] * a[6] * a[9] - a[4] * a[1] * a[10] + a[4] * a[2] * a[9] + a[8] * a[1] * a[6] - a[8] * a[2] * a[5];
+    const double det = a[0] * r[0] + a[1] * r[4] + a[2] * r[8] + a[3] * r[12];
+    if (!(det != 0.0) || !isfinite(det)) return 0;
+    for (int i = 0; i < 16; ++i) inv[i] = r[i] / det;
+    return 1;
+}
+
+static void mul4d(const double* a, const double* b, double* c) {
+    for (int col = 0; col < 4; ++col)
+        for (int row = 0; row < 4; ++row) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += a[k * 4 + row] * b[col * 4 + k];
+            c[col * 4 + row] = s;
+        }
+}
+
+typedef struct compat_inst {
+    float minv[12];
+    int32_t texture;
+} compat_inst;
+
+typedef struct compat_job {
+    const vto_grid* grids;
+    const compat_inst* inst;
+    uint32_t ninst;
+    float dirm[12], cam[3];
+    int32_t width, height;
+    float decode[256], thresh[255];
+    uint8_t* out;
+    uint64_t begin, end;
+} compat_job;
+
+static uint32_t srgb_encode_t(const float* thresh, float v) {
+    uint32_t lo = 0, hi = 255;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (thresh[mid] <= v)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+static void compat_pixel(const compat_job* f, int32_t px, int32_t py) {
+    const float inv_w = 2.0f / (float)f->width;
+    const float xn = ((float)px + 0.5f) * inv_w - 1.0f;
+    const float yn = ((float)py + 0.5f) * inv_w - 1.0f;
+    float dw[3];
+    for (int r = 0; r < 3; ++r)
+        dw[r] = ((f->dirm[4 * r] * xn + f->dirm[4 * r + 1] * yn) + f->dirm[4 * r + 2]) + f->dirm[4 * r + 3];
+    const float len = sqrtf((dw[0] * dw[0] + dw[1] * dw[1]) + dw[2] * dw[2]);
+    for (int r = 0; r < 3; ++r) dw[r] = dw[r] / len;
+    uint32_t col[3] = {VTO_SKY_RGBA & 0xFFu, (VTO_SKY_RGBA >> 8) & 0xFFu, (VTO_SKY_RGBA >> 16) & 0xFFu};
+    uint32_t ca = VTO_SKY_RGBA >> 24;
+    float depth = INFINITY;
+    for (uint32_t i = 0; i < f->ninst; ++i) {
+        const compat_inst* I = &f->inst[i];
+        const vto_grid* g = &f->grids[I->texture];
+        float om[3], dm[3];
+        for (int r = 0; r < 3; ++r) {
+            const float* m = I->minv + 4 * r;
+            om[r] = ((m[0] * f->cam[0] + m[1] * f->cam[1]) + m[2] * f->cam[2]) + m[3];
+            dm[r] = (m[0] * dw[0] + m[1] * dw[1]) + m[2] * dw[2];
+        }
+        float tn = -INFINITY, tf = INFINITY;
+        int ax = -1, miss = 0;
+        for (int a = 0; a < 3; ++a) {
+            if (dm[a] == 0.0f) {
+                if (om[a] < -0.5f || om[a] > 0.5f) miss = 1;
+                continue;
+            }
+            const float ta = (-0.5f - om[a]) / dm[a];
+            const float tb = (0.5f - om[a]) / dm[a];
+            const float lo = ta < tb ? ta : tb, hi = ta < tb ? tb : ta;
+            if (lo > tn) {
+                tn = lo;
+                ax = a;
+            }
+            if (hi < tf) tf = hi;
+        }
+        if (miss || tn > tf || tf < 0.0f || tn <= 0.0f) continue;
+        if (!(tn < depth)) continue;
+        const float size[3] = {(float)g->nx, (float)g->ny, (float)g->nz};
+        float pos[3];
+        for (int b = 0; b < 3; ++b) {
+            float mp = om[b] + tn * dm[b];
+            mp = mp < -0.5f ? -0.5f : (mp > 0.5f ? 0.5f : mp);
+            if (b == ax) mp = dm[b] > 0.0f ? -0.5f : 0.5f;
+            pos[b] = (mp + 0.5f) * size[b];
+        }
+        vto_dda_out r;
+        vto_dda_f32(g, pos, dm, &r, NULL);
+        if (!r.hit) continue;
+        const uint32_t tex = voxel_rgba(g, r.v[0], r.v[1], r.v[2]);
+        const float a = (float)(tex >> 24) / 255.0f;
+        const float ia = 1.0f - a;
+        for (int c = 0; c < 3; ++c) {
+            const float v = f->decode[(tex >> (8 * c)) & 0xFFu] * a + f->decode[col[c]] * ia;
+            col[c] = srgb_encode_t(f->thresh, v);
+        }
+        ca = tex >> 24;
+        depth = tn;
+    }
+    uint8_t* o = f->out + 4 * ((size_t)py * f->width + px);
+    o[0] = (uint8_t)col[0];
+    o[1] = (uint8_t)col[1];
+    o[2] = (uint8_t)col[2];
+    o[3] = (uint8_t)ca;
+}
+
+static void* compat_worker(void* arg) {
+    compat_job* j = (compat_job*)arg;
+    for (uint64_t p = j->begin; p < j->end; ++p)
+        compat_pixel(j, (int32_t)(p % (uint64_t)j->width), (int32_t)(p / (uint64_t)j->width));
+    return NULL;
+}
+
+int vto_compat_render(const vto_grid* grids, uint32_t ngrids, const float* instances,
+                      uint32_t ninst, const float P[16], const float C[16], int32_t width,
+                      int32_t height, uint8_t* rgba, int threads) {
+    double p[16], cm[16], c0[16], ip[16], ic[16], ic0[16], dm[16];
+    for (int i = 0; i < 16; ++i) {
+        p[i] = P[i];
+        cm[i] = C[i];
+        c0[i] = C[i];
+    }
+    c0[12] = c0[13] = c0[14] = 0.0;
+    if (!invert4d(p, ip) || !invert4d(cm, ic) || !invert4d(c0, ic0)) return -1;
+    mul4d(ic0, ip, dm);
+    compat_job f;
+    memset(&f, 0, sizeof(f));
+    for (int r = 0; r < 3; ++r)
+        for (int k = 0; k < 4; ++k) f.dirm[4 * r + k] = (float)dm[k * 4 + r];
+    for (int r = 0; r < 3; ++r) f.cam[r] = (float)ic[12 + r];
+    f.width = width;
+    f.height = height;
+    for (int i = 0; i < 256; ++i) f.decode[i] = (float)srgb_to_linear_d(i / 255.0);
+    for (int k = 0; k < 255; ++k) f.thresh[k] = (float)srgb_to_linear_d((k + 0.5) / 255.0);
+    compat_inst* inst = (compat_inst*)calloc(ninst ? ninst : 1, sizeof(compat_inst));
+    uint32_t n = 0;
+    for (uint32_t i = 0; i < ninst; ++i) {
+        const float* m = instances + 16 * i;
+        int32_t tid;
+        memcpy(&tid, &m[15], 4);
+        if (tid < 0 || (uint32_t)tid >= ngrids) continue;
+        double md[16], mi[16];
+        for (int k = 0; k < 16; ++k) md[k] = m[k];
+        md[15] = 1.0;
+        if (!invert4d(md, mi)) continue;
+        for (int r = 0; r < 3; ++r)
+            for (int k = 0; k < 4; ++k) inst[n].minv[4 * r + k] = (float)mi[k * 4 + r];
+        inst[n].texture = tid;
+        ++n;
+    }
+    f.grids = grids;
+    f.inst = inst;
+    f.ninst = n;
+    f.out = rgba;
+    if (threads <= 0) threads = vto_hardware_threads();
+    const uint64_t total = (uint64_t)width * height;
+    compat_job* jobs = (compat_job*)calloc((size_t)threads, sizeof(compat_job));
+    pthread_t* tids = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
+    for (int t = 0; t < threads; ++t) {
+        jobs[t] = f;
+        jobs[t].begin = total * (uint64_t)t / (uint64_t)threads;
+        jobs[t].end = total * (uint64_t)(t + 1) / (uint64_t)threads;
+        pthread_create(&tids[t], NULL, compat_worker, &jobs[t]);
+    }
+    for (int t = 0; t < threads; ++t) pthread_join(tids[t], NULL);
+    free(tids);
+    free(jobs);
+    free(inst);
+    return 0;
 }

@@ -21,8 +21,8 @@
  * literal IEEE product 0 * inf = NaN would freeze rays with a zero direction component.
  *
  * Parity pin: the reference has no golden vectors for this path and its shaders need a graphics
- * API.  oracle/ref_tracefrag builds shaders/trace.frag itself as C++ through a GLSL-compatibility
- * header (oracle/glsl_compat.hpp); tests compare this restatement against that build where the
+ * API.  oracle/build.py (build_ref) compiles shaders/trace.frag itself as C++ through a
+ * GLSL-compatibility header (oracle/glsl_compat.hpp, driven by oracle/ref_harness.cpp); tests compare this restatement against that build where the
  * reference tree is present.  Camera ray generation, the slab entry, face ids, t, shading and
  * shadow rays are this project's own specification (the reference derives rays from rasterised
  * cube faces and has no shading), stated once here and mirrored by the kernels.
@@ -93,7 +93,6 @@ typedef struct vto_hit64 {
 #define VTO_FLAG_SHADOW_RAY 0x08u
 #define VTO_FLAG_INVALID 0x10u
 #define VTO_FLAG_SHADOWED 0x20u
-#define VTO_FLAG_TIE 0x40u
 #define VTO_FLAG_HIT 0x80u
 
 /* Allocate and fill g->brick_nonempty; vto_grid_release frees it. */
@@ -151,6 +150,13 @@ void vto_trace_rays(const vto_grid* g, const float* rays, uint64_t n, vto_hit* h
 /* binary64 traversal of a ray buffer (for t accuracy and tie-divergence statistics). */
 void vto_trace_rays_f64(const vto_grid* g, const float* rays, uint64_t n, vto_hit64* hits,
                         int threads);
+
+/* The reference's multi-instance frame as libvtrace's headless render_tick computes it: RGBA8
+ * sRGB pixels, row-major from the top row.  instances: n column-major mat4 (texture id in the bits
+ * of element [3][3]); grids: the textures by id.  Returns 0, or -1 for singular matrices. */
+int vto_compat_render(const vto_grid* grids, uint32_t ngrids, const float* instances,
+                      uint32_t ninst, const float P[16], const float C[16], int32_t width,
+                      int32_t height, uint8_t* rgba, int threads);
 
 int vto_hardware_threads(void);
 

@@ -1,0 +1,114 @@
+"""The reference-compatible C entry points (entry, add_texture, start/end_update_instances,
+render_tick, get_input_data_pointer, cleanup) driven in the order vtrace's Rust host calls them
+(src/render.rs:184-320), with the headless framebuffer checked against the oracle."""
+import ctypes
+import math
+import struct
+
+import numpy as np
+import pytest
+
+import vtrace_gb300 as vt
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+
+def perspective(fov, aspect, near, far):
+    """glm::perspective (OpenGL clip conventions), column-major, as src/render.rs:208-210."""
+    f = 1.0 / math.tan(fov / 2.0)
+    m = np.zeros((4, 4), np.float32)  # m[col][row]
+    m[0][0] = f / aspect
+    m[1][1] = f
+    m[2][2] = (far + near) / (near - far)
+    m[2][3] = -1.0
+    m[3][2] = 2.0 * far * near / (near - far)
+    return m
+
+
+def look_at(eye, center, up):
+    """glm::look_at, column-major, as src/render.rs:212-214."""
+    eye, center, up = (np.asarray(v, np.float64) for v in (eye, center, up))
+    f = center - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[0, :3] = s
+    m[1, :3] = u
+    m[2, :3] = -f
+    m[:3, 3] = [-s @ eye, -u @ eye, f @ eye]
+    return np.ascontiguousarray(m.T, np.float32)  # column-major storage
+
+
+def instance(rot_deg, axis, scale, translate, texture_id):
+    a = math.radians(rot_deg)
+    ax = np.asarray(axis, np.float64)
+    ax /= np.linalg.norm(ax)
+    K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+    R = np.eye(3) + math.sin(a) * K + (1 - math.cos(a)) * (K @ K)
+    M = np.eye(4)
+    M[:3, :3] = R @ np.diag(scale)
+    M[:3, 3] = translate
+    cm = np.ascontiguousarray(M.T, np.float32).reshape(16)
+    cm[15] = struct.unpack("<f", struct.pack("<i", texture_id))[0]  # trace.vert:38
+    return cm
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import torch
+    assert torch.cuda.is_available()
+    return vt.lib()
+
+
+def test_reference_call_sequence(lib):
+    L = lib
+    assert L.entry() == 0
+    rng = np.random.default_rng(3)
+    # two textures: x-fastest RGBA8, some translucent texels
+    t0 = np.zeros((16, 16, 16, 4), np.uint8)
+    solid = rng.random((16, 16, 16)) < 0.08
+    t0[solid] = rng.integers(0, 256, (int(solid.sum()), 4), dtype=np.uint8)
+    t0[solid, 3] = rng.choice([255, 255, 128, 40], int(solid.sum()))
+    t1 = np.zeros((10, 12, 8, 4), np.uint8)  # (z, y, x): 8 x 12 x 10
+    t1[2:8, 3:9, 1:7] = (200, 60, 30, 255)
+    id0 = L.add_texture(t0.ctypes.data, 16, 16, 16)
+    id1 = L.add_texture(t1.ctypes.data, 8, 12, 10)
+    assert (id0, id1) == (0, 1)
+    insts = np.stack([
+        instance(0, (0, 1, 0), (4, 4, 4), (0, 0, -6), 0),
+        instance(30, (1, 1, 0), (3, 5, 3), (2.5, -1, -9), 1),
+        instance(-20, (0, 0, 1), (6, 6, 6), (-3, 1, -12), 0),
+        instance(0, (0, 1, 0), (1, 1, 1), (0, 0, -3), 7),        # unbound texture: not drawn
+        instance(0, (0, 1, 0), (50, 50, 50), (0, 0, 0), 1),      # camera inside: culled
+    ])
+    ptr = L.start_update_instances(len(insts))
+    assert ptr
+    ctypes.memmove(ptr, insts.ctypes.data, insts.nbytes)
+    assert L.end_update_instances(len(insts)) == 0
+    P = perspective(80.0 / 180.0 * 3.1415926, 1.0, 0.01, 10000.0)  # src/render.rs:190,199
+    C = look_at((0.5, 0.8, 2.0), (0.0, 0.0, -8.0), (0.0, 1.0, 0.0))
+    info = vt.RenderTickInfo(P.ctypes.data, C.ctypes.data)
+    w, h = ctypes.c_int32(0), ctypes.c_int32(0)
+    assert L.render_tick(ctypes.byref(w), ctypes.byref(h), ctypes.byref(info)) == 0
+    assert (w.value, h.value) == (1000, 1000)
+    fb = np.zeros((1000, 1000, 4), np.uint8)
+    assert L.vt_framebuffer_download(fb.ctypes.data, fb.nbytes) == 0
+    grids = [po.Grid(texels=t0.view(np.uint32)[..., 0]), po.Grid(texels=t1.view(np.uint32)[..., 0])]
+    want = po.compat_render(grids, insts, P, C, 1000, 1000)
+    diff = np.nonzero((fb != want).any(-1))
+    assert len(diff[0]) == 0, (len(diff[0]), fb[diff][:3], want[diff][:3])
+    sky = np.array([0xC0, 0xE8, 0xF6, 0xFF], np.uint8)
+    covered = (fb != sky).any(-1).mean()
+    assert 0.01 < covered < 0.9
+    inp = L.get_input_data_pointer()
+    assert bytes(inp.contents.keys) == b"\0" * 6
+    # zero instances are treated as one (lib/memory.c:236,251)
+    assert L.start_update_instances(0)
+    assert L.end_update_instances(0) == 0
+    assert L.render_tick(ctypes.byref(w), ctypes.byref(h), ctypes.byref(info)) == 0
+    L.cleanup()
+    assert L.render_tick(ctypes.byref(w), ctypes.byref(h), ctypes.byref(info)) == -1
+    assert L.add_texture(t0.ctypes.data, 16, 16, 16) == -1

@@ -56,7 +56,6 @@ def device_trace(torch, grid, rays):
     d_hits = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
     vt.trace_rays(grid, d_rays, n, d_hits)
     torch.cuda.synchronize()
-    vt.check(vt.lib().vt_init(0))
     return hits_from_dev(d_hits), d_rays, d_hits
 
 
@@ -106,7 +105,9 @@ def test_rgba8_grid_matches_oracle(torch, path):
         g.destroy()
 
 
-def expected_bricks(vox, pal):
+def expected_bricks(vox, pal, cap=31):
+    """Directory (slot, or 0x80000000 | Chebyshev brick distance to the nearest occupied brick,
+    1..cap), masks and occupied-voxel count, by brute force."""
     nz, ny, nx = vox.shape
     occ = (pal[vox] >> 24) != 0
     bx, by, bz = (nx + 7) // 8, (ny + 7) // 8, (nz + 7) // 8
@@ -118,7 +119,15 @@ def expected_bricks(vox, pal):
     words = (bits.astype(np.uint64) << np.arange(64, dtype=np.uint64)).sum(axis=2, dtype=np.uint64)
     nonempty = bits.any(axis=(1, 2))
     slots = np.cumsum(nonempty) - 1
-    directory = np.where(nonempty, slots, 0xFFFFFFFF).astype(np.uint32)
+    zz, yy, xx = np.meshgrid(np.arange(bz), np.arange(by), np.arange(bx), indexing="ij")
+    coords = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], 1)
+    occ_c = coords[nonempty]
+    if len(occ_c):
+        d = np.abs(coords[:, None, :] - occ_c[None, :, :]).max(-1).min(1)
+    else:
+        d = np.full(len(coords), cap)
+    d = np.clip(d, 1, cap)
+    directory = np.where(nonempty, slots, 0x80000000 | d).astype(np.uint32)
     return directory, words[nonempty], int(occ.sum())
 
 
@@ -153,7 +162,7 @@ def test_terrain256_full_frame_and_counters(torch):
         og = po.Grid(w["voxels"], w["palette"])
         want, ostats = po.render(og, oracle_camera(cam), oracle_light(light), stats=True)
         assert_hits_equal(img, want, "terrain256 640x480")
-        assert (img["face"] & vt.FLAG_HIT).astype(bool).mean() > 0.5
+        assert (img["face"] & vt.FLAG_HIT).astype(bool).mean() > 0.3
         gstats = vt.render_stats(g, cam, light, d_hits)
         assert gstats == ostats
         img2 = hits_from_dev(d_hits).reshape(cam.height, cam.width)
@@ -270,5 +279,47 @@ def test_errors_are_reported_not_fatal(torch):
         # an empty grid: everything misses
         hits = vt.trace_rays_host(g, np.array([[4, 4, -5, 0, 0, 1]], np.float32))
         assert not hits["face"][0] & vt.FLAG_HIT
+    finally:
+        g.destroy()
+
+
+def special_rays(rng, dims, n):
+    """Axis-parallel, planar, exact-diagonal and grazing rays from inside and outside."""
+    size = np.array(dims, np.float32)
+    o = (rng.random((n, 3)) * 1.4 - 0.2).astype(np.float32) * size
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    k = n // 6
+    d[:k, 1:] = 0                                   # along x
+    d[k:2 * k, rng.integers(0, 3)] = 0              # in a coordinate plane
+    d[2 * k:3 * k] = rng.choice([-1.0, 1.0], (k, 3)).astype(np.float32)  # exact diagonals
+    o[2 * k:3 * k] = np.floor(o[2 * k:3 * k]) + 0.5
+    d[3 * k:4 * k, 2] *= 1e-4                       # grazing
+    o[4 * k:5 * k] = np.round(o[4 * k:5 * k])       # voxel corners
+    return np.concatenate([o, d], 1).astype(np.float32)
+
+
+@pytest.mark.parametrize("dims,count", [((200, 136, 264), 12), ((256, 256, 256), 3),
+                                        ((97, 300, 41), 40)])
+def test_empty_space_skipping_is_exact(torch, dims, count):
+    """Large empty regions (distance field up to its cap) crossed by the per-axis chains must
+    give the same records as the oracle's voxel-by-voxel loop, and as the counting kernel."""
+    nx, ny, nz = dims
+    vox = vt.gen_shapes(dims, 5 + count, count=count, rmin=2.0, rmax=9.0)
+    pal = vt.gen_palette(6)
+    g = vt.Grid.from_u8(vox, pal)
+    try:
+        d, _ = g.bricks()
+        assert ((d >> 31) == 1).any() and (d[(d >> 31) == 1] & 0xFF).max() > 3
+        rng = np.random.default_rng(count)
+        rays = np.concatenate([special_rays(rng, dims, 60000), vt.gen_rays_uniform(dims, count, 60000)])
+        hits, d_rays, d_hits = device_trace(torch, g, rays)
+        og = po.Grid(vox, pal)
+        want = po.trace_rays(og, rays)
+        assert_hits_equal(hits, want, "skipping kernel %r" % (dims,))
+        assert ((hits["face"] & vt.FLAG_HIT) != 0).sum() > 1000
+        vt.trace_rays_stats(g, d_rays, rays.shape[0], d_hits)
+        assert_hits_equal(hits_from_dev(d_hits), want, "counting kernel %r" % (dims,))
+        wd, _, _ = expected_bricks(vox, pal)
+        np.testing.assert_array_equal(d, wd)
     finally:
         g.destroy()

@@ -26,7 +26,6 @@ FACE_MASK = 0x07
 FLAG_SHADOW_RAY = 0x08
 FLAG_INVALID = 0x10
 FLAG_SHADOWED = 0x20
-FLAG_TIE = 0x40
 FLAG_HIT = 0x80
 SKY_RGBA = 0xFFF6E8C0
 PAYLOAD_U8 = 1
@@ -169,12 +168,16 @@ def _ptr(x):
     raise TypeError("expected a pointer, an ndarray or a tensor, got %r" % type(x))
 
 
+CUDA_STREAM_LEGACY = 0x1
+
+
 def _stream(s):
+    """None -> the library's own stream; 0 (the legacy default stream's handle, e.g. torch's
+    default stream) -> cudaStreamLegacy; anything else is passed through."""
     if s is None:
         return None
-    if isinstance(s, int):
-        return s
-    return s.cuda_stream
+    h = s if isinstance(s, int) else s.cuda_stream
+    return h if h != 0 else CUDA_STREAM_LEGACY
 
 
 def init(device=0):

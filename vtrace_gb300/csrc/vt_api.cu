@@ -92,7 +92,7 @@ int32_t check_dims(uint32_t nx, uint32_t ny, uint32_t nz) {
     if (nx > kMaxDim || ny > kMaxDim || nz > kMaxDim)
         return fail(VT_EINVAL, "grid dimension above 65535 (hit records hold 16-bit coordinates)");
     const uint64_t bricks = (uint64_t)((nx + 7) / 8) * ((ny + 7) / 8) * ((nz + 7) / 8);
-    if (bricks > 0xFFFFFFF0ull) return fail(VT_EINVAL, "grid has more than 2^32 bricks");
+    if (bricks > 0x7FFFFFF0ull) return fail(VT_EINVAL, "grid has more than 2^31 bricks");
     return VT_OK;
 }
 
@@ -159,6 +159,8 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
         e = launch_brick_compact(d_src, format, (int32_t)nx, (int32_t)ny, (int32_t)nz, s, g->dir,
                                  g->masks, g->payload, stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick compact kernel"); break; }
+        e = launch_brick_distance(s, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "brick distance kernels"); break; }
         e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick build"); break; }
         g->bytes = g->bricks * 4 + slots * 64 + slots * psize + (g->palette ? 1024 : 0);

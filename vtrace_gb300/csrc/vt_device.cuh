@@ -4,8 +4,9 @@
 // operation in IEEE binary32 round-to-nearest, written with explicit __f*_rn intrinsics so that no
 // multiply-add is ever contracted.  The grid is read through the brick layout built by
 // vt_grid.cu:
-//   dir[brick]            u32 slot of an occupied 8^3 brick, kEmptyBrick otherwise
-//                         (brick = bx + BX * (by + BY * bz), x fastest)
+//   dir[brick]            occupied 8^3 brick: its slot (bit 31 clear); empty brick: kEmptyBit |
+//                         Chebyshev distance in bricks to the nearest occupied brick (>= 1,
+//                         capped at kMaxBrickDistance); brick = bx + BX * (by + BY * bz)
 //   masks[slot * 8 + lz]  u64 occupancy of z-slice lz, bit (ly * 8 + lx)
 //   payload[slot*512+li]  voxel value at li = lx + 8 * (ly + 8 * lz) (u8 index or RGBA8)
 // A voxel is occupied iff its colour's alpha byte is nonzero (trace.frag:78).
@@ -19,7 +20,10 @@
 
 namespace vt {
 
-constexpr uint32_t kEmptyBrick = 0xFFFFFFFFu;
+constexpr uint32_t kEmptyBit = 0x80000000u;
+constexpr uint32_t kMaxBrickDistance = 31;
+
+__device__ __forceinline__ bool brick_empty(uint32_t e) { return (e & kEmptyBit) != 0u; }
 
 struct GridView {
     const uint32_t* dir;
@@ -123,7 +127,7 @@ __device__ __forceinline__ void dda_literal(const GridView& g, int32_t vx, int32
                                          int32_t stx, int32_t sty, int32_t stz, float dlx,
                                          float dly, float dlz, float sx, float sy, float sz,
                                          DDAResult& r, Tally<STATS>& tl) {
-    uint32_t steps = 0, slot = kEmptyBrick;
+    uint32_t steps = 0, slot = kEmptyBit;
     int32_t last = 0;
     bool tie = false, hit = false;
     long long prev = -1;
@@ -133,10 +137,10 @@ __device__ __forceinline__ void dda_literal(const GridView& g, int32_t vx, int32
         slot = __ldg(g.dir + brick);
         if (brick != prev) {
             tl.brick();
-            if (slot != kEmptyBrick) tl.nonempty();
+            if (!brick_empty(slot)) tl.nonempty();
         }
         prev = brick;
-        if (slot != kEmptyBrick) {
+        if (!brick_empty(slot)) {
             tl.tested();
             const uint64_t w = __ldg(g.masks + (size_t)slot * 8 + (vz & 7));
             if ((w >> (((vy & 7) << 3) | (vx & 7))) & 1ull) {
@@ -167,6 +171,23 @@ __device__ __forceinline__ void dda_literal(const GridView& g, int32_t vx, int32
     r.tie = tie;
 }
 
+// One iteration of trace.frag:83-86 on the loop state of dda() / dda_skip(); fminf equals GLSL
+// min here because the fast paths only run when no side distance is NaN.
+#define VT_DDA_STEP                                                          \
+    {                                                                        \
+        const float mnx = fminf(sy, sz), mny = fminf(sz, sx), mnz = fminf(sx, sy); \
+        mx = sx <= mnx;                                                      \
+        my = sy <= mny;                                                      \
+        mz = sz <= mnz;                                                      \
+        if (mx) sx = __fadd_rn(sx, dlx);                                     \
+        if (my) sy = __fadd_rn(sy, dly);                                     \
+        if (mz) sz = __fadd_rn(sz, dlz);                                     \
+        if (mx) vx += stx;                                                   \
+        if (my) vy += sty;                                                   \
+        if (mz) vz += stz;                                                   \
+        ++steps;                                                             \
+    }
+
 // The reference DDA (trace.frag:68-87) from grid-space point (px,py,pz) along (dx,dy,dz).
 //
 // Same voxel sequence, step count and hit as the literal loop; the work is organised by brick:
@@ -190,23 +211,9 @@ __device__ __forceinline__ void dda(const GridView& g, float px, float py, float
     }
     const int32_t vx0 = vx, vy0 = vy, vz0 = vz;
     const uint32_t max_steps = g.max_steps;
-    uint32_t steps = 0, slot = kEmptyBrick;
+    uint32_t steps = 0, slot = kEmptyBit;
     bool mx = false, my = false, mz = false, hit = false;
 
-#define VT_DDA_STEP                                                          \
-    {                                                                        \
-        const float mnx = fminf(sy, sz), mny = fminf(sz, sx), mnz = fminf(sx, sy); \
-        mx = sx <= mnx;                                                      \
-        my = sy <= mny;                                                      \
-        mz = sz <= mnz;                                                      \
-        if (mx) sx = __fadd_rn(sx, dlx);                                     \
-        if (my) sy = __fadd_rn(sy, dly);                                     \
-        if (mz) sz = __fadd_rn(sz, dlz);                                     \
-        if (mx) vx += stx;                                                   \
-        if (my) vy += sty;                                                   \
-        if (mz) vz += stz;                                                   \
-        ++steps;                                                             \
-    }
 
     if (grid_inside(g, vx, vy, vz)) {
         for (;;) {
@@ -217,7 +224,7 @@ __device__ __forceinline__ void dda(const GridView& g, float px, float py, float
             const int32_t ey = sty > 0 ? min((byi << 3) + 8, g.ny) : (sty < 0 ? (byi << 3) - 1 : INT_MIN);
             const int32_t ez = stz > 0 ? min((bzi << 3) + 8, g.nz) : (stz < 0 ? (bzi << 3) - 1 : INT_MIN);
             tl.brick();
-            if (slot == kEmptyBrick) {
+            if (brick_empty(slot)) {
                 do VT_DDA_STEP while (vx != ex && vy != ey && vz != ez && steps < max_steps);
             } else {
                 tl.nonempty();
@@ -237,7 +244,6 @@ __device__ __forceinline__ void dda(const GridView& g, float px, float py, float
             if (steps >= max_steps || !grid_inside(g, vx, vy, vz)) break;
         }
     }
-#undef VT_DDA_STEP
     tl.steps(steps);
     r.vx = vx;
     r.vy = vy;
@@ -249,6 +255,142 @@ __device__ __forceinline__ void dda(const GridView& g, float px, float py, float
     // every iteration advanced at least one axis by one voxel, monotonically: some iteration
     // advanced two or more iff the voxel moves outnumber the iterations
     r.tie = (uint32_t)(abs(vx - vx0) + abs(vy - vy0) + abs(vz - vz0)) != steps;
+}
+
+// Exact value of k successive binary32 additions of d to s (the reference's side += delta
+// recurrence for one axis, trace.frag:84).
+__device__ __forceinline__ float add_chain(float s, float d, int32_t k) {
+#pragma unroll 1
+    for (; k >= 4; k -= 4) {
+        s = __fadd_rn(s, d);
+        s = __fadd_rn(s, d);
+        s = __fadd_rn(s, d);
+        s = __fadd_rn(s, d);
+    }
+#pragma unroll 1
+    for (; k > 0; --k) s = __fadd_rn(s, d);
+    return s;
+}
+
+// Crossing of an empty box of voxels [lo, hi) by the reference DDA, computed per axis.
+//
+// In trace.frag's loop each axis a advances on the iterations where its side distance is the
+// minimum; its values form the sequence S_a(0) = side_a, S_a(k+1) = S_a(k) + delta_a (binary32).
+// Ties merge into one iteration, so after any iteration whose minimum is T every axis b has
+// taken n_b = #{k : S_b(k) <= T} steps.  The box is left on the iteration where some axis takes
+// its N_a-th step (N_a = moves to the box face), i.e. at T* = min_a S_a(N_a - 1).  Nothing in
+// the box is occupied, so that iteration is reached without a hit, and the state after it is:
+// side_b = S_b(n_b), voxel_b += step_b * n_b, and the axes that stepped on it are those whose
+// last processed value equals T*.  S is evaluated with real binary32 additions (add_chain), so
+// the result is bit-identical to iterating, at one addition per axis step instead of a full
+// three-axis iteration.
+__device__ __forceinline__ void cross_empty_axis(float& s, int32_t& v, float delta, int32_t st,
+                                                 int32_t n_exit, float t_exit, float t_star,
+                                                 bool& stepped_last) {
+    if (st == 0) {
+        stepped_last = false;
+        return;
+    }
+    if (t_exit == t_star) {  // this axis leaves the box on the final iteration as well
+        s = __fadd_rn(t_exit, delta);
+        v += st * n_exit;
+        stepped_last = true;
+        return;
+    }
+    if (s > t_star) {  // no step of this axis happens before the box is left
+        stepped_last = false;
+        return;
+    }
+    // 1 <= n < n_exit: start a little below the estimate and finish with exact comparisons
+    int32_t k = (int32_t)__fdividef(__fsub_rn(t_star, s), delta) - 1;
+    k = k < 0 ? 0 : (k > n_exit - 2 ? n_exit - 2 : k);
+    float x = add_chain(s, delta, k);
+    if (x > t_star) {  // the estimate overshot: restart from the first value
+        k = 0;
+        x = s;
+    }
+    float last = x;
+    while (x <= t_star && k < n_exit) {
+        last = x;
+        x = __fadd_rn(x, delta);
+        ++k;
+    }
+    s = x;
+    v += st * k;
+    stepped_last = last == t_star;
+}
+
+// Same result as dda() (hit, voxel, slot, final mask), organised for speed: occupied bricks are
+// walked voxel by voxel against their occupancy bits; an empty brick at Chebyshev distance D from
+// the nearest occupied brick is part of an empty cube of (2D-1)^3 bricks, which the ray crosses
+// in one cross_empty_axis() per axis.  The step count and tie flag of the literal loop are not
+// tracked here (the counting kernels use dda()).
+__device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, float pz,
+                                         float dx, float dy, float dz, DDAResult& r) {
+    const float len = __fsqrt_rn(
+        __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+    int32_t vx, vy, vz, stx, sty, stz;
+    float dlx, dly, dlz, sx, sy, sz;
+    dda_setup_axis(px, dx, g.nx, len, vx, stx, dlx, sx);
+    dda_setup_axis(py, dy, g.ny, len, vy, sty, dly, sy);
+    dda_setup_axis(pz, dz, g.nz, len, vz, stz, dlz, sz);
+    if (isnan(sx) || isnan(sy) || isnan(sz)) {
+        Tally<false> tl;
+        dda_literal<false>(g, vx, vy, vz, stx, sty, stz, dlx, dly, dlz, sx, sy, sz, r, tl);
+        return;
+    }
+    const uint32_t max_steps = g.max_steps;
+    uint32_t steps = 0, slot = kEmptyBit;  // steps: only bounds the occupied-brick loop
+    bool mx = false, my = false, mz = false, hit = false;
+    // every pass of this loop advances at least one axis, monotonically, inside the grid
+    int32_t guard = g.nx + g.ny + g.nz + 2;
+    while (grid_inside(g, vx, vy, vz) && --guard > 0) {
+        const int32_t bxi = vx >> 3, byi = vy >> 3, bzi = vz >> 3;
+        const uint32_t e =
+            __ldg(g.dir + ((size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi)));
+        if (!brick_empty(e)) {
+            slot = e;
+            const uint64_t* mk = g.masks + (size_t)slot * 8;
+            const int32_t ex = stx > 0 ? min((bxi << 3) + 8, g.nx) : (stx < 0 ? (bxi << 3) - 1 : INT_MIN);
+            const int32_t ey = sty > 0 ? min((byi << 3) + 8, g.ny) : (sty < 0 ? (byi << 3) - 1 : INT_MIN);
+            const int32_t ez = stz > 0 ? min((bzi << 3) + 8, g.nz) : (stz < 0 ? (bzi << 3) - 1 : INT_MIN);
+            const uint32_t stop = steps + 24;  // a brick is left within 22 iterations
+            for (;;) {
+                const uint64_t w = __ldg(mk + (vz & 7));
+                if ((w >> (((vy & 7) << 3) | (vx & 7))) & 1ull) {
+                    hit = true;
+                    break;
+                }
+                VT_DDA_STEP
+                if (vx == ex || vy == ey || vz == ez || steps >= stop) break;
+            }
+            if (hit) break;
+        } else {
+            const int32_t D1 = max((int32_t)(e & 0xFFu), 1) - 1;
+            const int32_t lox = max((bxi - D1) << 3, 0), hix = min((bxi + D1 + 1) << 3, g.nx);
+            const int32_t loy = max((byi - D1) << 3, 0), hiy = min((byi + D1 + 1) << 3, g.ny);
+            const int32_t loz = max((bzi - D1) << 3, 0), hiz = min((bzi + D1 + 1) << 3, g.nz);
+            const int32_t nxe = stx > 0 ? hix - vx : vx - lox + 1;
+            const int32_t nye = sty > 0 ? hiy - vy : vy - loy + 1;
+            const int32_t nze = stz > 0 ? hiz - vz : vz - loz + 1;
+            const float tx = stx ? add_chain(sx, dlx, nxe - 1) : INFINITY;
+            const float ty = sty ? add_chain(sy, dly, nye - 1) : INFINITY;
+            const float tz = stz ? add_chain(sz, dlz, nze - 1) : INFINITY;
+            const float ts = fminf(fminf(tx, ty), tz);
+            cross_empty_axis(sx, vx, dlx, stx, nxe, tx, ts, mx);
+            cross_empty_axis(sy, vy, dly, sty, nye, ty, ts, my);
+            cross_empty_axis(sz, vz, dlz, stz, nze, tz, ts, mz);
+        }
+    }
+    (void)max_steps;
+    r.vx = vx;
+    r.vy = vy;
+    r.vz = vz;
+    r.steps = steps;
+    r.slot = slot;
+    r.last = (mx ? 1 : 0) | (my ? 2 : 0) | (mz ? 4 : 0);
+    r.hit = hit;
+    r.tie = false;
 }
 
 // Ray/box entry against [0,nx]x[0,ny]x[0,nz]: 0 = miss, 1 = enters from outside, 2 = origin
@@ -343,13 +485,16 @@ __device__ __forceinline__ HitRec trace_ray(const GridView& g, const float o[3],
     const int kind = slab_entry(g, o, d, pos, t_entry, entry_axis);
     if (kind == 0) return miss_rec(0u, 0u);
     DDAResult r;
-    dda<STATS>(g, pos[0], pos[1], pos[2], d[0], d[1], d[2], r, tl);
-    const uint32_t flags = r.tie ? VT_HIT_FLAG_TIE : 0u;
+    if (STATS)
+        dda<STATS>(g, pos[0], pos[1], pos[2], d[0], d[1], d[2], r, tl);
+    else
+        dda_skip(g, pos[0], pos[1], pos[2], d[0], d[1], d[2], r);
     if (r.tie) tl.tie();
+    const uint32_t flags = 0u;
     if (!r.hit) return miss_rec(flags, 0u);
     uint32_t face = 0;
     float t = 0.0f;
-    if (r.steps > 0) {
+    if (r.last != 0) {  // the ray moved: the face of the final iteration's step
         const int a = (r.last & 1) ? 0 : ((r.last & 2) ? 1 : 2);
         const int32_t va = a == 0 ? r.vx : (a == 1 ? r.vy : r.vz);
         const float da = a == 0 ? d[0] : (a == 1 ? d[1] : d[2]);
@@ -483,3 +628,5 @@ __device__ __forceinline__ HitRec shade_ray(const GridView& g, const LightView& 
 }
 
 }  // namespace vt
+
+#undef VT_DDA_STEP

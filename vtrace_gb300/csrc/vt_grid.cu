@@ -34,7 +34,7 @@ static uint64_t scan_partials(uint64_t n) {
 
 size_t build_scratch_bytes(uint64_t bricks) {
     return (size_t)(align_up(bricks * 64, 256) + align_up(bricks * 4, 256) * 2 +
-                    align_up(scan_partials(bricks) * 4, 256) + 256);
+                    align_up(scan_partials(bricks) * 4, 256) + 256 + align_up(bricks, 256) * 2);
 }
 
 BuildScratch carve_build_scratch(void* base, uint64_t bricks) {
@@ -49,6 +49,10 @@ BuildScratch carve_build_scratch(void* base, uint64_t bricks) {
     s.block_sums = (uint32_t*)p;
     p += align_up(scan_partials(bricks) * 4, 256);
     s.occupied = (unsigned long long*)p;
+    p += 256;
+    s.dist_a = (uint8_t*)p;
+    p += align_up(bricks, 256);
+    s.dist_b = (uint8_t*)p;
     return s;
 }
 
@@ -236,7 +240,7 @@ __global__ void __launch_bounds__(256) brick_compact_kernel(
     if (brick >= bricks) return;
     const uint32_t f = __ldg(flags + brick);
     const uint32_t slot = __ldg(offsets + brick);
-    if (lz == 0) dir[brick] = f ? slot : kEmptyBrick;
+    if (lz == 0) dir[brick] = f ? slot : kEmptyBit;  // distance filled in by the distance passes
     if (!f) return;
     masks[(size_t)slot * 8 + lz] = __ldg(words + brick * 8 + lz);
     const BrickCoord c = brick_coord(brick, bx, by);
@@ -293,6 +297,47 @@ cudaError_t launch_brick_compact(const void* src, uint32_t format, int32_t nx, i
     else
         brick_compact_kernel<VT_PAYLOAD_RGBA8><<<blocks, 256, 0, stream>>>(
             src, nx, ny, nz, bx, by, bricks, s.words, s.flags, s.offsets, dir, masks, payload);
+    return cudaGetLastError();
+}
+
+// Chebyshev (L-infinity) distance, in bricks, from each empty brick to the nearest occupied one,
+// capped at kMaxBrickDistance.  The transform is separable: pass x computes the 1D distance
+// along x; passes y and z take min over the line of max(|offset|, previous pass), which composes
+// max over axes.  Each thread handles one brick and scans a window of +-kMaxBrickDistance.
+template <int AXIS>
+__global__ void __launch_bounds__(256) brick_distance_kernel(uint32_t* __restrict__ dir,
+                                                             const uint8_t* __restrict__ in,
+                                                             uint8_t* __restrict__ out,
+                                                             int32_t bx, int32_t by, int32_t bz,
+                                                             uint64_t bricks) {
+    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= bricks) return;
+    const BrickCoord c = brick_coord(b, bx, by);
+    const int32_t pos = AXIS == 0 ? c.bxi : (AXIS == 1 ? c.byi : c.bzi);
+    const int32_t n = AXIS == 0 ? bx : (AXIS == 1 ? by : bz);
+    const int64_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? (int64_t)bx : (int64_t)bx * by);
+    const int32_t cap = (int32_t)kMaxBrickDistance;
+    const int32_t lo = max(pos - cap, 0), hi = min(pos + cap, n - 1);
+    int32_t best = cap;
+    for (int32_t p = lo; p <= hi; ++p) {
+        const int64_t idx = (int64_t)b + (int64_t)(p - pos) * stride;
+        const int32_t val = AXIS == 0 ? (brick_empty(__ldg(dir + idx)) ? cap : 0) : (int32_t)__ldg(in + idx);
+        best = min(best, max(abs(p - pos), val));
+    }
+    if (AXIS < 2) {
+        out[b] = (uint8_t)best;
+    } else if (brick_empty(dir[b])) {
+        dir[b] = kEmptyBit | (uint32_t)max(best, 1);
+    }
+}
+
+cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,
+                                  int32_t bz, cudaStream_t stream) {
+    const uint64_t bricks = (uint64_t)bx * by * bz;
+    const unsigned blocks = (unsigned)((bricks + 255) / 256);
+    brick_distance_kernel<0><<<blocks, 256, 0, stream>>>(dir, nullptr, s.dist_a, bx, by, bz, bricks);
+    brick_distance_kernel<1><<<blocks, 256, 0, stream>>>(dir, s.dist_a, s.dist_b, bx, by, bz, bricks);
+    brick_distance_kernel<2><<<blocks, 256, 0, stream>>>(dir, s.dist_b, nullptr, bx, by, bz, bricks);
     return cudaGetLastError();
 }
 

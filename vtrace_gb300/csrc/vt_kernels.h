@@ -24,6 +24,8 @@ struct BuildScratch {
     uint32_t* offsets = nullptr;    // bricks: exclusive prefix sum of flags (the slot)
     uint32_t* block_sums = nullptr; // scan partials
     unsigned long long* occupied = nullptr;
+    uint8_t* dist_a = nullptr;      // bricks: distance transform, first pass
+    uint8_t* dist_b = nullptr;      // bricks: distance transform, second pass
 };
 size_t build_scratch_bytes(uint64_t bricks);
 // Carves BuildScratch out of one buffer of build_scratch_bytes(bricks) bytes.
@@ -38,5 +40,9 @@ cudaError_t launch_brick_scan(const BuildScratch& s, uint64_t bricks, cudaStream
 cudaError_t launch_brick_compact(const void* src, uint32_t format, int32_t nx, int32_t ny,
                                  int32_t nz, const BuildScratch& s, uint32_t* dir,
                                  uint64_t* masks, void* payload, cudaStream_t stream);
+
+// Phase 4: Chebyshev distance of every empty brick to the nearest occupied one, into dir.
+cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,
+                                  int32_t bz, cudaStream_t stream);
 
 }  // namespace vt
