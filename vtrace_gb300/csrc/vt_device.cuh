@@ -367,9 +367,9 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
             if (hit) break;
         } else {
             const int32_t D1 = max((int32_t)(e & 0xFFu), 1) - 1;
-            const int32_t lox = max((bxi - D1) << 3, 0), hix = min((bxi + D1 + 1) << 3, g.nx);
-            const int32_t loy = max((byi - D1) << 3, 0), hiy = min((byi + D1 + 1) << 3, g.ny);
-            const int32_t loz = max((bzi - D1) << 3, 0), hiz = min((bzi + D1 + 1) << 3, g.nz);
+            const int32_t lox = max((bxi - D1) * 8, 0), hix = min((bxi + D1 + 1) * 8, g.nx);
+            const int32_t loy = max((byi - D1) * 8, 0), hiy = min((byi + D1 + 1) * 8, g.ny);
+            const int32_t loz = max((bzi - D1) * 8, 0), hiz = min((bzi + D1 + 1) * 8, g.nz);
             const int32_t nxe = stx > 0 ? hix - vx : vx - lox + 1;
             const int32_t nye = sty > 0 ? hiy - vy : vy - loy + 1;
             const int32_t nze = stz > 0 ? hiz - vz : vz - loz + 1;
