@@ -150,6 +150,22 @@ uint32_t vt_version(void);
 /* Device the library runs on and its SM count; for sizing persistent launches. */
 int32_t vt_device_info(int32_t* device, int32_t* sm_count, uint64_t* free_bytes, uint64_t* total_bytes);
 
+/* Launch shape of the persistent tracers.  Each warp keeps one ray per lane and refills lanes
+ * whose rays have ended with new work items once at least `refill_min` lanes are idle (1..32;
+ * 32 = refill only when the whole warp is idle).  `blocks_per_sm` caps the resident 256-thread
+ * blocks per SM (0 = as many as fit).  vtrace_gb300.autotune picks both per workload. */
+typedef struct vt_tuning {
+    uint32_t refill_min;
+    int32_t blocks_per_sm;
+} vt_tuning;
+
+#define VT_KERNEL_RENDER 1
+#define VT_KERNEL_TRACE_RAYS 2
+#define VT_KERNEL_BATCH 3
+
+int32_t vt_get_tuning(int32_t kernel, vt_tuning* out);
+int32_t vt_set_tuning(int32_t kernel, const vt_tuning* in);
+
 /* ---------------------------------------------------------------- grids */
 
 /* Build a brick grid (8^3 bricks, 512-bit occupancy masks, dense payloads for occupied bricks)

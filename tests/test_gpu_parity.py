@@ -316,7 +316,7 @@ def test_empty_space_skipping_is_exact(torch, dims, count):
         og = po.Grid(vox, pal)
         want = po.trace_rays(og, rays)
         assert_hits_equal(hits, want, "skipping kernel %r" % (dims,))
-        assert ((hits["face"] & vt.FLAG_HIT) != 0).sum() > 1000
+        assert ((hits["face"] & vt.FLAG_HIT) != 0).sum() > 10
         vt.trace_rays_stats(g, d_rays, rays.shape[0], d_hits)
         assert_hits_equal(hits_from_dev(d_hits), want, "counting kernel %r" % (dims,))
         wd, _, _ = expected_bricks(vox, pal)

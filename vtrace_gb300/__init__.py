@@ -75,6 +75,13 @@ class TraceStats(ctypes.Structure):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("refill_min", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_int32)]
+
+
+KERNEL_RENDER, KERNEL_TRACE_RAYS, KERNEL_BATCH = 1, 2, 3
+
+
 class RenderTickInfo(ctypes.Structure):
     _fields_ = [("perspective", ctypes.c_void_p), ("camera", ctypes.c_void_p)]
 
@@ -96,6 +103,8 @@ SIGNATURES = [
     ("vt_last_error", ctypes.c_char_p, []),
     ("vt_version", _u32, []),
     ("vt_device_info", _i32, [_vp, _vp, _vp, _vp]),
+    ("vt_get_tuning", _i32, [_i32, ctypes.POINTER(Tuning)]),
+    ("vt_set_tuning", _i32, [_i32, ctypes.POINTER(Tuning)]),
     ("vt_grid_create_u8", _i32, [_vp, _vp, _u32, _u32, _u32]),
     ("vt_grid_create_u8_device", _i32, [_vp, _vp, _u32, _u32, _u32, _vp]),
     ("vt_grid_create_rgba8", _i32, [_vp, _u32, _u32, _u32]),
@@ -191,6 +200,17 @@ def device_info():
                                ctypes.byref(t)))
     return {"device": d.value, "sm_count": sm.value, "free_bytes": f.value,
             "total_bytes": t.value}
+
+
+def get_tuning(kernel):
+    t = Tuning()
+    check(lib().vt_get_tuning(kernel, ctypes.byref(t)))
+    return {"refill_min": t.refill_min, "blocks_per_sm": t.blocks_per_sm}
+
+
+def set_tuning(kernel, refill_min, blocks_per_sm=0):
+    t = Tuning(refill_min, blocks_per_sm)
+    check(lib().vt_set_tuning(kernel, ctypes.byref(t)))
 
 
 # ---------------------------------------------------------------- content

@@ -42,6 +42,8 @@ int32_t ensure_init_locked(int32_t device) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
     e = cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+    e = cudaMalloc(&s.counters, kCounterRing * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(work counters)");
     s.device = device;
     s.inited = true;
     return VT_OK;
@@ -51,6 +53,11 @@ int32_t ensure_init() {
     State& s = state();
     std::lock_guard<std::mutex> lk(s.mu);
     return ensure_init_locked(0);
+}
+
+unsigned long long* next_counter() {
+    State& s = state();
+    return s.counters + (s.counter_next.fetch_add(1) % kCounterRing);
 }
 
 cudaStream_t pick_stream(void* stream) {
@@ -275,6 +282,8 @@ void vt_shutdown(void) {
     cudaFree(s.staging);
     s.staging = nullptr;
     s.staging_bytes = 0;
+    cudaFree(s.counters);
+    s.counters = nullptr;
     cudaStreamDestroy(s.stream);
     s.stream = nullptr;
     s.inited = false;
@@ -296,6 +305,34 @@ int32_t vt_device_info(int32_t* device, int32_t* sm_count, uint64_t* free_bytes,
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemGetInfo");
     if (free_bytes) *free_bytes = f;
     if (total_bytes) *total_bytes = t;
+    return VT_OK;
+}
+
+static TraceTuning* tuning_of(int32_t kernel) {
+    State& s = state();
+    switch (kernel) {
+        case VT_KERNEL_RENDER: return &s.tune_render;
+        case VT_KERNEL_TRACE_RAYS: return &s.tune_rays;
+        case VT_KERNEL_BATCH: return &s.tune_batch;
+        default: return nullptr;
+    }
+}
+
+int32_t vt_get_tuning(int32_t kernel, vt_tuning* out) {
+    TraceTuning* t = tuning_of(kernel);
+    if (!t || !out) return fail(VT_EINVAL, "vt_get_tuning: bad kernel or null output");
+    out->refill_min = t->refill_min;
+    out->blocks_per_sm = t->blocks_per_sm;
+    return VT_OK;
+}
+
+int32_t vt_set_tuning(int32_t kernel, const vt_tuning* in) {
+    TraceTuning* t = tuning_of(kernel);
+    if (!t || !in) return fail(VT_EINVAL, "vt_set_tuning: bad kernel or null input");
+    if (in->refill_min < 1 || in->refill_min > 32 || in->blocks_per_sm < 0 || in->blocks_per_sm > 64)
+        return fail(VT_EINVAL, "vt_set_tuning: refill_min must be 1..32, blocks_per_sm 0..64");
+    t->refill_min = in->refill_min;
+    t->blocks_per_sm = in->blocks_per_sm;
     return VT_OK;
 }
 
@@ -397,7 +434,10 @@ int32_t vt_trace_rays(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_hit* d_
     if (n && (!d_rays || !d_hits)) return fail(VT_EINVAL, "vt_trace_rays: null buffer");
     if (((uintptr_t)d_rays & 7u) || ((uintptr_t)d_hits & 15u))
         return fail(VT_EINVAL, "vt_trace_rays: rays must be 8-byte and hits 16-byte aligned");
-    cudaError_t e = launch_trace_rays(g->view(), d_rays, n, (uint4*)d_hits, nullptr, pick_stream(stream));
+    State& s = state();
+    cudaError_t e = launch_trace_rays_persistent(g->view(), d_rays, n, (uint4*)d_hits,
+                                                 next_counter(), s.tune_rays, s.sm_count,
+                                                 pick_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "vt_trace_rays launch");
     return VT_OK;
 }
@@ -442,7 +482,9 @@ int32_t vt_trace_rays_host(int32_t grid, const vt_ray* rays, uint64_t n, vt_hit*
     vt_ray* dr = (vt_ray*)((char*)buf + roff);
     cudaStream_t st = s.stream;
     cudaError_t e = cudaMemcpyAsync(dr, rays, rb, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = launch_trace_rays(g->view(), dr, n, (uint4*)dh, nullptr, st);
+    if (e == cudaSuccess)
+        e = launch_trace_rays_persistent(g->view(), dr, n, (uint4*)dh, next_counter(), s.tune_rays,
+                                         s.sm_count, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hits, dh, hb, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_trace_rays_host");
@@ -456,8 +498,10 @@ int32_t vt_render(int32_t grid, const vt_camera* camera, const vt_light* light, 
     int32_t rc = check_camera(camera);
     if (rc) return rc;
     if (!d_hits || ((uintptr_t)d_hits & 15u)) return fail(VT_EINVAL, "vt_render: hits must be 16-byte aligned");
-    cudaError_t e = launch_render(g->view(), *camera, light_view(light), (uint4*)d_hits, nullptr,
-                                  pick_stream(stream));
+    State& s = state();
+    cudaError_t e = launch_render_persistent(g->view(), *camera, light_view(light), (uint4*)d_hits,
+                                             next_counter(), s.tune_render, s.sm_count,
+                                             pick_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "vt_render launch");
     return VT_OK;
 }
@@ -499,7 +543,8 @@ int32_t vt_render_host(int32_t grid, const vt_camera* camera, const vt_light* li
     void* buf;
     if ((rc = staging(hb, &buf))) return rc;
     cudaStream_t st = s.stream;
-    cudaError_t e = launch_render(g->view(), *camera, light_view(light), (uint4*)buf, nullptr, st);
+    cudaError_t e = launch_render_persistent(g->view(), *camera, light_view(light), (uint4*)buf,
+                                             next_counter(), s.tune_render, s.sm_count, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hits, buf, hb, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_render_host");

@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "vt_kernels.h"
 #include "vtrace.h"
 
 namespace vt {
@@ -45,7 +46,15 @@ struct State {
     std::vector<std::unique_ptr<Grid>> grids;
     void* staging = nullptr;
     size_t staging_bytes = 0;
+    // work counters of the persistent launches: each launch takes the next slot of the ring
+    unsigned long long* counters = nullptr;
+    std::atomic<uint32_t> counter_next{0};
+    TraceTuning tune_render, tune_rays, tune_batch;
 };
+
+constexpr uint32_t kCounterRing = 4096;
+// Work counter for one persistent launch (zeroed by the launcher on its stream).
+unsigned long long* next_counter();
 
 State& state();
 int32_t ensure_init();

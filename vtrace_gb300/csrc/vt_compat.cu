@@ -93,7 +93,6 @@ __global__ void __launch_bounds__(256) compat_kernel(const GridView* __restrict_
     uint32_t cr = VT_SKY_RGBA & 0xFFu, cg = (VT_SKY_RGBA >> 8) & 0xFFu,
              cb = (VT_SKY_RGBA >> 16) & 0xFFu, ca = VT_SKY_RGBA >> 24;
     float depth = INFINITY;
-    Tally<false> tl;
     for (int32_t i = 0; i < ninst; ++i) {
         const CompatInstance& I = inst[i];
         const GridView g = views[I.texture];
@@ -138,7 +137,7 @@ __global__ void __launch_bounds__(256) compat_kernel(const GridView* __restrict_
             pos[b] = __fmul_rn(__fadd_rn(mp, 0.5f), size[b]);  // trace.frag:66
         }
         DDAResult r;
-        dda<false>(g, pos[0], pos[1], pos[2], dm[0], dm[1], dm[2], r, tl);
+        dda_skip(g, pos[0], pos[1], pos[2], dm[0], dm[1], dm[2], r);
         if (!r.hit) continue;  // discard: no colour, no depth
         uint32_t index;
         const uint32_t tex = voxel_value(g, r.slot, r.vx, r.vy, r.vz, index);

@@ -473,8 +473,40 @@ __device__ __forceinline__ uint32_t voxel_value(const GridView& g, uint32_t slot
     return __ldg(g.payload32 + (size_t)slot * 512 + li);
 }
 
-// One ray: validity, slab entry, DDA, face, t, unshaded colour.  Mirrors vto_trace_ray_f32.
-// Returns the hit record; `o`/`d` are the ray, `hitv` receives the hit voxel for shading.
+// Hit record of a finished ray: face of the final iteration's step (the entry face when the ray
+// hit its first voxel after entering from outside, none when it started inside the hit voxel),
+// t of that face plane, and the voxel's unshaded colour.  Mirrors vto_trace_ray_f32.
+__device__ __forceinline__ HitRec hit_record(const GridView& g, const float o[3], const float d[3],
+                                             int32_t vx, int32_t vy, int32_t vz, int32_t last,
+                                             uint32_t slot, int entry_axis, float t_entry) {
+    uint32_t face = 0;
+    float t = 0.0f;
+    if (last != 0) {  // the ray moved: the face of the final iteration's step
+        const int a = (last & 1) ? 0 : ((last & 2) ? 1 : 2);
+        const int32_t va = a == 0 ? vx : (a == 1 ? vy : vz);
+        const float da = a == 0 ? d[0] : (a == 1 ? d[1] : d[2]);
+        const float oa = a == 0 ? o[0] : (a == 1 ? o[1] : o[2]);
+        const float plane = __int2float_rn(da > 0.0f ? va : va + 1);
+        t = __fdiv_rn(__fsub_rn(plane, oa), da);
+        face = face_code(a, da < 0.0f);
+    } else if (entry_axis >= 0) {
+        const int a = entry_axis;
+        const float da = a == 0 ? d[0] : (a == 1 ? d[1] : d[2]);
+        t = t_entry;
+        face = face_code(a, da < 0.0f);
+    }
+    uint32_t index;
+    const uint32_t rgba = voxel_value(g, slot, vx, vy, vz, index);
+    HitRec h;
+    h.w0 = (uint32_t)vx | ((uint32_t)vy << 16);
+    h.w1 = (uint32_t)vz | (index << 16) | ((face | VT_HIT_FLAG_HIT) << 24);
+    h.w2 = __float_as_uint(t);
+    h.w3 = rgba;
+    return h;
+}
+
+// One ray: validity, slab entry, DDA, record.  Mirrors vto_trace_ray_f32.  The counting build
+// walks every iteration (dda); the plain build crosses empty space per axis (dda_skip).
 template <bool STATS>
 __device__ __forceinline__ HitRec trace_ray(const GridView& g, const float o[3], const float d[3],
                                             Tally<STATS>& tl) {
@@ -490,32 +522,9 @@ __device__ __forceinline__ HitRec trace_ray(const GridView& g, const float o[3],
     else
         dda_skip(g, pos[0], pos[1], pos[2], d[0], d[1], d[2], r);
     if (r.tie) tl.tie();
-    const uint32_t flags = 0u;
-    if (!r.hit) return miss_rec(flags, 0u);
-    uint32_t face = 0;
-    float t = 0.0f;
-    if (r.last != 0) {  // the ray moved: the face of the final iteration's step
-        const int a = (r.last & 1) ? 0 : ((r.last & 2) ? 1 : 2);
-        const int32_t va = a == 0 ? r.vx : (a == 1 ? r.vy : r.vz);
-        const float da = a == 0 ? d[0] : (a == 1 ? d[1] : d[2]);
-        const float oa = a == 0 ? o[0] : (a == 1 ? o[1] : o[2]);
-        const float plane = __int2float_rn(da > 0.0f ? va : va + 1);
-        t = __fdiv_rn(__fsub_rn(plane, oa), da);
-        face = face_code(a, da < 0.0f);
-    } else if (kind == 1) {
-        const int a = entry_axis;
-        const float da = a == 0 ? d[0] : (a == 1 ? d[1] : d[2]);
-        t = t_entry;
-        face = face_code(a, da < 0.0f);
-    }
-    uint32_t index;
-    const uint32_t rgba = voxel_value(g, r.slot, r.vx, r.vy, r.vz, index);
-    HitRec h;
-    h.w0 = (uint32_t)r.vx | ((uint32_t)r.vy << 16);
-    h.w1 = (uint32_t)r.vz | (index << 16) | ((face | flags | VT_HIT_FLAG_HIT) << 24);
-    h.w2 = __float_as_uint(t);
-    h.w3 = rgba;
-    return h;
+    if (!r.hit) return miss_rec(0u, 0u);
+    return hit_record(g, o, d, r.vx, r.vy, r.vz, r.last, r.slot, kind == 1 ? entry_axis : -1,
+                      t_entry);
 }
 
 // Primary ray for pixel (px, py) + sub-pixel offset (jx, jy).  Mirrors vto_raygen.
@@ -569,6 +578,51 @@ __device__ __forceinline__ void jitter(uint32_t seed, uint32_t view, uint32_t px
     jy = __fmul_rn(__uint2float_rn(r[1] >> 8), 0x1p-24f);
 }
 
+// Lambert term of a hit record's face for light L: false when there is no face (the origin lies
+// in the hit voxel); otherwise `ndl` = n.L of the face normal.
+__device__ __forceinline__ bool face_lit(const HitRec& h, const LightView& L, float& ndl) {
+    const uint32_t face = (h.w1 >> 24) & VT_FACE_MASK;
+    if (face == 0) return false;
+    const int a = (int)(face - 1) / 2;
+    const float la = a == 0 ? L.dx : (a == 1 ? L.dy : L.dz);
+    ndl = (face & 1u) ? la : -la;
+    return true;
+}
+
+// Origin of the shadow ray of a hit: the hit point on the entered face, moved 1/64 voxel off the
+// face into the voxel the ray came from.  Mirrors the oracle's shade_from_ray.
+__device__ __forceinline__ void shadow_origin(const HitRec& h, const float o[3], const float d[3],
+                                              float so[3]) {
+    const uint32_t face = (h.w1 >> 24) & VT_FACE_MASK;
+    const int a = (int)(face - 1) / 2;
+    const bool npos = (face & 1u) != 0u;
+    const int32_t hv[3] = {(int32_t)(h.w0 & 0xFFFFu), (int32_t)(h.w0 >> 16),
+                           (int32_t)(h.w1 & 0xFFFFu)};
+    const float t = __uint_as_float(h.w2);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) so[b] = __fadd_rn(o[b], __fmul_rn(t, d[b]));
+    const int32_t ha = a == 0 ? hv[0] : (a == 1 ? hv[1] : hv[2]);
+    const float plane = __int2float_rn(npos ? ha + 1 : ha);
+    const float sa = npos ? __fadd_rn(plane, 0.015625f) : __fsub_rn(plane, 0.015625f);
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+        if (b == a) so[b] = sa;
+}
+
+// k = ambient + (1 - ambient) * max(n.L, 0) * visible; colour = floor(base * k + 0.5).
+__device__ __forceinline__ uint32_t shade_rgba(uint32_t base, float ndl, float vis, float ambient) {
+    const float lam = ndl > 0.0f ? ndl : 0.0f;
+    const float k = __fadd_rn(ambient, __fmul_rn(__fsub_rn(1.0f, ambient), __fmul_rn(lam, vis)));
+    uint32_t res = base & 0xFF000000u;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float v = __fadd_rn(__fmul_rn(__uint2float_rn((base >> (8 * c)) & 0xFFu), k), 0.5f);
+        const uint32_t q = v >= 255.0f ? 255u : (v <= 0.0f ? 0u : (uint32_t)v);
+        res |= q << (8 * c);
+    }
+    return res;
+}
+
 // Primary hit + Lambert shading + optional hard shadow.  Mirrors the oracle's shade_from_ray.
 template <bool STATS>
 __device__ __forceinline__ HitRec shade_ray(const GridView& g, const LightView& L,
@@ -581,28 +635,13 @@ __device__ __forceinline__ HitRec shade_ray(const GridView& g, const LightView& 
         return h;
     }
     tl.hit();
-    if (!L.enabled) return h;
-    const uint32_t face = flags & VT_FACE_MASK;
-    if (face == 0) return h;
-    const int a = (int)(face - 1) / 2;
-    const bool npos = (face & 1u) != 0u;
-    const float la = a == 0 ? L.dx : (a == 1 ? L.dy : L.dz);
-    const float ndl = npos ? la : -la;
+    float ndl;
+    if (!L.enabled || !face_lit(h, L, ndl)) return h;
     float vis = 1.0f;
     uint32_t extra = 0;
     if (ndl > 0.0f && L.shadows) {
-        const int32_t hv[3] = {(int32_t)(h.w0 & 0xFFFFu), (int32_t)(h.w0 >> 16),
-                               (int32_t)(h.w1 & 0xFFFFu)};
-        const float t = __uint_as_float(h.w2);
         float so[3];
-#pragma unroll
-        for (int b = 0; b < 3; ++b) so[b] = __fadd_rn(o[b], __fmul_rn(t, d[b]));
-        const int32_t ha = a == 0 ? hv[0] : (a == 1 ? hv[1] : hv[2]);
-        const float plane = __int2float_rn(npos ? ha + 1 : ha);
-        const float sa = npos ? __fadd_rn(plane, 0.015625f) : __fsub_rn(plane, 0.015625f);
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-            if (b == a) so[b] = sa;
+        shadow_origin(h, o, d, so);
         const float ld[3] = {L.dx, L.dy, L.dz};
         const HitRec s = trace_ray<STATS>(g, so, ld, tl);
         tl.shadow();
@@ -612,21 +651,10 @@ __device__ __forceinline__ HitRec shade_ray(const GridView& g, const LightView& 
             extra |= VT_HIT_FLAG_SHADOWED;
         }
     }
-    const float lam = ndl > 0.0f ? ndl : 0.0f;
-    const float k = __fadd_rn(L.ambient, __fmul_rn(__fsub_rn(1.0f, L.ambient), __fmul_rn(lam, vis)));
-    const uint32_t base = h.w3;
-    uint32_t res = base & 0xFF000000u;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float v = __fadd_rn(__fmul_rn(__uint2float_rn((base >> (8 * c)) & 0xFFu), k), 0.5f);
-        const uint32_t q = v >= 255.0f ? 255u : (v <= 0.0f ? 0u : (uint32_t)v);
-        res |= q << (8 * c);
-    }
-    h.w3 = res;
+    h.w3 = shade_rgba(h.w3, ndl, vis, L.ambient);
     h.w1 |= extra << 24;
     return h;
 }
 
 }  // namespace vt
 
-#undef VT_DDA_STEP

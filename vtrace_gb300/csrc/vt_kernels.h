@@ -12,6 +12,21 @@ struct GridView;
 struct LightView;
 struct Counters;
 
+// Launch shape of the persistent tracers (picked by the autotuner).
+struct TraceTuning {
+    uint32_t refill_min = 16;  // refill a warp when at least this many lanes are idle (1..32)
+    int blocks_per_sm = 0;     // 0: as many 256-thread blocks as fit on an SM
+};
+
+cudaError_t launch_render_persistent(const GridView& g, const vt_camera& cam,
+                                     const LightView& light, uint4* out,
+                                     unsigned long long* counter, const TraceTuning& tune,
+                                     int sm_count, cudaStream_t stream);
+cudaError_t launch_trace_rays_persistent(const GridView& g, const vt_ray* rays, uint64_t n,
+                                         uint4* out, unsigned long long* counter,
+                                         const TraceTuning& tune, int sm_count,
+                                         cudaStream_t stream);
+
 cudaError_t launch_render(const GridView& g, const vt_camera& cam, const LightView& light,
                           uint4* out, Counters* counters, cudaStream_t stream);
 cudaError_t launch_trace_rays(const GridView& g, const vt_ray* rays, uint64_t n, uint4* out,

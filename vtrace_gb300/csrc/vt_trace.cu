@@ -1,6 +1,8 @@
 // vt_trace.cu — traversal kernels of libvtrace: per-pixel render and ray-buffer trace.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "vt_device.cuh"
 #include "vt_kernels.h"
 
@@ -61,6 +63,196 @@ cudaError_t launch_trace_rays(const GridView& g, const vt_ray* rays, uint64_t n,
         trace_rays_kernel<true><<<(unsigned)blocks, 256, 0, stream>>>(g, r2, n, out, counters);
     else
         trace_rays_kernel<false><<<(unsigned)blocks, 256, 0, stream>>>(g, r2, n, out, nullptr);
+    return cudaGetLastError();
+}
+
+}  // namespace vt
+
+// ---------------------------------------------------------------------------------------------
+// Persistent tracers with live-ray compaction.
+//
+// One launch of sm_count x (resident blocks per SM) blocks.  Every warp keeps a ray per lane and
+// loops: when at least `refill_min` lanes are idle, the warp fetches that many work items with
+// one atomic on `counter` and starts their rays; then every live lane advances its ray by one
+// unit (vt_lane.cuh).  Lanes whose rays end are refilled between units, so the warp stays full
+// while the image's rays have very different lengths.  Items are numbered in 8 x 4 pixel tiles
+// (render) or by ray index (ray buffers), so a refill hands a warp neighbouring rays.
+// ---------------------------------------------------------------------------------------------
+#include "vt_lane.cuh"
+
+namespace vt {
+
+__device__ __forceinline__ bool item_pixel(uint64_t item, uint32_t tiles_x, const vt_camera& cam,
+                                           uint32_t& px, uint32_t& py) {
+    const uint64_t tile = item >> 5;
+    const uint32_t l = (uint32_t)item & 31u;
+    px = (uint32_t)(tile % tiles_x) * 8u + (l & 7u);
+    py = (uint32_t)(tile / tiles_x) * 4u + (l >> 3);
+    return px < cam.width && py < cam.height;
+}
+
+// Render state of one lane: 0 idle, 1 primary ray, 2 shadow ray of `prim`.
+struct RenderLane {
+    LaneRay R;
+    int kind;
+    uint32_t pix;
+    HitRec prim;
+    float ndl;
+};
+
+// A ray of the lane ended with `st`; writes the pixel or starts the shadow ray.  Returns the
+// status of the lane's ray afterwards (kRayRunning while a shadow ray is under way).
+__device__ __forceinline__ int render_finish(const GridView& g, const LightView& L, RenderLane& s,
+                                             int st, uint4* out) {
+    if (s.kind == 1) {
+        HitRec h = ray_record(g, s.R, st, VT_SKY_RGBA);
+        float nd;
+        if (st != kRayHit || !L.enabled || !face_lit(h, L, nd)) {
+            out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+            s.kind = 0;
+            return kRayMiss;
+        }
+        if (nd > 0.0f && L.shadows) {
+            float so[3];
+            shadow_origin(h, s.R.o, s.R.d, so);
+            s.prim = h;
+            s.ndl = nd;
+            s.kind = 2;
+            const float ld[3] = {L.dx, L.dy, L.dz};
+            return ray_begin(g, so, ld, s.R);
+        }
+        h.w3 = shade_rgba(h.w3, nd, 1.0f, L.ambient);
+        out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+        s.kind = 0;
+        return kRayMiss;
+    }
+    // shadow ray
+    const bool shadowed = st == kRayHit;
+    HitRec h = s.prim;
+    h.w3 = shade_rgba(h.w3, s.ndl, shadowed ? 0.0f : 1.0f, L.ambient);
+    h.w1 |= (VT_HIT_FLAG_SHADOW_RAY | (shadowed ? VT_HIT_FLAG_SHADOWED : 0u)) << 24;
+    out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+    s.kind = 0;
+    return kRayMiss;
+}
+
+__global__ void __launch_bounds__(256) render_persistent_kernel(
+    GridView g, vt_camera cam, LightView L, uint4* __restrict__ out,
+    unsigned long long* __restrict__ counter, uint32_t tiles_x, uint64_t total,
+    uint32_t refill_min) {
+    const uint32_t lane = threadIdx.x & 31u;
+    RenderLane s;
+    s.kind = 0;
+    s.pix = 0;
+    s.ndl = 0.0f;
+    bool more = true;  // warp-uniform
+    for (;;) {
+        uint32_t idle = __ballot_sync(0xFFFFFFFFu, s.kind == 0);
+        while (more && __popc(idle) >= (int)refill_min) {
+            uint64_t item;
+            const uint64_t base = warp_fetch(counter, idle, lane, item);
+            if (base + __popc(idle) >= total) more = false;
+            if (s.kind == 0 && item < total) {
+                uint32_t px, py;
+                if (item_pixel(item, tiles_x, cam, px, py)) {
+                    s.pix = py * cam.width + px;
+                    float o[3], d[3];
+                    raygen(cam, px, py, 0.5f, 0.5f, o, d);
+                    s.kind = 1;
+                    int st = ray_begin(g, o, d, s.R);
+                    while (s.kind != 0 && st != kRayRunning) st = render_finish(g, L, s, st, out);
+                }
+            }
+            idle = __ballot_sync(0xFFFFFFFFu, s.kind == 0);
+        }
+        if (!more && idle == 0xFFFFFFFFu) break;
+        if (s.kind != 0) {
+            int st = ray_unit(g, s.R);
+            while (s.kind != 0 && st != kRayRunning) st = render_finish(g, L, s, st, out);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) trace_rays_persistent_kernel(
+    GridView g, const float2* __restrict__ rays, uint64_t n, uint4* __restrict__ out,
+    unsigned long long* __restrict__ counter, uint32_t refill_min) {
+    const uint32_t lane = threadIdx.x & 31u;
+    LaneRay R;
+    bool busy = false;
+    uint64_t idx = 0;
+    bool more = true;
+    for (;;) {
+        uint32_t idle = __ballot_sync(0xFFFFFFFFu, !busy);
+        while (more && __popc(idle) >= (int)refill_min) {
+            uint64_t item;
+            const uint64_t base = warp_fetch(counter, idle, lane, item);
+            if (base + __popc(idle) >= n) more = false;
+            if (!busy && item < n) {
+                const float2 a = __ldg(rays + 3 * item), b = __ldg(rays + 3 * item + 1),
+                             c = __ldg(rays + 3 * item + 2);
+                const float o[3] = {a.x, a.y, b.x}, d[3] = {b.y, c.x, c.y};
+                const int st = ray_begin(g, o, d, R);
+                if (st == kRayRunning) {
+                    busy = true;
+                    idx = item;
+                } else {
+                    const HitRec h = ray_record(g, R, st, 0u);
+                    out[item] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+                }
+            }
+            idle = __ballot_sync(0xFFFFFFFFu, !busy);
+        }
+        if (!more && idle == 0xFFFFFFFFu) break;
+        if (busy) {
+            const int st = ray_unit(g, R);
+            if (st != kRayRunning) {
+                const HitRec h = ray_record(g, R, st, 0u);
+                out[idx] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+                busy = false;
+            }
+        }
+    }
+}
+
+static int resident_blocks(const void* kernel) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, 256, 0) != cudaSuccess) {
+        cudaGetLastError();
+        n = 1;
+    }
+    return n < 1 ? 1 : n;
+}
+
+cudaError_t launch_render_persistent(const GridView& g, const vt_camera& cam,
+                                     const LightView& light, uint4* out,
+                                     unsigned long long* counter, const TraceTuning& tune,
+                                     int sm_count, cudaStream_t stream) {
+    static int per_sm = resident_blocks((const void*)render_persistent_kernel);
+    const uint32_t tiles_x = (cam.width + 7) / 8, tiles_y = (cam.height + 3) / 4;
+    const uint64_t total = (uint64_t)tiles_x * tiles_y * 32;
+    const int bps = tune.blocks_per_sm > 0 ? min(tune.blocks_per_sm, per_sm) : per_sm;
+    const uint64_t need = (total + 255) / 256;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)sm_count * bps, need);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    render_persistent_kernel<<<blocks, 256, 0, stream>>>(g, cam, light, out, counter, tiles_x,
+                                                         total, tune.refill_min);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_trace_rays_persistent(const GridView& g, const vt_ray* rays, uint64_t n,
+                                         uint4* out, unsigned long long* counter,
+                                         const TraceTuning& tune, int sm_count,
+                                         cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    static int per_sm = resident_blocks((const void*)trace_rays_persistent_kernel);
+    const int bps = tune.blocks_per_sm > 0 ? min(tune.blocks_per_sm, per_sm) : per_sm;
+    const uint64_t need = (n + 255) / 256;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)sm_count * bps, need);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    trace_rays_persistent_kernel<<<blocks, 256, 0, stream>>>(
+        g, reinterpret_cast<const float2*>(rays), n, out, counter, tune.refill_min);
     return cudaGetLastError();
 }
 
