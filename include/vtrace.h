@@ -150,13 +150,15 @@ uint32_t vt_version(void);
 /* Device the library runs on and its SM count; for sizing persistent launches. */
 int32_t vt_device_info(int32_t* device, int32_t* sm_count, uint64_t* free_bytes, uint64_t* total_bytes);
 
-/* Launch shape of the persistent tracers.  Each warp keeps one ray per lane and refills lanes
- * whose rays have ended with new work items once at least `refill_min` lanes are idle (1..32;
- * 32 = refill only when the whole warp is idle).  `blocks_per_sm` caps the resident 256-thread
- * blocks per SM (0 = as many as fit).  vtrace_gb300.autotune picks both per workload. */
+/* Launch shape of a tracing entry point.  persistent = 0: one thread per ray, rays packed in
+ * 8 x 4 pixel tiles per warp.  persistent = 1: resident warps keep one ray per lane and refill
+ * lanes whose rays have ended with new work once at least `refill_min` lanes are idle (1..32;
+ * 32 = only when the whole warp is idle), with at most `blocks_per_sm` 256-thread blocks per SM
+ * (0 = as many as fit).  vtrace_gb300.autotune picks them per workload. */
 typedef struct vt_tuning {
     uint32_t refill_min;
     int32_t blocks_per_sm;
+    uint32_t persistent;
 } vt_tuning;
 
 #define VT_KERNEL_RENDER 1

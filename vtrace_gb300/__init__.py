@@ -76,7 +76,8 @@ class TraceStats(ctypes.Structure):
 
 
 class Tuning(ctypes.Structure):
-    _fields_ = [("refill_min", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_int32)]
+    _fields_ = [("refill_min", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_int32),
+                ("persistent", ctypes.c_uint32)]
 
 
 KERNEL_RENDER, KERNEL_TRACE_RAYS, KERNEL_BATCH = 1, 2, 3
@@ -205,11 +206,12 @@ def device_info():
 def get_tuning(kernel):
     t = Tuning()
     check(lib().vt_get_tuning(kernel, ctypes.byref(t)))
-    return {"refill_min": t.refill_min, "blocks_per_sm": t.blocks_per_sm}
+    return {"refill_min": t.refill_min, "blocks_per_sm": t.blocks_per_sm,
+            "persistent": t.persistent}
 
 
-def set_tuning(kernel, refill_min, blocks_per_sm=0):
-    t = Tuning(refill_min, blocks_per_sm)
+def set_tuning(kernel, refill_min=16, blocks_per_sm=0, persistent=True):
+    t = Tuning(refill_min, blocks_per_sm, 1 if persistent else 0)
     check(lib().vt_set_tuning(kernel, ctypes.byref(t)))
 
 

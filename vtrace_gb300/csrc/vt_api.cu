@@ -60,6 +60,24 @@ unsigned long long* next_counter() {
     return s.counters + (s.counter_next.fetch_add(1) % kCounterRing);
 }
 
+cudaError_t launch_frame(const GridView& g, const vt_camera& cam, const LightView& light,
+                         uint4* out, cudaStream_t stream) {
+    State& s = state();
+    if (s.tune_render.persistent)
+        return launch_render_persistent(g, cam, light, out, next_counter(), s.tune_render,
+                                        s.sm_count, stream);
+    return launch_render(g, cam, light, out, nullptr, stream);
+}
+
+cudaError_t launch_rays(const GridView& g, const vt_ray* rays, uint64_t n, uint4* out,
+                        cudaStream_t stream) {
+    State& s = state();
+    if (s.tune_rays.persistent)
+        return launch_trace_rays_persistent(g, rays, n, out, next_counter(), s.tune_rays,
+                                            s.sm_count, stream);
+    return launch_trace_rays(g, rays, n, out, nullptr, stream);
+}
+
 cudaStream_t pick_stream(void* stream) {
     return stream ? (cudaStream_t)stream : state().stream;
 }
@@ -323,6 +341,7 @@ int32_t vt_get_tuning(int32_t kernel, vt_tuning* out) {
     if (!t || !out) return fail(VT_EINVAL, "vt_get_tuning: bad kernel or null output");
     out->refill_min = t->refill_min;
     out->blocks_per_sm = t->blocks_per_sm;
+    out->persistent = t->persistent;
     return VT_OK;
 }
 
@@ -333,6 +352,7 @@ int32_t vt_set_tuning(int32_t kernel, const vt_tuning* in) {
         return fail(VT_EINVAL, "vt_set_tuning: refill_min must be 1..32, blocks_per_sm 0..64");
     t->refill_min = in->refill_min;
     t->blocks_per_sm = in->blocks_per_sm;
+    t->persistent = in->persistent ? 1u : 0u;
     return VT_OK;
 }
 
@@ -434,10 +454,7 @@ int32_t vt_trace_rays(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_hit* d_
     if (n && (!d_rays || !d_hits)) return fail(VT_EINVAL, "vt_trace_rays: null buffer");
     if (((uintptr_t)d_rays & 7u) || ((uintptr_t)d_hits & 15u))
         return fail(VT_EINVAL, "vt_trace_rays: rays must be 8-byte and hits 16-byte aligned");
-    State& s = state();
-    cudaError_t e = launch_trace_rays_persistent(g->view(), d_rays, n, (uint4*)d_hits,
-                                                 next_counter(), s.tune_rays, s.sm_count,
-                                                 pick_stream(stream));
+    cudaError_t e = launch_rays(g->view(), d_rays, n, (uint4*)d_hits, pick_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "vt_trace_rays launch");
     return VT_OK;
 }
@@ -482,9 +499,7 @@ int32_t vt_trace_rays_host(int32_t grid, const vt_ray* rays, uint64_t n, vt_hit*
     vt_ray* dr = (vt_ray*)((char*)buf + roff);
     cudaStream_t st = s.stream;
     cudaError_t e = cudaMemcpyAsync(dr, rays, rb, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-        e = launch_trace_rays_persistent(g->view(), dr, n, (uint4*)dh, next_counter(), s.tune_rays,
-                                         s.sm_count, st);
+    if (e == cudaSuccess) e = launch_rays(g->view(), dr, n, (uint4*)dh, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hits, dh, hb, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_trace_rays_host");
@@ -498,10 +513,8 @@ int32_t vt_render(int32_t grid, const vt_camera* camera, const vt_light* light, 
     int32_t rc = check_camera(camera);
     if (rc) return rc;
     if (!d_hits || ((uintptr_t)d_hits & 15u)) return fail(VT_EINVAL, "vt_render: hits must be 16-byte aligned");
-    State& s = state();
-    cudaError_t e = launch_render_persistent(g->view(), *camera, light_view(light), (uint4*)d_hits,
-                                             next_counter(), s.tune_render, s.sm_count,
-                                             pick_stream(stream));
+    cudaError_t e = launch_frame(g->view(), *camera, light_view(light), (uint4*)d_hits,
+                                 pick_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "vt_render launch");
     return VT_OK;
 }
@@ -543,8 +556,7 @@ int32_t vt_render_host(int32_t grid, const vt_camera* camera, const vt_light* li
     void* buf;
     if ((rc = staging(hb, &buf))) return rc;
     cudaStream_t st = s.stream;
-    cudaError_t e = launch_render_persistent(g->view(), *camera, light_view(light), (uint4*)buf,
-                                             next_counter(), s.tune_render, s.sm_count, st);
+    cudaError_t e = launch_frame(g->view(), *camera, light_view(light), (uint4*)buf, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hits, buf, hb, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_render_host");

@@ -49,12 +49,20 @@ struct State {
     // work counters of the persistent launches: each launch takes the next slot of the ring
     unsigned long long* counters = nullptr;
     std::atomic<uint32_t> counter_next{0};
-    TraceTuning tune_render, tune_rays, tune_batch;
+    // defaults from sweeps on GB300: coherent camera rays keep their 8 x 4 tiles (refills would
+    // mix tiles), incoherent ray buffers refill a warp once 8 lanes are idle
+    TraceTuning tune_render{16, 0, 0}, tune_rays{8, 0, 1}, tune_batch{16, 0, 0};
 };
 
 constexpr uint32_t kCounterRing = 4096;
 // Work counter for one persistent launch (zeroed by the launcher on its stream).
 unsigned long long* next_counter();
+
+// The timed launches of vt_render / vt_trace_rays, in the shape the current tuning selects.
+cudaError_t launch_frame(const GridView& g, const vt_camera& cam, const LightView& light,
+                         uint4* out, cudaStream_t stream);
+cudaError_t launch_rays(const GridView& g, const vt_ray* rays, uint64_t n, uint4* out,
+                        cudaStream_t stream);
 
 State& state();
 int32_t ensure_init();

@@ -272,7 +272,34 @@ __device__ __forceinline__ float add_chain(float s, float d, int32_t k) {
     return s;
 }
 
-// Crossing of an empty box of voxels [lo, hi) by the reference DDA, computed per axis.
+// Number of an axis's events S(k) <= t_star among k < n_exit, with S(k) evaluated exactly; the
+// axis is known not to reach its exit (S(n_exit - 1) > t_star).  Starts from the estimate
+// floor((t_star - s) / delta) and settles it with exact additions and comparisons.
+__device__ __forceinline__ void advance_axis(float& s, int32_t& v, float delta, int32_t st,
+                                             int32_t n_exit, float t_star, bool& stepped_last) {
+    if (st == 0 || s > t_star) {
+        stepped_last = false;
+        return;
+    }
+    int32_t k = (int32_t)__fdividef(__fsub_rn(t_star, s), delta);
+    k = k < 0 ? 0 : (k > n_exit - 2 ? n_exit - 2 : k);
+    float x = add_chain(s, delta, k);  // S(k)
+    if (x > t_star) {                  // the estimate overshot: walk up from S(0)
+        k = 0;
+        x = s;
+    }
+    float y = __fadd_rn(x, delta);  // S(k + 1)
+    while (y <= t_star && k + 1 < n_exit) {
+        x = y;
+        y = __fadd_rn(y, delta);
+        ++k;
+    }
+    s = y;
+    v += st * (k + 1);
+    stepped_last = x == t_star;
+}
+
+// Crossing of an empty box of voxels by the reference DDA, computed per axis.
 //
 // In trace.frag's loop each axis a advances on the iterations where its side distance is the
 // minimum; its values form the sequence S_a(0) = side_a, S_a(k+1) = S_a(k) + delta_a (binary32).
@@ -281,49 +308,61 @@ __device__ __forceinline__ float add_chain(float s, float d, int32_t k) {
 // its N_a-th step (N_a = moves to the box face), i.e. at T* = min_a S_a(N_a - 1).  Nothing in
 // the box is occupied, so that iteration is reached without a hit, and the state after it is:
 // side_b = S_b(n_b), voxel_b += step_b * n_b, and the axes that stepped on it are those whose
-// last processed value equals T*.  S is evaluated with real binary32 additions (add_chain), so
-// the result is bit-identical to iterating, at one addition per axis step instead of a full
-// three-axis iteration.
-__device__ __forceinline__ void cross_empty_axis(float& s, int32_t& v, float delta, int32_t st,
-                                                 int32_t n_exit, float t_exit, float t_star,
-                                                 bool& stepped_last) {
-    if (st == 0) {
-        stepped_last = false;
-        return;
+// last processed value equals T*.
+//
+// Only the axes that can leave first need their exit value S_a(N_a - 1) exactly: the
+// approximation s + (N-1) * delta is within (N + 2) * 2^-24 of the exact chain relative to its
+// magnitude, so any axis whose approximation exceeds the smallest by more than the sum of both
+// bounds (taken 4x larger here) cannot be the minimum.  Every value compared is computed with
+// real binary32 additions, so the result is bit-identical to iterating the reference loop.
+__device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, int32_t& vx,
+                                             int32_t& vy, int32_t& vz, float dlx, float dly,
+                                             float dlz, int32_t stx, int32_t sty, int32_t stz,
+                                             int32_t nxe, int32_t nye, int32_t nze, bool& mx,
+                                             bool& my, bool& mz) {
+    const float ax = stx ? __fadd_rn(sx, __fmul_rn(__int2float_rn(nxe - 1), dlx)) : INFINITY;
+    const float ay = sty ? __fadd_rn(sy, __fmul_rn(__int2float_rn(nye - 1), dly)) : INFINITY;
+    const float az = stz ? __fadd_rn(sz, __fmul_rn(__int2float_rn(nze - 1), dlz)) : INFINITY;
+    const float ex = __fmul_rn(__fmul_rn(__int2float_rn(nxe + 2), ax), 0x1p-22f);
+    const float ey = __fmul_rn(__fmul_rn(__int2float_rn(nye + 2), ay), 0x1p-22f);
+    const float ez = __fmul_rn(__fmul_rn(__int2float_rn(nze + 2), az), 0x1p-22f);
+    // candidate leaving axis and its error bound
+    const float amin = fminf(fminf(ax, ay), az);
+    const float emin = amin == ax ? ex : (amin == ay ? ey : ez);
+    const bool cx = stx && ax <= __fadd_rn(amin, __fadd_rn(emin, ex));
+    const bool cy = sty && ay <= __fadd_rn(amin, __fadd_rn(emin, ey));
+    const bool cz = stz && az <= __fadd_rn(amin, __fadd_rn(emin, ez));
+    const float tx = cx ? add_chain(sx, dlx, nxe - 1) : INFINITY;
+    const float ty = cy ? add_chain(sy, dly, nye - 1) : INFINITY;
+    const float tz = cz ? add_chain(sz, dlz, nze - 1) : INFINITY;
+    const float ts = fminf(fminf(tx, ty), tz);
+    if (cx && tx == ts) {
+        sx = __fadd_rn(tx, dlx);
+        vx += stx * nxe;
+        mx = true;
+    } else {
+        advance_axis(sx, vx, dlx, stx, nxe, ts, mx);
     }
-    if (t_exit == t_star) {  // this axis leaves the box on the final iteration as well
-        s = __fadd_rn(t_exit, delta);
-        v += st * n_exit;
-        stepped_last = true;
-        return;
+    if (cy && ty == ts) {
+        sy = __fadd_rn(ty, dly);
+        vy += sty * nye;
+        my = true;
+    } else {
+        advance_axis(sy, vy, dly, sty, nye, ts, my);
     }
-    if (s > t_star) {  // no step of this axis happens before the box is left
-        stepped_last = false;
-        return;
+    if (cz && tz == ts) {
+        sz = __fadd_rn(tz, dlz);
+        vz += stz * nze;
+        mz = true;
+    } else {
+        advance_axis(sz, vz, dlz, stz, nze, ts, mz);
     }
-    // 1 <= n < n_exit: start a little below the estimate and finish with exact comparisons
-    int32_t k = (int32_t)__fdividef(__fsub_rn(t_star, s), delta) - 1;
-    k = k < 0 ? 0 : (k > n_exit - 2 ? n_exit - 2 : k);
-    float x = add_chain(s, delta, k);
-    if (x > t_star) {  // the estimate overshot: restart from the first value
-        k = 0;
-        x = s;
-    }
-    float last = x;
-    while (x <= t_star && k < n_exit) {
-        last = x;
-        x = __fadd_rn(x, delta);
-        ++k;
-    }
-    s = x;
-    v += st * k;
-    stepped_last = last == t_star;
 }
 
 // Same result as dda() (hit, voxel, slot, final mask), organised for speed: occupied bricks are
 // walked voxel by voxel against their occupancy bits; an empty brick at Chebyshev distance D from
 // the nearest occupied brick is part of an empty cube of (2D-1)^3 bricks, which the ray crosses
-// in one cross_empty_axis() per axis.  The step count and tie flag of the literal loop are not
+// in one cross_region().  The step count and tie flag of the literal loop are not
 // tracked here (the counting kernels use dda()).
 __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, float pz,
                                          float dx, float dy, float dz, DDAResult& r) {
@@ -373,13 +412,8 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
             const int32_t nxe = stx > 0 ? hix - vx : vx - lox + 1;
             const int32_t nye = sty > 0 ? hiy - vy : vy - loy + 1;
             const int32_t nze = stz > 0 ? hiz - vz : vz - loz + 1;
-            const float tx = stx ? add_chain(sx, dlx, nxe - 1) : INFINITY;
-            const float ty = sty ? add_chain(sy, dly, nye - 1) : INFINITY;
-            const float tz = stz ? add_chain(sz, dlz, nze - 1) : INFINITY;
-            const float ts = fminf(fminf(tx, ty), tz);
-            cross_empty_axis(sx, vx, dlx, stx, nxe, tx, ts, mx);
-            cross_empty_axis(sy, vy, dly, sty, nye, ty, ts, my);
-            cross_empty_axis(sz, vz, dlz, stz, nze, tz, ts, mz);
+            cross_region(sx, sy, sz, vx, vy, vz, dlx, dly, dlz, stx, sty, stz, nxe, nye, nze, mx,
+                         my, mz);
         }
     }
     (void)max_steps;

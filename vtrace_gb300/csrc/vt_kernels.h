@@ -16,6 +16,7 @@ struct Counters;
 struct TraceTuning {
     uint32_t refill_min = 16;  // refill a warp when at least this many lanes are idle (1..32)
     int blocks_per_sm = 0;     // 0: as many 256-thread blocks as fit on an SM
+    uint32_t persistent = 1;   // 0: one thread per ray in 8 x 4 pixel tiles, no refill
 };
 
 cudaError_t launch_render_persistent(const GridView& g, const vt_camera& cam,

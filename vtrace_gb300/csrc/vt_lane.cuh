@@ -2,7 +2,7 @@
 //
 // A persistent warp keeps one ray per lane.  Each pass of its loop advances every live lane by
 // one unit of traversal — one occupied brick walked voxel by voxel, or one empty region crossed
-// per axis (cross_empty_axis) — so lanes whose rays end can be refilled with new rays between
+// per axis (cross_region) — so lanes whose rays end can be refilled with new rays between
 // units instead of idling until the longest ray of the warp is done.  The units are the loop
 // body of dda_skip(), split so that the loop state lives in LaneRay; results are identical.
 #pragma once
@@ -106,13 +106,8 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
         const int32_t nxe = stx > 0 ? hix - vx : vx - lox + 1;
         const int32_t nye = sty > 0 ? hiy - vy : vy - loy + 1;
         const int32_t nze = stz > 0 ? hiz - vz : vz - loz + 1;
-        const float tx = stx ? add_chain(sx, dlx, nxe - 1) : INFINITY;
-        const float ty = sty ? add_chain(sy, dly, nye - 1) : INFINITY;
-        const float tz = stz ? add_chain(sz, dlz, nze - 1) : INFINITY;
-        const float ts = fminf(fminf(tx, ty), tz);
-        cross_empty_axis(sx, vx, dlx, stx, nxe, tx, ts, mx);
-        cross_empty_axis(sy, vy, dly, sty, nye, ty, ts, my);
-        cross_empty_axis(sz, vz, dlz, stz, nze, tz, ts, mz);
+        cross_region(sx, sy, sz, vx, vy, vz, dlx, dly, dlz, stx, sty, stz, nxe, nye, nze, mx, my,
+                     mz);
     }
     if (status == kRayRunning && (!grid_inside(g, vx, vy, vz) || --R.guard <= 0)) status = kRayMiss;
     R.vx = vx;
