@@ -184,6 +184,25 @@ int32_t vt_grid_create_u8_device(const uint8_t* d_voxels, const uint32_t* palett
  * add_texture (lib/memory.c:286-385).  Occupied iff alpha > 0. */
 int32_t vt_grid_create_rgba8(const uint8_t* rgba, uint32_t nx, uint32_t ny, uint32_t nz);
 int32_t vt_grid_destroy(int32_t grid);
+/* No counterpart in the reference.  Builds the brick layout of an x-fastest u8 grid into buffers
+ * the caller owns, allocating nothing, for callers that cannot allocate device memory while they
+ * run (a pager rebuilding chunks inside a real-time frame loop, where cudaMalloc/cudaFree would
+ * synchronise the device; code recording into a captured stream; a fixed memory budget).
+ * All pointers are device memory: d_voxels (nx*ny*nz bytes), d_palette (256 RGBA8),
+ * d_directory (one u32 per brick), d_masks (8 u64 per brick) and d_payload (512 bytes per brick)
+ * sized for every brick of the grid, and d_counts (2 u64: occupied bricks, occupied voxels).
+ * Outputs have the layout of vt_grid_download_bricks; payload slot s holds voxel values at
+ * lx + 8*(ly + 8*lz).  The build's scratch is a 2.5 MiB static device array: grids of at most
+ * 32768 bricks (e.g. 256^3 voxels) are accepted, larger ones return VT_ELIMIT.  Every call
+ * shares that array, so calls whose work overlaps on the GPU (different streams) race; serialise
+ * them on one stream.  Asynchronous on `stream` (NULL = the legacy default stream); the first call
+ * on each device looks up the array's device address and should come before any stream capture.
+ * Returns VT_OK, VT_EINVAL (null or misaligned pointer, bad size), VT_ELIMIT or VT_ECUDA; it
+ * does not set vt_last_error. */
+int32_t vt_grid_build_u8_noalloc(const uint8_t* d_voxels, const uint32_t* d_palette,
+                                 uint32_t nx, uint32_t ny, uint32_t nz, uint32_t* d_directory,
+                                 uint64_t* d_masks, uint8_t* d_payload, uint64_t* d_counts,
+                                 void* stream);
 int32_t vt_grid_get_info(int32_t grid, vt_grid_info* info);
 /* Copy the grid's brick directory and occupancy masks to host memory; either may be NULL.
  * directory: bricks_total u32, x-fastest over bricks; an occupied brick's entry is its slot

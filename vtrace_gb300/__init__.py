@@ -110,6 +110,7 @@ SIGNATURES = [
     ("vt_grid_create_u8_device", _i32, [_vp, _vp, _u32, _u32, _u32, _vp]),
     ("vt_grid_create_rgba8", _i32, [_vp, _u32, _u32, _u32]),
     ("vt_grid_destroy", _i32, [_i32]),
+    ("vt_grid_build_u8_noalloc", _i32, [_vp, _vp, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp]),
     ("vt_grid_get_info", _i32, [_i32, ctypes.POINTER(GridInfo)]),
     ("vt_grid_download_bricks", _i32, [_i32, _vp, _vp]),
     ("vt_trace_rays", _i32, [_i32, _vp, _u64, _vp, _vp]),
