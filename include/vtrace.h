@@ -239,6 +239,39 @@ int32_t vt_trace_rays_stats(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_h
 int32_t vt_camera_look_at(const float eye[3], const float target[3], const float up[3],
                           float vfov_degrees, uint32_t width, uint32_t height, vt_camera* out);
 
+/* ---------------------------------------------------------------- batched multi-view */
+
+/* One view of a batch: a camera over a grid with `spp` jittered samples per pixel.  Sample s of
+ * pixel (px, py) uses the sub-pixel offset Philox4x32-10(counter = {px, py, s, view_id},
+ * key = {seed, 0x56544752}) words 0 and 1, each >> 8 and scaled by 2^-24, and is written to
+ * d_out[(py * width + px) * spp + s] (device memory, 16-byte aligned).  The light is used when
+ * flags & VT_VIEW_LIGHT. */
+typedef struct vt_view {
+    int32_t grid;
+    uint32_t spp;
+    uint32_t seed;
+    uint32_t view_id;
+    uint32_t flags;
+    vt_camera camera;
+    vt_light light;
+    vt_hit* d_out;
+} vt_view;
+
+#define VT_VIEW_LIGHT 1u
+
+/* Build a batch of up to 256 views: one persistent work-stealing launch over all their samples
+ * (uneven sizes are balanced by dynamic fetching), captured once into a CUDA graph.  The grids
+ * stay referenced (vt_grid_destroy returns VT_EBUSY) until vt_batch_destroy.  The launch shape
+ * is the VT_KERNEL_BATCH tuning at creation time. */
+int32_t vt_batch_create(const vt_view* views, uint32_t n, int32_t* batch_out);
+/* Replay the batch's graph on `stream` (asynchronous). */
+int32_t vt_batch_run(int32_t batch, void* stream);
+/* The same launch without the graph (for comparison and for streams that cannot take graphs). */
+int32_t vt_batch_run_direct(int32_t batch, void* stream);
+/* Primary rays (sum of width * height * spp) and work items of a batch. */
+int32_t vt_batch_info(int32_t batch, uint64_t* primary_rays, uint64_t* work_items);
+int32_t vt_batch_destroy(int32_t batch);
+
 /* ---------------------------------------------------------------- scene generators (host) */
 
 /* Seeded synthetic content, deterministic across platforms (integer hashing and IEEE binary32

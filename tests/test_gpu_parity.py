@@ -345,3 +345,38 @@ def test_launch_shapes_agree(torch, persistent, refill_min):
         for k, t in saved.items():
             vt.set_tuning(k, t["refill_min"], t["blocks_per_sm"], t["persistent"])
         g.destroy()
+
+
+def test_batched_multiview_matches_oracle(torch):
+    """A small batch of uneven views over several grids, replayed from its CUDA graph twice and
+    launched directly once, against the oracle's jittered per-view render."""
+    scenes, views = workloads.multiview(n_scenes=3, n_views=7, sizes=(64, 96, 48),
+                                        min_px=40 * 30, max_px=200 * 150)
+    grids = [vt.Grid.from_u8(s["voxels"], s["palette"]) for s in scenes]
+    try:
+        outs, specs = [], []
+        for v in views:
+            c = v["camera"]
+            buf = torch.zeros(c.width * c.height * v["spp"] * 16, dtype=torch.uint8, device="cuda")
+            outs.append(buf)
+            specs.append(vt.make_view(grids[v["scene"]], c, buf, v["spp"], v["seed"],
+                                      v["view_id"], v["light"]))
+        b = vt.Batch(specs)
+        with pytest.raises(vt.VtError):
+            grids[0].destroy()  # referenced by the batch
+        ogrids = [po.Grid(s["voxels"], s["palette"]) for s in scenes]
+        for run in range(3):
+            for o in outs:
+                o.zero_()
+            b.run(graph=run < 2)
+            torch.cuda.synchronize()
+            for v, o in zip(views, outs):
+                want = po.render_view(ogrids[v["scene"]], oracle_camera(v["camera"]),
+                                      oracle_light(v["light"]), v["spp"], v["seed"], v["view_id"])
+                assert_hits_equal(hits_from_dev(o), want, "batch view %d run %d" % (v["view_id"], run))
+        assert b.primary_rays == sum(v["camera"].width * v["camera"].height * v["spp"] for v in views)
+        b.destroy()
+    finally:
+        for g in grids:
+            if g.id is not None:
+                g.destroy()

@@ -83,6 +83,15 @@ class Tuning(ctypes.Structure):
 KERNEL_RENDER, KERNEL_TRACE_RAYS, KERNEL_BATCH = 1, 2, 3
 
 
+class View(ctypes.Structure):
+    _fields_ = [("grid", ctypes.c_int32), ("spp", ctypes.c_uint32), ("seed", ctypes.c_uint32),
+                ("view_id", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("camera", Camera),
+                ("light", Light), ("d_out", ctypes.c_void_p)]
+
+
+VIEW_LIGHT = 1
+
+
 class RenderTickInfo(ctypes.Structure):
     _fields_ = [("perspective", ctypes.c_void_p), ("camera", ctypes.c_void_p)]
 
@@ -120,6 +129,11 @@ SIGNATURES = [
     ("vt_render_stats", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp,
                                ctypes.POINTER(TraceStats)]),
     ("vt_trace_rays_stats", _i32, [_i32, _vp, _u64, _vp, ctypes.POINTER(TraceStats)]),
+    ("vt_batch_create", _i32, [ctypes.POINTER(View), _u32, ctypes.POINTER(ctypes.c_int32)]),
+    ("vt_batch_run", _i32, [_i32, _vp]),
+    ("vt_batch_run_direct", _i32, [_i32, _vp]),
+    ("vt_batch_info", _i32, [_i32, _vp, _vp]),
+    ("vt_batch_destroy", _i32, [_i32]),
     ("vt_camera_look_at", _i32, [_vp, _vp, _vp, _f32, _u32, _u32, ctypes.POINTER(Camera)]),
     ("vt_gen_palette", _i32, [_u32, _vp]),
     ("vt_gen_terrain", _i32, [_u32, _u32, _u32, _u32, _u32, _f32, _vp]),
@@ -367,3 +381,40 @@ def render_stats(grid, camera, light, d_hits):
                                 ctypes.byref(light) if light is not None else None,
                                 _ptr(d_hits), ctypes.byref(st)))
     return st.as_dict()
+
+
+# ---------------------------------------------------------------- batched multi-view
+
+class Batch:
+    """Many views (grid, camera, spp, light, device output) rendered by one persistent launch
+    replayed from a captured CUDA graph."""
+
+    def __init__(self, views):
+        arr = (View * len(views))(*views)
+        bid = ctypes.c_int32(-1)
+        check(lib().vt_batch_create(arr, len(views), ctypes.byref(bid)))
+        self.id = bid.value
+        p, w = ctypes.c_uint64(), ctypes.c_uint64()
+        check(lib().vt_batch_info(self.id, ctypes.byref(p), ctypes.byref(w)))
+        self.primary_rays, self.work_items = p.value, w.value
+
+    def run(self, stream=None, graph=True):
+        f = lib().vt_batch_run if graph else lib().vt_batch_run_direct
+        check(f(self.id, _stream(stream)))
+
+    def destroy(self):
+        if self.id is not None:
+            check(lib().vt_batch_destroy(self.id))
+            self.id = None
+
+
+def make_view(grid, camera, d_out, spp=1, seed=0, view_id=0, light=None):
+    v = View()
+    v.grid = grid.id if isinstance(grid, Grid) else int(grid)
+    v.spp, v.seed, v.view_id = spp, seed, view_id
+    v.flags = VIEW_LIGHT if light is not None else 0
+    v.camera = camera
+    if light is not None:
+        v.light = light
+    v.d_out = _ptr(d_out)
+    return v

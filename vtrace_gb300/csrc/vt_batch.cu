@@ -1,4 +1,337 @@
-// vt_batch.cu — batched multi-view rendering (persistent work-stealing kernel, CUDA graph).
-#include "vt_api_internal.h"
+// vt_batch.cu — batched multi-view rendering: many cameras over many grids, uneven image sizes
+// and sample counts, in one persistent work-stealing launch replayed from a captured CUDA graph.
+//
+// A batch flattens all its views into one item space: view v owns items [begin_v, begin_v +
+// tiles_v * spp_v * 32), item = ((tile * spp + sample) * 32 + lane-in-tile), so a warp refill
+// hands out neighbouring pixels of one tile and one sample.  Resident warps fetch items with one
+// atomic per refill (vt_lane.cuh), find the item's view by binary search over the view table
+// (held in shared memory), and trace it with the view's grid, camera and light.  Samples are
+// jittered with Philox4x32-10 keyed by (seed, view id, pixel, sample), the same jitter the
+// oracle uses.  The launch — counter reset plus kernel — is captured once into a CUDA graph at
+// vt_batch_create and replayed by vt_batch_run.
+#include <cuda_runtime.h>
 
-void vt_batch_release_all() {}
+#include <algorithm>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "vt_api_internal.h"
+#include "vt_device.cuh"
+#include "vt_internal.h"
+#include "vt_lane.cuh"
+
+namespace vt {
+
+constexpr uint32_t kMaxBatchViews = 256;
+
+struct BatchView {
+    GridView g;
+    vt_camera cam;
+    LightView light;
+    uint4* out;
+    unsigned long long begin;  // first item of the view
+    uint32_t tiles_x;
+    uint32_t spp;
+    uint32_t seed;
+    uint32_t view_id;
+};
+
+struct BatchLane {
+    LaneRay R;
+    int kind;
+    uint32_t pix;
+    HitRec prim;
+    float ndl;
+    uint32_t view;
+};
+
+__device__ __forceinline__ int batch_finish(const BatchView& V, BatchLane& s, int st) {
+    if (s.kind == 1) {
+        HitRec h = ray_record(V.g, s.R, st, VT_SKY_RGBA);
+        float nd;
+        if (st != kRayHit || !V.light.enabled || !face_lit(h, V.light, nd)) {
+            V.out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+            s.kind = 0;
+            return kRayMiss;
+        }
+        if (nd > 0.0f && V.light.shadows) {
+            float so[3];
+            shadow_origin(h, s.R.o, s.R.d, so);
+            s.prim = h;
+            s.ndl = nd;
+            s.kind = 2;
+            const float ld[3] = {V.light.dx, V.light.dy, V.light.dz};
+            return ray_begin(V.g, so, ld, s.R);
+        }
+        h.w3 = shade_rgba(h.w3, nd, 1.0f, V.light.ambient);
+        V.out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+        s.kind = 0;
+        return kRayMiss;
+    }
+    const bool shadowed = st == kRayHit;
+    HitRec h = s.prim;
+    h.w3 = shade_rgba(h.w3, s.ndl, shadowed ? 0.0f : 1.0f, V.light.ambient);
+    h.w1 |= (VT_HIT_FLAG_SHADOW_RAY | (shadowed ? VT_HIT_FLAG_SHADOWED : 0u)) << 24;
+    V.out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+    s.kind = 0;
+    return kRayMiss;
+}
+
+__global__ void __launch_bounds__(256) batch_kernel(const BatchView* __restrict__ table,
+                                                    uint32_t nviews, uint64_t total,
+                                                    unsigned long long* __restrict__ counter,
+                                                    uint32_t refill_min) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    BatchView* views = reinterpret_cast<BatchView*>(smem_raw);
+    {
+        const uint32_t words = nviews * (uint32_t)(sizeof(BatchView) / 4);
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(table);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(smem_raw);
+        for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = __ldg(src + i);
+        __syncthreads();
+    }
+    const uint32_t lane = threadIdx.x & 31u;
+    BatchLane s;
+    s.kind = 0;
+    s.pix = 0;
+    s.ndl = 0.0f;
+    s.view = 0;
+    bool more = true;
+    for (;;) {
+        uint32_t idle = __ballot_sync(0xFFFFFFFFu, s.kind == 0);
+        while (more && __popc(idle) >= (int)refill_min) {
+            uint64_t item;
+            const uint64_t base = warp_fetch(counter, idle, lane, item);
+            if (base + __popc(idle) >= total) more = false;
+            if (s.kind == 0 && item < total) {
+                // the view owning the item: last view with begin <= item
+                uint32_t lo = 0, hi = nviews - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi + 1) >> 1;
+                    if (views[mid].begin <= item)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                const BatchView& V = views[lo];
+                const uint64_t local = item - V.begin;
+                const uint64_t ts = local >> 5;
+                const uint32_t l = (uint32_t)local & 31u;
+                const uint64_t tile = ts / V.spp;
+                const uint32_t sample = (uint32_t)(ts - tile * V.spp);
+                const uint32_t px = (uint32_t)(tile % V.tiles_x) * 8u + (l & 7u);
+                const uint32_t py = (uint32_t)(tile / V.tiles_x) * 4u + (l >> 3);
+                if (px < V.cam.width && py < V.cam.height) {
+                    float jx, jy, o[3], d[3];
+                    jitter(V.seed, V.view_id, px, py, sample, jx, jy);
+                    raygen(V.cam, px, py, jx, jy, o, d);
+                    s.view = lo;
+                    s.pix = ((py * V.cam.width) + px) * V.spp + sample;
+                    s.kind = 1;
+                    int st = ray_begin(V.g, o, d, s.R);
+                    while (s.kind != 0 && st != kRayRunning) st = batch_finish(V, s, st);
+                }
+            }
+            idle = __ballot_sync(0xFFFFFFFFu, s.kind == 0);
+        }
+        if (!more && idle == 0xFFFFFFFFu) break;
+        if (s.kind != 0) {
+            const BatchView& V = views[s.view];
+            int st = ray_unit(V.g, s.R);
+            while (s.kind != 0 && st != kRayRunning) st = batch_finish(V, s, st);
+        }
+    }
+}
+
+struct Batch {
+    std::vector<int32_t> grids;  // referenced grid ids (refcounted while the batch lives)
+    BatchView* d_table = nullptr;
+    unsigned long long* d_counter = nullptr;
+    uint32_t nviews = 0;
+    uint64_t total = 0;
+    uint64_t rays_primary = 0;
+    TraceTuning tune;
+    unsigned blocks = 0;
+    size_t smem = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+static std::mutex g_batch_mu;
+static std::vector<std::unique_ptr<Batch>> g_batches;
+
+static void batch_free(Batch& b) {
+    if (b.exec) cudaGraphExecDestroy(b.exec);
+    if (b.graph) cudaGraphDestroy(b.graph);
+    cudaFree(b.d_table);
+    cudaFree(b.d_counter);
+    for (int32_t id : b.grids) {
+        Grid* g = lookup_grid(id);
+        if (g) g->refs.fetch_sub(1);
+    }
+    b.exec = nullptr;
+    b.graph = nullptr;
+    b.d_table = nullptr;
+    b.d_counter = nullptr;
+    b.grids.clear();
+}
+
+static cudaError_t batch_launch(const Batch& b, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    batch_kernel<<<b.blocks, 256, b.smem, stream>>>(b.d_table, b.nviews, b.total, b.d_counter,
+                                                     b.tune.refill_min);
+    return cudaGetLastError();
+}
+
+}  // namespace vt
+
+using namespace vt;
+
+void vt_batch_release_all() {
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    for (auto& b : g_batches)
+        if (b) batch_free(*b);
+    g_batches.clear();
+}
+
+extern "C" {
+
+int32_t vt_batch_create(const vt_view* views, uint32_t n, int32_t* batch_out) {
+    if (!views || !batch_out || n == 0) return fail(VT_EINVAL, "vt_batch_create: no views");
+    if (n > kMaxBatchViews) return fail(VT_ELIMIT, "vt_batch_create: more than 256 views");
+    int32_t rc = ensure_init();
+    if (rc) return rc;
+    State& st = state();
+    std::unique_ptr<Batch> b(new Batch());
+    std::vector<BatchView> table(n);
+    uint64_t begin = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const vt_view& v = views[i];
+        Grid* g = lookup_grid(v.grid);
+        if (!g) {
+            batch_free(*b);
+            return fail(VT_ENOTFOUND, "vt_batch_create: unknown grid in view " + std::to_string(i));
+        }
+        if ((rc = check_camera(&v.camera))) {
+            batch_free(*b);
+            return rc;
+        }
+        if (v.spp == 0 || v.spp > 64 || !v.d_out || ((uintptr_t)v.d_out & 15u)) {
+            batch_free(*b);
+            return fail(VT_EINVAL, "vt_batch_create: view " + std::to_string(i) +
+                                       " needs spp in 1..64 and a 16-byte aligned output");
+        }
+        g->refs.fetch_add(1);
+        b->grids.push_back(v.grid);
+        BatchView& T = table[i];
+        memset(&T, 0, sizeof(T));
+        T.g = g->view();
+        T.cam = v.camera;
+        T.light = light_view((v.flags & VT_VIEW_LIGHT) ? &v.light : nullptr);
+        T.out = (uint4*)v.d_out;
+        T.begin = begin;
+        T.tiles_x = (v.camera.width + 7) / 8;
+        T.spp = v.spp;
+        T.seed = v.seed;
+        T.view_id = v.view_id;
+        const uint64_t tiles = (uint64_t)T.tiles_x * ((v.camera.height + 3) / 4);
+        begin += tiles * v.spp * 32;
+        b->rays_primary += (uint64_t)v.camera.width * v.camera.height * v.spp;
+    }
+    b->nviews = n;
+    b->total = begin;
+    b->tune = st.tune_batch;
+    b->smem = (size_t)n * sizeof(BatchView);
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, 256, b->smem);
+    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    if (b->tune.blocks_per_sm > 0) per_sm = std::min(per_sm, b->tune.blocks_per_sm);
+    b->blocks = (unsigned)std::min<uint64_t>((uint64_t)st.sm_count * per_sm, (b->total + 255) / 256);
+    if (cudaMalloc(&b->d_table, b->smem) != cudaSuccess ||
+        cudaMalloc(&b->d_counter, sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        batch_free(*b);
+        return fail(VT_ENOMEM, "vt_batch_create: cudaMalloc failed");
+    }
+    e = cudaMemcpy(b->d_table, table.data(), b->smem, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        batch_free(*b);
+        return cuda_fail(e, "vt_batch_create: table upload");
+    }
+    // capture counter reset + kernel into a graph on a private stream
+    cudaStream_t cs;
+    e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t le = batch_launch(*b, cs);
+            e = cudaStreamEndCapture(cs, &b->graph);
+            if (e == cudaSuccess) e = le;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+        cudaStreamDestroy(cs);
+    }
+    if (e != cudaSuccess) {
+        batch_free(*b);
+        return cuda_fail(e, "vt_batch_create: graph capture");
+    }
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    for (size_t i = 0; i < g_batches.size(); ++i)
+        if (!g_batches[i]) {
+            g_batches[i] = std::move(b);
+            *batch_out = (int32_t)i;
+            return VT_OK;
+        }
+    g_batches.push_back(std::move(b));
+    *batch_out = (int32_t)(g_batches.size() - 1);
+    return VT_OK;
+}
+
+static Batch* lookup_batch(int32_t id) {
+    std::lock_guard<std::mutex> lk(g_batch_mu);
+    if (id < 0 || (size_t)id >= g_batches.size() || !g_batches[id]) return nullptr;
+    return g_batches[id].get();
+}
+
+int32_t vt_batch_run(int32_t batch, void* stream) {
+    Batch* b = lookup_batch(batch);
+    if (!b) return fail(VT_ENOTFOUND, "vt_batch_run: unknown batch");
+    cudaError_t e = cudaGraphLaunch(b->exec, pick_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "vt_batch_run: graph launch");
+    return VT_OK;
+}
+
+int32_t vt_batch_run_direct(int32_t batch, void* stream) {
+    Batch* b = lookup_batch(batch);
+    if (!b) return fail(VT_ENOTFOUND, "vt_batch_run_direct: unknown batch");
+    cudaError_t e = batch_launch(*b, pick_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "vt_batch_run_direct: launch");
+    return VT_OK;
+}
+
+int32_t vt_batch_info(int32_t batch, uint64_t* primary_rays, uint64_t* work_items) {
+    Batch* b = lookup_batch(batch);
+    if (!b) return fail(VT_ENOTFOUND, "vt_batch_info: unknown batch");
+    if (primary_rays) *primary_rays = b->rays_primary;
+    if (work_items) *work_items = b->total;
+    return VT_OK;
+}
+
+int32_t vt_batch_destroy(int32_t batch) {
+    std::unique_ptr<Batch> b;
+    {
+        std::lock_guard<std::mutex> lk(g_batch_mu);
+        if (batch < 0 || (size_t)batch >= g_batches.size() || !g_batches[batch])
+            return fail(VT_ENOTFOUND, "vt_batch_destroy: unknown batch");
+        b = std::move(g_batches[batch]);
+    }
+    cudaStreamSynchronize(state().stream);
+    cudaDeviceSynchronize();
+    batch_free(*b);
+    return VT_OK;
+}
+
+}  // extern "C"

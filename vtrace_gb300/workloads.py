@@ -9,6 +9,8 @@ libvtrace's deterministic host generators; camera and light poses come from nump
                directional light with one hard-shadow ray per lit hit
   cave512      512^3 3D-noise cave (~45% occupancy), 16,777,216 rays with origins uniform in the
                grid and directions uniform on the sphere
+  multiview    8 scenes (128^3-512^3, terrain / shapes / cave) and 64 cameras with resolutions
+               log-uniform between 320x240 and 3840x2160 and 1-4 jittered samples per pixel
 """
 import math
 
@@ -62,3 +64,43 @@ def cave512(n=512, rays=1 << 24, seed=3):
     pal = gen_palette(seed)
     r = gen_rays_uniform(n, seed + 1, rays)
     return {"name": "cave%d_%drays" % (n, rays), "voxels": vox, "palette": pal, "rays": r}
+
+
+def multiview(n_scenes=8, n_views=64, seed=4, min_px=320 * 240, max_px=3840 * 2160,
+              sizes=(128, 192, 256, 320, 384, 448, 512, 256), max_spp=4):
+    """Scenes (voxels, palette, kind) and view specs (scene index, camera, spp, light)."""
+    rng = np.random.default_rng(seed)
+    kinds = ["terrain", "shapes", "cave"]
+    scenes = []
+    for i in range(n_scenes):
+        n = int(sizes[i % len(sizes)])
+        kind = kinds[i % 3]
+        if kind == "terrain":
+            vox = gen_terrain(n, seed * 100 + i, octaves=5, occupancy=0.3)
+        elif kind == "shapes":
+            vox = gen_shapes(n, seed * 100 + i, count=max(50, n * n // 100), rmin=2.0,
+                             rmax=max(4.0, n / 25.0))
+        else:
+            vox = gen_cave(n, seed * 100 + i, occupancy=0.45)
+        scenes.append({"voxels": vox, "palette": gen_palette(seed * 100 + i), "kind": kind,
+                       "n": n})
+    views = []
+    for v in range(n_views):
+        si = v % n_scenes
+        n = scenes[si]["n"]
+        area = math.exp(rng.uniform(math.log(min_px), math.log(max_px)))
+        aspect = 16.0 / 9.0 if rng.random() < 0.5 else 4.0 / 3.0
+        h = max(1, int(round(math.sqrt(area / aspect))))
+        w = max(1, int(round(h * aspect)))
+        spp = int(rng.integers(1, max_spp + 1))
+        # caves are viewed from inside, the rest from outside the grid
+        if scenes[si]["kind"] == "cave":
+            eye = tuple(float(x) for x in rng.uniform(0.3 * n, 0.7 * n, 3))
+            target = tuple(float(x) for x in rng.uniform(0.0, n, 3))
+        else:
+            eye, target = seeded_pose((n, n, n), seed * 1000 + v, float(rng.uniform(0.9, 1.6)) * n)
+        cam = camera_look_at(eye, target, (0.0, 1.0, 0.0), 60.0, w, h)
+        light = seeded_light(seed * 1000 + v, shadows=bool(rng.random() < 0.5))
+        views.append({"scene": si, "camera": cam, "spp": spp, "seed": seed * 7 + v,
+                      "view_id": v, "light": light})
+    return scenes, views
