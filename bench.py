@@ -45,7 +45,10 @@ def parse_args():
     p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--config", choices=["shapes1024", "terrain256"], default="shapes1024")
+    p.add_argument("--config", choices=["shapes1024", "terrain256", "cave512", "multiview", "serve"],
+                   default="shapes1024")
+    p.add_argument("--serve-requests", type=int, default=1000,
+                   help="requests of the serving comparison added to the headline run (0: skip)")
     p.add_argument("--cpu-seconds", type=float, default=2.0,
                    help="wall-clock budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -55,6 +58,17 @@ def parse_args():
 def dist_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
             int(os.environ.get("WORLD_SIZE", "1")))
+
+
+def profiled_traffic(workload):
+    """DRAM bytes per launch of the render kernel from the committed ncu summary, or None."""
+    import re
+    path = os.path.join(ROOT, "profiles", "render_%s.md" % workload)
+    try:
+        m = re.search(r"\| dram_bytes_per_launch \| (\d+) \|", open(path).read())
+        return int(m.group(1)) if m else None
+    except OSError:
+        return None
 
 
 def measured_peak():
@@ -293,18 +307,157 @@ def run_ours(args):
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": None, "algorithmic_bytes_per_launch": algo_bytes,
+                     "traffic": profiled_traffic("shapes1024_1080p") if args.config == "shapes1024" else None,
+                     "traffic_source": "profiles/render_shapes1024_1080p.md (ncu, one launch)",
+                     "algorithmic_bytes_per_launch": algo_bytes,
                      "kernel": "vt::render_kernel<false>"},
         "clocks": clocks,
         "grid_info": grid.info(),
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(w, args.cpu_seconds)
+    grid.destroy()
+    del d_hits
+    if rank == 0 and args.serve_requests > 0 and world == 1:
+        line["serve"] = serve_compare(args.serve_requests, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    grid.destroy()
     if world > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+def serve_run(vt, svc_kwargs, scenes, reqs, torch):
+    """Feeds `reqs` at their Poisson arrival times into a service; returns latency/throughput."""
+    import threading
+    svc = vt.Service(**svc_kwargs)
+    try:
+        sids = [svc.add_scene(sc["voxels"], sc["palette"]) for sc in scenes]
+        sizes = [r["camera"].width * r["camera"].height * 4 for r in reqs]
+        out = torch.empty(sum(sizes), dtype=torch.uint8, pin_memory=True)
+        offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+        # warm the grid cache (scene builds are not part of request latency)
+        for sid, sc in zip(sids, scenes):
+            c = vt.camera_look_at((-1.0, 1.0, -1.0), (1.0, 1.0, 1.0), (0, 1, 0), 60.0, 8, 8)
+            svc.wait(svc.submit(sid, c, out[:256].data_ptr(), 1))
+        ids = [None] * len(reqs)
+        t0 = time.perf_counter() + 0.05
+
+        def feeder():
+            for k, r in enumerate(reqs):
+                delay = t0 + r["t"] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                ids[k] = svc.submit(sids[r["scene"]], r["camera"], out.data_ptr() + int(offs[k]),
+                                    r["spp"], r["seed"], r["view_id"], r["light"])
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        timings = [svc.wait(i, 600.0) for i in ids]
+        st = svc.stats()
+    finally:
+        svc.stop()
+    lat = np.array([(t["done_ns"] - t["submit_ns"]) / 1e6 for t in timings])
+    first = min(t["submit_ns"] for t in timings)
+    last = max(t["done_ns"] for t in timings)
+    samples = sum(t["samples"] for t in timings)
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "makespan_s": (last - first) / 1e9,
+            "msamples_per_s": samples / ((last - first) / 1e9) / 1e6,
+            "launches": st["launches"] - len(scenes), "requests": len(reqs)}
+
+
+def serve_compare(n_requests, stream=None, n_scenes=32):
+    """Batched continuous serving vs plain per-request launches on the same Poisson stream."""
+    import torch
+    import vtrace_gb300 as vt
+    from vtrace_gb300 import workloads
+    scenes = workloads.serving_scenes(n_scenes)
+    reqs = workloads.serving_requests(scenes, n_requests)
+    batched = serve_run(vt, {}, scenes, reqs, torch)
+    plain = serve_run(vt, {"plain": True}, scenes, reqs, torch)
+    return {"workload": "%d scenes 128^3-1024^3, %d requests, Poisson 2000/s, 320x240-1920x1080, "
+                        "1-8 spp (rays = camera samples)" % (n_scenes, n_requests),
+            "batched": batched, "plain": plain,
+            "throughput_ratio": batched["msamples_per_s"] / plain["msamples_per_s"],
+            "p99_ratio": batched["p99_ms"] / plain["p99_ms"]}
+
+
+def run_config(args):
+    """Non-headline configurations: one JSON line each (measured parity cases)."""
+    import torch
+    import vtrace_gb300 as vt
+    from vtrace_gb300 import workloads, autotune
+    torch.cuda.set_device(0)
+    vt.init(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    line = {"steps": args.steps, "warmup": args.warmup, "n_gpus": 1, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic (seeded generators, no dataset)"}
+    if args.config == "cave512":
+        w = workloads.cave512()
+        g = vt.Grid.from_u8(w["voxels"], w["palette"])
+        n = w["rays"].shape[0]
+        d_rays = torch.from_numpy(w["rays"].view(np.uint8).reshape(-1)).cuda()
+        d_hits = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+        ms = autotune.time_ms(lambda: vt.trace_rays(g, d_rays, n, d_hits, stream), stream,
+                              repeats=args.steps, warmup=args.warmup, flush=flush)
+        st = vt.trace_rays_stats(g, d_rays, n, d_hits)
+        host_rays = torch.from_numpy(w["rays"]).pin_memory()
+        host_hits = torch.empty(n * 16, dtype=torch.uint8, pin_memory=True)
+        vt.lib().vt_trace_rays_host(g.id, host_rays.data_ptr(), n, host_hits.data_ptr())
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            vt.check(vt.lib().vt_trace_rays_host(g.id, host_rays.data_ptr(), n, host_hits.data_ptr()))
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        algo = 40 * n + 4 * st["bricks_entered"] + 64 * st["nonempty_bricks_entered"]
+        peak, kind = measured_peak()
+        line.update(metric="Mrays/s (16M incoherent rays, 512^3 cave)", value=n / ms / 1e3,
+                    unit="Mrays/s", ms_per_step=ms, config={"workload": w["name"]},
+                    e2e={"value": n / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 24 * n,
+                         "d2h_bytes_per_step": 16 * n},
+                    roofline={"bound": "hbm", "achieved": algo / ms / 1e6, "peak": peak,
+                              "unit": "GB/s", "frac": algo / ms / 1e6 / peak,
+                              "peak_source": kind, "algorithmic_bytes_per_launch": algo},
+                    tuning=vt.get_tuning(vt.KERNEL_TRACE_RAYS), gpu_launches=args.steps)
+        g.destroy()
+    elif args.config == "multiview":
+        scenes, views = workloads.multiview()
+        grids = [vt.Grid.from_u8(sc["voxels"], sc["palette"]) for sc in scenes]
+        bufs, specs = [], []
+        for v in views:
+            c = v["camera"]
+            b = torch.empty(c.width * c.height * v["spp"] * 16, dtype=torch.uint8, device="cuda")
+            bufs.append(b)
+            specs.append(vt.make_view(grids[v["scene"]], c, b, v["spp"], v["seed"], v["view_id"],
+                                      v["light"]))
+        batch = vt.Batch(specs)
+        ms = autotune.time_ms(lambda: batch.run(stream), stream, repeats=args.steps,
+                              warmup=args.warmup, flush=flush)
+        shadow = sum(int(((b.view(-1, 16)[:, 7] & vt.FLAG_SHADOW_RAY) != 0).sum().item()) for b in bufs)
+        rays = batch.primary_rays + shadow
+        singles = [vt.Batch([sp]) for sp in specs]
+        ms_single = autotune.time_ms(lambda: [x.run(stream) for x in singles], stream,
+                                     repeats=max(1, args.steps // 2), warmup=1, flush=flush)
+        line.update(metric="Mrays/s (64 views over 8 scenes, 1-4 spp, one graph replay)",
+                    value=rays / ms / 1e3, unit="Mrays/s", ms_per_step=ms,
+                    config={"workload": "multiview", "views": len(views),
+                            "primary_rays": batch.primary_rays, "shadow_rays": shadow},
+                    per_view_launches={"ms": ms_single, "value": rays / ms_single / 1e3},
+                    gpu_launches=args.steps)
+        for x in singles + [batch]:
+            x.destroy()
+        for gr in grids:
+            gr.destroy()
+    else:  # serve
+        r = serve_compare(max(args.serve_requests, 2000))
+        line.update(metric="serve p50/p99 latency and Msamples/s vs plain per-request launches",
+                    value=r["batched"]["msamples_per_s"], unit="Msamples/s",
+                    ms_per_step=r["batched"]["p50_ms"], config={"workload": r["workload"]},
+                    serve=r)
+    print(json.dumps(line), flush=True)
     return 0
 
 
@@ -312,6 +465,8 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config in ("cave512", "multiview", "serve"):
+        return run_config(args)
     return run_ours(args)
 
 

@@ -272,6 +272,67 @@ int32_t vt_batch_run_direct(int32_t batch, void* stream);
 int32_t vt_batch_info(int32_t batch, uint64_t* primary_rays, uint64_t* work_items);
 int32_t vt_batch_destroy(int32_t batch);
 
+/* ---------------------------------------------------------------- serving */
+
+/* A continuous-batching render service: requests arrive from any thread; a dispatcher thread keeps
+ * up to max_inflight launches on the device (one stream each), packing the oldest pending requests
+ * (up to max_views_per_launch views / max_samples_per_launch samples) into one persistent
+ * work-stealing launch as launch slots free up; each request's samples are averaged into an RGBA8
+ * image copied to the caller's host buffer.  Scene brick grids stay resident in a cache bounded by
+ * hbm_budget_bytes, built on first use, least-recently-used unreferenced scenes evicted.
+ * max_inflight = 1 with max_views_per_launch = 1 is the plain per-request baseline. */
+typedef struct vt_serve_config {
+    uint64_t hbm_budget_bytes;
+    uint32_t max_inflight;           /* concurrent launches, 1..32 */
+    uint32_t max_views_per_launch;   /* 1..256 */
+    uint64_t max_samples_per_launch; /* pack requests up to this many samples per launch */
+    uint32_t poll_interval_us;       /* completion polling period of the dispatcher */
+    uint32_t refill_min;             /* persistent-warp refill threshold of the launches */
+} vt_serve_config;
+
+/* One render request.  The image is width*height RGBA8 (row-major from the top row): per pixel
+ * and channel, (sum of the spp samples' colours + spp/2) / spp, samples jittered as in vt_view.
+ * host_rgba must stay valid until the request is polled done (pinned memory avoids a staging
+ * copy). */
+typedef struct vt_serve_request {
+    int32_t scene;
+    uint32_t spp;
+    uint32_t seed;
+    uint32_t view_id;
+    uint32_t flags; /* VT_VIEW_LIGHT */
+    vt_camera camera;
+    vt_light light;
+    uint8_t* host_rgba;
+} vt_serve_request;
+
+typedef struct vt_serve_timing {
+    int64_t submit_ns; /* steady clock at vt_serve_submit */
+    int64_t launch_ns; /* when its launch was enqueued */
+    int64_t done_ns;   /* when the dispatcher saw its image in host memory */
+    uint64_t samples;
+} vt_serve_timing;
+
+typedef struct vt_serve_stats {
+    uint64_t submitted, completed, launches, views_launched, samples;
+    uint64_t scene_loads, evictions, resident_bytes, pending;
+} vt_serve_stats;
+
+int32_t vt_serve_default_config(vt_serve_config* cfg);
+int32_t vt_serve_start(const vt_serve_config* cfg, int32_t* service_out);
+/* Register a scene (x-fastest u8 voxels and palette in host memory, kept valid by the caller for
+ * the life of the service: the cache rebuilds evicted scenes from it). */
+int32_t vt_serve_add_scene(int32_t service, const uint8_t* voxels, const uint32_t* palette,
+                           uint32_t nx, uint32_t ny, uint32_t nz, int32_t* scene_out);
+int32_t vt_serve_submit(int32_t service, const vt_serve_request* req, uint64_t* request_id);
+/* Wait up to timeout_us for a request: VT_OK (image written; the request is released),
+ * VT_ENOTREADY, or the request's error (VT_ENOMEM when its scene exceeds the budget,
+ * VT_ECANCELED when the service stopped first). */
+int32_t vt_serve_poll(int32_t service, uint64_t request_id, uint32_t timeout_us,
+                      vt_serve_timing* timing);
+int32_t vt_serve_get_stats(int32_t service, vt_serve_stats* out);
+/* Finish in-flight launches, cancel pending requests, free everything of the service. */
+int32_t vt_serve_stop(int32_t service);
+
 /* ---------------------------------------------------------------- scene generators (host) */
 
 /* Seeded synthetic content, deterministic across platforms (integer hashing and IEEE binary32

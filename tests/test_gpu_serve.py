@@ -1,0 +1,144 @@
+"""The continuous-batching service: every request's image is the same whether it ran alone or
+packed with others into shared launches, and equals the oracle's averaged jittered samples; the
+grid cache respects its HBM budget; failures are reported per request."""
+import numpy as np
+import pytest
+
+import vtrace_gb300 as vt
+from vtrace_gb300 import workloads
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    assert t.cuda.is_available()
+    vt.init(0)
+    return t
+
+
+def oracle_image(scene, v):
+    og = po.Grid(scene["voxels"], scene["palette"])
+    cam = po.make_camera(v["camera"].as_dict())
+    L = v["light"]
+    light = po.make_light(list(L.dir), L.ambient, bool(L.shadows))
+    hits = po.render_view(og, cam, light, v["spp"], v["seed"], v["view_id"])
+    c = hits["rgba"].reshape(-1, v["spp"]).astype(np.uint64)
+    out = np.zeros((c.shape[0], 4), np.uint8)
+    for k in range(4):
+        ch = (c >> np.uint64(8 * k)) & np.uint64(255)
+        out[:, k] = ((ch.sum(1) + v["spp"] // 2) // v["spp"]).astype(np.uint8)
+    return out.reshape(v["camera"].height, v["camera"].width, 4)
+
+
+def small_world(n_views=12):
+    return workloads.multiview(n_scenes=3, n_views=n_views, sizes=(64, 96, 48), min_px=40 * 30,
+                               max_px=160 * 120)
+
+
+def pinned(torch, cam):
+    return torch.zeros(cam.height * cam.width * 4, dtype=torch.uint8, pin_memory=True)
+
+
+def test_results_same_alone_and_in_the_mix(torch):
+    scenes, views = small_world()
+    svc = vt.Service()
+    try:
+        sids = [svc.add_scene(s["voxels"], s["palette"]) for s in scenes]
+        alone = []
+        for v in views:  # one at a time: every launch carries a single request
+            buf = pinned(torch, v["camera"])
+            svc.wait(svc.submit(sids[v["scene"]], v["camera"], buf, v["spp"], v["seed"],
+                                v["view_id"], v["light"]))
+            alone.append(buf.numpy().copy())
+        launches_alone = svc.stats()["launches"]
+        bufs = [pinned(torch, v["camera"]) for v in views]
+        rids = [svc.submit(sids[v["scene"]], v["camera"], b, v["spp"], v["seed"], v["view_id"],
+                           v["light"]) for v, b in zip(views, bufs)]
+        timings = [svc.wait(r) for r in rids]
+        st = svc.stats()
+        assert st["launches"] - launches_alone < len(views)  # requests shared launches
+        for a, b, v in zip(alone, bufs, views):
+            np.testing.assert_array_equal(a, b.numpy(), err_msg="view %d" % v["view_id"])
+        for i in (0, 4, 7, 11):
+            img = bufs[i].numpy().reshape(views[i]["camera"].height, views[i]["camera"].width, 4)
+            np.testing.assert_array_equal(img, oracle_image(scenes[views[i]["scene"]], views[i]))
+        assert all(t["submit_ns"] <= t["launch_ns"] <= t["done_ns"] for t in timings)
+    finally:
+        svc.stop()
+
+
+def test_plain_mode_gives_the_same_images(torch):
+    scenes, views = small_world(6)
+    svc = vt.Service(plain=True)
+    try:
+        sids = [svc.add_scene(s["voxels"], s["palette"]) for s in scenes]
+        bufs = [pinned(torch, v["camera"]) for v in views]
+        rids = [svc.submit(sids[v["scene"]], v["camera"], b, v["spp"], v["seed"], v["view_id"],
+                           v["light"]) for v, b in zip(views, bufs)]
+        for r in rids:
+            svc.wait(r)
+        assert svc.stats()["launches"] == len(views)
+        for b, v in zip(bufs, views):
+            img = b.numpy().reshape(v["camera"].height, v["camera"].width, 4)
+            np.testing.assert_array_equal(img, oracle_image(scenes[v["scene"]], v))
+    finally:
+        svc.stop()
+
+
+def test_cache_evicts_least_recently_used_under_its_budget(torch):
+    scenes, views = small_world(8)
+    # room for the largest scene's bound only: alternating scenes force evictions
+    bound = max(((s["n"] + 7) // 8) ** 3 * (4 + 64 + 512) + 1024 for s in scenes)
+    svc = vt.Service(hbm_budget_bytes=bound + 1024)
+    try:
+        sids = [svc.add_scene(s["voxels"], s["palette"]) for s in scenes]
+        for v in views:
+            buf = pinned(torch, v["camera"])
+            svc.wait(svc.submit(sids[v["scene"]], v["camera"], buf, v["spp"], v["seed"],
+                                v["view_id"], v["light"]))
+            img = buf.numpy().reshape(v["camera"].height, v["camera"].width, 4)
+            np.testing.assert_array_equal(img, oracle_image(scenes[v["scene"]], v))
+        st = svc.stats()
+        assert st["evictions"] > 0 and st["resident_bytes"] <= bound + 1024
+    finally:
+        svc.stop()
+
+
+def test_failures_are_reported_per_request(torch):
+    scenes, views = small_world(4)
+    svc = vt.Service(hbm_budget_bytes=1 << 20)  # smaller than any scene's bound
+    try:
+        sid = svc.add_scene(scenes[1]["voxels"], scenes[1]["palette"])
+        v = views[0]
+        with pytest.raises(vt.VtError):
+            svc.submit(sid + 5, v["camera"], pinned(torch, v["camera"]))
+        rid = svc.submit(sid, v["camera"], pinned(torch, v["camera"]), v["spp"])
+        with pytest.raises(vt.VtError) as e:
+            svc.wait(rid)
+        assert e.value.code == -2  # VT_ENOMEM: the scene cannot fit the budget
+    finally:
+        svc.stop()
+    # stopping with requests still queued cancels them; a poller blocked on one returns
+    import threading
+    svc = vt.Service(max_inflight=1, max_views_per_launch=1)
+    sid = svc.add_scene(scenes[0]["voxels"], scenes[0]["palette"])
+    big = vt.camera_look_at((-40.0, 80.0, -40.0), (32.0, 16.0, 32.0), (0, 1, 0), 60.0, 1280, 720)
+    bufs = [pinned(torch, big) for _ in range(40)]
+    rids = [svc.submit(sid, big, b, 8, seed=k) for k, b in enumerate(bufs)]
+    got = {}
+
+    def waiter():
+        try:
+            got["timing"] = svc.poll(rids[-1], 30_000_000)
+        except vt.VtError as err:
+            got["code"] = err.code
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    svc.stop()
+    th.join(timeout=60)
+    assert not th.is_alive()
+    assert got.get("code") == -7  # VT_ECANCELED

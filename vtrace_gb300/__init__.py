@@ -92,6 +92,33 @@ class View(ctypes.Structure):
 VIEW_LIGHT = 1
 
 
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
+                ("max_views_per_launch", ctypes.c_uint32),
+                ("max_samples_per_launch", ctypes.c_uint64), ("poll_interval_us", ctypes.c_uint32),
+                ("refill_min", ctypes.c_uint32)]
+
+
+class ServeRequest(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_int32), ("spp", ctypes.c_uint32), ("seed", ctypes.c_uint32),
+                ("view_id", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("camera", Camera),
+                ("light", Light), ("host_rgba", ctypes.c_void_p)]
+
+
+class ServeTiming(ctypes.Structure):
+    _fields_ = [("submit_ns", ctypes.c_int64), ("launch_ns", ctypes.c_int64),
+                ("done_ns", ctypes.c_int64), ("samples", ctypes.c_uint64)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "submitted", "completed", "launches", "views_launched", "samples", "scene_loads",
+        "evictions", "resident_bytes", "pending")]
+
+    def as_dict(self):
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
 class RenderTickInfo(ctypes.Structure):
     _fields_ = [("perspective", ctypes.c_void_p), ("camera", ctypes.c_void_p)]
 
@@ -134,6 +161,13 @@ SIGNATURES = [
     ("vt_batch_run_direct", _i32, [_i32, _vp]),
     ("vt_batch_info", _i32, [_i32, _vp, _vp]),
     ("vt_batch_destroy", _i32, [_i32]),
+    ("vt_serve_default_config", _i32, [ctypes.POINTER(ServeConfig)]),
+    ("vt_serve_start", _i32, [ctypes.POINTER(ServeConfig), ctypes.POINTER(ctypes.c_int32)]),
+    ("vt_serve_add_scene", _i32, [_i32, _vp, _vp, _u32, _u32, _u32, ctypes.POINTER(ctypes.c_int32)]),
+    ("vt_serve_submit", _i32, [_i32, ctypes.POINTER(ServeRequest), ctypes.POINTER(ctypes.c_uint64)]),
+    ("vt_serve_poll", _i32, [_i32, _u64, _u32, ctypes.POINTER(ServeTiming)]),
+    ("vt_serve_get_stats", _i32, [_i32, ctypes.POINTER(ServeStats)]),
+    ("vt_serve_stop", _i32, [_i32]),
     ("vt_camera_look_at", _i32, [_vp, _vp, _vp, _f32, _u32, _u32, ctypes.POINTER(Camera)]),
     ("vt_gen_palette", _i32, [_u32, _vp]),
     ("vt_gen_terrain", _i32, [_u32, _u32, _u32, _u32, _u32, _f32, _vp]),
@@ -418,3 +452,78 @@ def make_view(grid, camera, d_out, spp=1, seed=0, view_id=0, light=None):
         v.light = light
     v.d_out = _ptr(d_out)
     return v
+
+
+# ---------------------------------------------------------------- serving
+
+class Service:
+    """Continuous-batching render service (see vt_serve_* in include/vtrace.h)."""
+
+    def __init__(self, hbm_budget_bytes=None, max_inflight=None, max_views_per_launch=None,
+                 max_samples_per_launch=None, plain=False, refill_min=None):
+        cfg = ServeConfig()
+        check(lib().vt_serve_default_config(ctypes.byref(cfg)))
+        if hbm_budget_bytes is not None:
+            cfg.hbm_budget_bytes = hbm_budget_bytes
+        if max_inflight is not None:
+            cfg.max_inflight = max_inflight
+        if max_views_per_launch is not None:
+            cfg.max_views_per_launch = max_views_per_launch
+        if max_samples_per_launch is not None:
+            cfg.max_samples_per_launch = max_samples_per_launch
+        if refill_min is not None:
+            cfg.refill_min = refill_min
+        if plain:
+            cfg.max_inflight, cfg.max_views_per_launch = 1, 1
+        sid = ctypes.c_int32(-1)
+        check(lib().vt_serve_start(ctypes.byref(cfg), ctypes.byref(sid)))
+        self.id = sid.value
+        self._keep = []
+
+    def add_scene(self, voxels, palette):
+        voxels = np.ascontiguousarray(voxels, np.uint8)
+        palette = np.ascontiguousarray(palette, np.uint32)
+        self._keep.append((voxels, palette))
+        nz, ny, nx = voxels.shape
+        out = ctypes.c_int32(-1)
+        check(lib().vt_serve_add_scene(self.id, voxels.ctypes.data, palette.ctypes.data, nx, ny,
+                                       nz, ctypes.byref(out)))
+        return out.value
+
+    def submit(self, scene, camera, out_rgba, spp=1, seed=0, view_id=0, light=None):
+        r = ServeRequest()
+        r.scene, r.spp, r.seed, r.view_id = scene, spp, seed, view_id
+        r.flags = VIEW_LIGHT if light is not None else 0
+        r.camera = camera
+        if light is not None:
+            r.light = light
+        r.host_rgba = _ptr(out_rgba)
+        rid = ctypes.c_uint64(0)
+        check(lib().vt_serve_submit(self.id, ctypes.byref(r), ctypes.byref(rid)))
+        return rid.value
+
+    def poll(self, request_id, timeout_us=0):
+        """None while the request runs; its timing dict when done; raises on a failure."""
+        t = ServeTiming()
+        rc = lib().vt_serve_poll(self.id, request_id, timeout_us, ctypes.byref(t))
+        if rc == -8:
+            return None
+        check(rc)
+        return {"submit_ns": t.submit_ns, "launch_ns": t.launch_ns, "done_ns": t.done_ns,
+                "samples": t.samples}
+
+    def wait(self, request_id, timeout_s=60.0):
+        timing = self.poll(request_id, int(timeout_s * 1e6))
+        if timing is None:
+            raise VtError(-5, "request %d not done after %.1f s" % (request_id, timeout_s))
+        return timing
+
+    def stats(self):
+        st = ServeStats()
+        check(lib().vt_serve_get_stats(self.id, ctypes.byref(st)))
+        return st.as_dict()
+
+    def stop(self):
+        if self.id is not None:
+            check(lib().vt_serve_stop(self.id))
+            self.id = None

@@ -18,25 +18,12 @@
 #include <vector>
 
 #include "vt_api_internal.h"
+#include "vt_batch.h"
 #include "vt_device.cuh"
 #include "vt_internal.h"
 #include "vt_lane.cuh"
 
 namespace vt {
-
-constexpr uint32_t kMaxBatchViews = 256;
-
-struct BatchView {
-    GridView g;
-    vt_camera cam;
-    LightView light;
-    uint4* out;
-    unsigned long long begin;  // first item of the view
-    uint32_t tiles_x;
-    uint32_t spp;
-    uint32_t seed;
-    uint32_t view_id;
-};
 
 struct BatchLane {
     LaneRay R;
@@ -178,12 +165,54 @@ static void batch_free(Batch& b) {
     b.grids.clear();
 }
 
-static cudaError_t batch_launch(const Batch& b, cudaStream_t stream) {
-    cudaError_t e = cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned long long), stream);
+uint64_t batch_view_items(const vt_camera& cam, uint32_t spp) {
+    const uint64_t tiles = (uint64_t)((cam.width + 7) / 8) * ((cam.height + 3) / 4);
+    return tiles * spp * 32;
+}
+
+BatchView make_batch_view(const Grid& g, const vt_camera& cam, const vt_light* light,
+                          uint32_t spp, uint32_t seed, uint32_t view_id, void* out,
+                          uint64_t begin) {
+    BatchView T;
+    memset(&T, 0, sizeof(T));
+    T.g = g.view();
+    T.cam = cam;
+    T.light = light_view(light);
+    T.out = (uint4*)out;
+    T.begin = begin;
+    T.tiles_x = (cam.width + 7) / 8;
+    T.spp = spp;
+    T.seed = seed;
+    T.view_id = view_id;
+    return T;
+}
+
+unsigned batch_blocks(uint32_t n, uint64_t total, const TraceTuning& tune) {
+    const size_t smem = (size_t)n * sizeof(BatchView);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, 256, smem) !=
+            cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    if (tune.blocks_per_sm > 0) per_sm = std::min(per_sm, tune.blocks_per_sm);
+    const uint64_t need = (total + 255) / 256;
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)state().sm_count * per_sm, need));
+}
+
+cudaError_t launch_batch(const BatchView* d_table, uint32_t n, uint64_t total,
+                         unsigned long long* counter, const TraceTuning& tune, unsigned blocks,
+                         cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
-    batch_kernel<<<b.blocks, 256, b.smem, stream>>>(b.d_table, b.nviews, b.total, b.d_counter,
-                                                     b.tune.refill_min);
+    batch_kernel<<<blocks, 256, (size_t)n * sizeof(BatchView), stream>>>(d_table, n, total, counter,
+                                                                         tune.refill_min);
     return cudaGetLastError();
+}
+
+static cudaError_t batch_launch(const Batch& b, cudaStream_t stream) {
+    return launch_batch(b.d_table, b.nviews, b.total, b.d_counter, b.tune, b.blocks, stream);
 }
 
 }  // namespace vt
@@ -226,30 +255,17 @@ int32_t vt_batch_create(const vt_view* views, uint32_t n, int32_t* batch_out) {
         }
         g->refs.fetch_add(1);
         b->grids.push_back(v.grid);
-        BatchView& T = table[i];
-        memset(&T, 0, sizeof(T));
-        T.g = g->view();
-        T.cam = v.camera;
-        T.light = light_view((v.flags & VT_VIEW_LIGHT) ? &v.light : nullptr);
-        T.out = (uint4*)v.d_out;
-        T.begin = begin;
-        T.tiles_x = (v.camera.width + 7) / 8;
-        T.spp = v.spp;
-        T.seed = v.seed;
-        T.view_id = v.view_id;
-        const uint64_t tiles = (uint64_t)T.tiles_x * ((v.camera.height + 3) / 4);
-        begin += tiles * v.spp * 32;
+        table[i] = make_batch_view(*g, v.camera, (v.flags & VT_VIEW_LIGHT) ? &v.light : nullptr,
+                                   v.spp, v.seed, v.view_id, v.d_out, begin);
+        begin += batch_view_items(v.camera, v.spp);
         b->rays_primary += (uint64_t)v.camera.width * v.camera.height * v.spp;
     }
     b->nviews = n;
     b->total = begin;
     b->tune = st.tune_batch;
     b->smem = (size_t)n * sizeof(BatchView);
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, 256, b->smem);
-    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
-    if (b->tune.blocks_per_sm > 0) per_sm = std::min(per_sm, b->tune.blocks_per_sm);
-    b->blocks = (unsigned)std::min<uint64_t>((uint64_t)st.sm_count * per_sm, (b->total + 255) / 256);
+    b->blocks = batch_blocks(n, b->total, b->tune);
+    cudaError_t e;
     if (cudaMalloc(&b->d_table, b->smem) != cudaSuccess ||
         cudaMalloc(&b->d_counter, sizeof(unsigned long long)) != cudaSuccess) {
         cudaGetLastError();

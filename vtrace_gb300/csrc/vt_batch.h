@@ -1,0 +1,39 @@
+// vt_batch.h — batched multi-view launch shared by vt_batch.cu and vt_serve.cu (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "vt_api_internal.h"
+#include "vt_device.cuh"
+
+namespace vt {
+
+constexpr uint32_t kMaxBatchViews = 256;
+
+// One view of a batched launch, as the kernel reads it (the table is copied to shared memory).
+struct BatchView {
+    GridView g;
+    vt_camera cam;
+    LightView light;
+    uint4* out;                // per-sample records, [(py * width + px) * spp + s]
+    unsigned long long begin;  // first work item of the view
+    uint32_t tiles_x;
+    uint32_t spp;
+    uint32_t seed;
+    uint32_t view_id;
+};
+
+// Work items of a view: 8 x 4 pixel tiles x spp x 32 lanes.
+uint64_t batch_view_items(const vt_camera& cam, uint32_t spp);
+BatchView make_batch_view(const Grid& g, const vt_camera& cam, const vt_light* light,
+                          uint32_t spp, uint32_t seed, uint32_t view_id, void* out,
+                          uint64_t begin);
+// Blocks of a persistent batched launch over `total` items with an `n`-view table.
+unsigned batch_blocks(uint32_t n, uint64_t total, const TraceTuning& tune);
+// Counter reset + persistent kernel over a device view table.
+cudaError_t launch_batch(const BatchView* d_table, uint32_t n, uint64_t total,
+                         unsigned long long* counter, const TraceTuning& tune, unsigned blocks,
+                         cudaStream_t stream);
+
+}  // namespace vt

@@ -11,6 +11,8 @@ libvtrace's deterministic host generators; camera and light poses come from nump
                grid and directions uniform on the sphere
   multiview    8 scenes (128^3-512^3, terrain / shapes / cave) and 64 cameras with resolutions
                log-uniform between 320x240 and 3840x2160 and 1-4 jittered samples per pixel
+  serving      32 scenes (128^3-1024^3) and a Poisson stream of render requests (mean rate
+               2,000/s) with resolutions log-uniform between 320x240 and 1920x1080, 1-8 spp
 """
 import math
 
@@ -104,3 +106,49 @@ def multiview(n_scenes=8, n_views=64, seed=4, min_px=320 * 240, max_px=3840 * 21
         views.append({"scene": si, "camera": cam, "spp": spp, "seed": seed * 7 + v,
                       "view_id": v, "light": light})
     return scenes, views
+
+
+def serving_scenes(n_scenes=32, seed=5, lo=128, hi=1024):
+    """Scene sizes log-uniform in [lo, hi] (multiples of 8); shapes and terrain everywhere, caves
+    for the small ones (their noise is the slowest generator)."""
+    rng = np.random.default_rng(seed)
+    scenes = []
+    for i in range(n_scenes):
+        n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi))) / 8.0)) * 8
+        kind = ["shapes", "terrain", "cave"][i % 3]
+        if kind == "cave" and n > 256:
+            kind = "shapes"
+        if kind == "terrain":
+            vox = gen_terrain(n, seed * 1000 + i, octaves=5, occupancy=0.3)
+        elif kind == "shapes":
+            vox = gen_shapes(n, seed * 1000 + i, count=max(50, n * n // 100), rmin=2.0,
+                             rmax=max(4.0, n / 25.0))
+        else:
+            vox = gen_cave(n, seed * 1000 + i, occupancy=0.45)
+        scenes.append({"voxels": vox, "palette": gen_palette(seed * 1000 + i), "kind": kind, "n": n})
+    return scenes
+
+
+def serving_requests(scenes, count, rate=2000.0, seed=6, min_px=320 * 240, max_px=1920 * 1080,
+                     max_spp=8):
+    """`count` requests with Poisson arrival times (seconds from 0) at mean `rate` per second."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, count))
+    reqs = []
+    for k in range(count):
+        si = int(rng.integers(0, len(scenes)))
+        n = scenes[si]["n"]
+        area = math.exp(rng.uniform(math.log(min_px), math.log(max_px)))
+        aspect = 16.0 / 9.0 if rng.random() < 0.5 else 4.0 / 3.0
+        h = max(1, int(round(math.sqrt(area / aspect))))
+        w = max(1, int(round(h * aspect)))
+        if scenes[si]["kind"] == "cave":
+            eye = tuple(float(x) for x in rng.uniform(0.3 * n, 0.7 * n, 3))
+            target = tuple(float(x) for x in rng.uniform(0.0, n, 3))
+        else:
+            eye, target = seeded_pose((n, n, n), seed * 100000 + k, float(rng.uniform(0.9, 1.6)) * n)
+        reqs.append({"t": float(t[k]), "scene": si,
+                     "camera": camera_look_at(eye, target, (0.0, 1.0, 0.0), 60.0, w, h),
+                     "spp": int(rng.integers(1, max_spp + 1)), "seed": k, "view_id": k,
+                     "light": seeded_light(seed * 100000 + k, shadows=False)})
+    return reqs
