@@ -109,7 +109,7 @@ def test_cache_evicts_least_recently_used_under_its_budget(torch):
 
 def test_failures_are_reported_per_request(torch):
     scenes, views = small_world(4)
-    svc = vt.Service(hbm_budget_bytes=1 << 20)  # smaller than any scene's bound
+    svc = vt.Service(hbm_budget_bytes=64 << 10)  # smaller than any scene's bound
     try:
         sid = svc.add_scene(scenes[1]["voxels"], scenes[1]["palette"])
         v = views[0]
