@@ -210,6 +210,10 @@ int32_t vt_grid_get_info(int32_t grid, vt_grid_info* info);
  * the nearest occupied brick (1..31, saturating).  masks: bricks_nonempty * 8 u64 by slot, word
  * lz holding bit (ly * 8 + lx) of z-slice lz. */
 int32_t vt_grid_download_bricks(int32_t grid, uint32_t* directory, uint64_t* masks);
+/* Copy the grid's forward-distance words (bricks_total u32): for a ray octant
+ * o = (dx<0) | (dy<0)<<1 | (dz<0)<<2, nibble o holds the largest K <= 15 such that the K x K x K
+ * bricks starting at the brick and extending along the octant's directions are all empty. */
+int32_t vt_grid_download_octants(int32_t grid, uint32_t* octants);
 
 /* ---------------------------------------------------------------- tracing */
 

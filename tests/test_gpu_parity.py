@@ -283,6 +283,28 @@ def test_errors_are_reported_not_fatal(torch):
         g.destroy()
 
 
+def expected_octants(directory, dims, cap=15):
+    """Forward distance per ray octant by brute force: largest K <= cap whose K^3 box of bricks
+    from the brick along the octant's directions holds no occupied brick."""
+    nx, ny, nz = dims
+    bx, by, bz = (nx + 7) // 8, (ny + 7) // 8, (nz + 7) // 8
+    occ = ((directory >> 31) == 0).reshape(bz, by, bx)
+    occ_c = np.argwhere(occ)[:, ::-1]  # (x, y, z)
+    zz, yy, xx = np.meshgrid(np.arange(bz), np.arange(by), np.arange(bx), indexing="ij")
+    coords = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], 1)
+    out = np.zeros(len(coords), np.uint32)
+    for o in range(8):
+        sgn = np.array([-1 if o & 1 else 1, -1 if o & 2 else 1, -1 if o & 4 else 1])
+        if len(occ_c):
+            rel = (occ_c[None, :, :] - coords[:, None, :]) * sgn  # forward offsets
+            fwd = (rel >= 0).all(-1)
+            m = np.where(fwd, rel.max(-1), cap).min(1)
+        else:
+            m = np.full(len(coords), cap)
+        out |= (np.minimum(m, cap).astype(np.uint32) << np.uint32(4 * o))
+    return out
+
+
 def special_rays(rng, dims, n):
     """Axis-parallel, planar, exact-diagonal and grazing rays from inside and outside."""
     size = np.array(dims, np.float32)
@@ -321,6 +343,7 @@ def test_empty_space_skipping_is_exact(torch, dims, count):
         assert_hits_equal(hits_from_dev(d_hits), want, "counting kernel %r" % (dims,))
         wd, _, _ = expected_bricks(vox, pal)
         np.testing.assert_array_equal(d, wd)
+        np.testing.assert_array_equal(g.octants(), expected_octants(d, dims))
     finally:
         g.destroy()
 

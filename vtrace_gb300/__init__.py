@@ -149,6 +149,7 @@ SIGNATURES = [
     ("vt_grid_build_u8_noalloc", _i32, [_vp, _vp, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp]),
     ("vt_grid_get_info", _i32, [_i32, ctypes.POINTER(GridInfo)]),
     ("vt_grid_download_bricks", _i32, [_i32, _vp, _vp]),
+    ("vt_grid_download_octants", _i32, [_i32, _vp]),
     ("vt_trace_rays", _i32, [_i32, _vp, _u64, _vp, _vp]),
     ("vt_trace_rays_host", _i32, [_i32, _vp, _u64, _vp]),
     ("vt_render", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp, _vp]),
@@ -367,6 +368,11 @@ class Grid:
         m = np.zeros(max(1, inf["bricks_nonempty"]) * 8, np.uint64)
         check(lib().vt_grid_download_bricks(self.id, d.ctypes.data, m.ctypes.data))
         return d, m[: inf["bricks_nonempty"] * 8].reshape(-1, 8)
+
+    def octants(self):
+        out = np.zeros(self.info()["bricks_total"], np.uint32)
+        check(lib().vt_grid_download_octants(self.id, out.ctypes.data))
+        return out
 
     def destroy(self):
         if self.id is not None and self.id >= 0:

@@ -85,6 +85,7 @@ cudaStream_t pick_stream(void* stream) {
 GridView Grid::view() const {
     GridView v;
     v.dir = dir;
+    v.oct = oct;
     v.masks = masks;
     v.payload8 = format == VT_PAYLOAD_U8 ? (const uint8_t*)payload : nullptr;
     v.payload32 = format == VT_PAYLOAD_RGBA8 ? (const uint32_t*)payload : nullptr;
@@ -101,6 +102,8 @@ GridView Grid::view() const {
 }
 
 void Grid::release() {
+    cudaFree(oct);
+    oct = nullptr;
     cudaFree(dir);
     cudaFree(masks);
     cudaFree(payload);
@@ -175,6 +178,7 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
         const uint64_t slots = g->nonempty ? g->nonempty : 1;
         const size_t psize = format == VT_PAYLOAD_U8 ? 512 : 2048;
         if (cudaMalloc(&g->dir, g->bricks * 4) != cudaSuccess ||
+            cudaMalloc(&g->oct, g->bricks * 4) != cudaSuccess ||
             cudaMalloc(&g->masks, slots * 64) != cudaSuccess ||
             cudaMalloc(&g->payload, slots * psize) != cudaSuccess) {
             cudaGetLastError();
@@ -186,9 +190,13 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick compact kernel"); break; }
         e = launch_brick_distance(s, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick distance kernels"); break; }
+        // the occupancy words are no longer needed: their scratch holds the octant passes
+        e = launch_brick_octants(g->dir, (uint8_t*)s.words, (uint16_t*)((uint8_t*)s.words + ((g->bricks + 255) / 256) * 256),
+                                 g->oct, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "brick octant kernels"); break; }
         e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick build"); break; }
-        g->bytes = g->bricks * 4 + slots * 64 + slots * psize + (g->palette ? 1024 : 0);
+        g->bytes = g->bricks * 8 + slots * 64 + slots * psize + (g->palette ? 1024 : 0);
     } while (0);
     cudaFree(scratch);
     if (rc != VT_OK) {
@@ -444,6 +452,17 @@ int32_t vt_grid_download_bricks(int32_t grid, uint32_t* directory, uint64_t* mas
         e = cudaMemcpyAsync(masks, g->masks, g->nonempty * 64, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_grid_download_bricks");
+    return VT_OK;
+}
+
+int32_t vt_grid_download_octants(int32_t grid, uint32_t* octants) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_grid_download_octants: unknown grid");
+    if (!octants) return fail(VT_EINVAL, "vt_grid_download_octants: null output");
+    cudaStream_t st = state().stream;
+    cudaError_t e = cudaMemcpyAsync(octants, g->oct, g->bricks * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_grid_download_octants");
     return VT_OK;
 }
 

@@ -27,6 +27,7 @@ struct Grid {
     uint64_t bricks = 0, nonempty = 0, occupied = 0;
     uint32_t format = VT_PAYLOAD_U8;
     uint32_t* dir = nullptr;
+    uint32_t* oct = nullptr;  // forward distances per ray octant
     uint64_t* masks = nullptr;
     void* payload = nullptr;
     uint32_t* palette = nullptr;

@@ -27,6 +27,7 @@ __device__ __forceinline__ bool brick_empty(uint32_t e) { return (e & kEmptyBit)
 
 struct GridView {
     const uint32_t* dir;
+    const uint32_t* oct;  // forward distances per ray octant (4 bits x 8), or nullptr
     const uint64_t* masks;
     const uint8_t* payload8;    // VT_PAYLOAD_U8
     const uint32_t* payload32;  // VT_PAYLOAD_RGBA8
@@ -359,10 +360,49 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
     }
 }
 
+// The empty box of voxels the ray crosses next from the empty brick (bxi, byi, bzi): the forward
+// box of the ray's octant (K bricks along each stepping direction, from the octant word) when it
+// reaches further than the centred cube of bricks within Chebyshev distance D - 1 (from the
+// directory entry), else that cube; clipped to the grid.
+__device__ __forceinline__ void empty_box(const GridView& g, uint32_t e, size_t bidx, int32_t bxi,
+                                          int32_t byi, int32_t bzi, int32_t stx, int32_t sty,
+                                          int32_t stz, uint32_t oct_shift, int32_t& lox,
+                                          int32_t& hix, int32_t& loy, int32_t& hiy, int32_t& loz,
+                                          int32_t& hiz) {
+    const int32_t D = max((int32_t)(e & 0xFFu), 1);
+    const int32_t K = g.oct ? (int32_t)((__ldg(g.oct + bidx) >> oct_shift) & 15u) : 0;
+    if (K > D) {
+        lox = stx < 0 ? (bxi - K + 1) * 8 : bxi * 8;
+        hix = stx < 0 ? (bxi + 1) * 8 : (bxi + K) * 8;
+        loy = sty < 0 ? (byi - K + 1) * 8 : byi * 8;
+        hiy = sty < 0 ? (byi + 1) * 8 : (byi + K) * 8;
+        loz = stz < 0 ? (bzi - K + 1) * 8 : bzi * 8;
+        hiz = stz < 0 ? (bzi + 1) * 8 : (bzi + K) * 8;
+    } else {
+        const int32_t D1 = D - 1;
+        lox = (bxi - D1) * 8;
+        hix = (bxi + D1 + 1) * 8;
+        loy = (byi - D1) * 8;
+        hiy = (byi + D1 + 1) * 8;
+        loz = (bzi - D1) * 8;
+        hiz = (bzi + D1 + 1) * 8;
+    }
+    lox = max(lox, 0);
+    loy = max(loy, 0);
+    loz = max(loz, 0);
+    hix = min(hix, g.nx);
+    hiy = min(hiy, g.ny);
+    hiz = min(hiz, g.nz);
+}
+
+__device__ __forceinline__ uint32_t octant_shift(int32_t stx, int32_t sty, int32_t stz) {
+    return 4u * ((stx < 0 ? 1u : 0u) | (sty < 0 ? 2u : 0u) | (stz < 0 ? 4u : 0u));
+}
+
 // Same result as dda() (hit, voxel, slot, final mask), organised for speed: occupied bricks are
 // walked voxel by voxel against their occupancy bits; an empty brick at Chebyshev distance D from
-// the nearest occupied brick is part of an empty cube of (2D-1)^3 bricks, which the ray crosses
-// in one cross_region().  The step count and tie flag of the literal loop are not
+// the nearest occupied brick is part of an empty cube of (2D-1)^3 bricks, and of the forward box
+// of the ray's octant (empty_box); the ray crosses the larger in one cross_region().  The step count and tie flag of the literal loop are not
 // tracked here (the counting kernels use dda()).
 __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, float pz,
                                          float dx, float dy, float dz, DDAResult& r) {
@@ -379,14 +419,15 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
         return;
     }
     const uint32_t max_steps = g.max_steps;
+    const uint32_t oshift = octant_shift(stx, sty, stz);
     uint32_t steps = 0, slot = kEmptyBit;  // steps: only bounds the occupied-brick loop
     bool mx = false, my = false, mz = false, hit = false;
     // every pass of this loop advances at least one axis, monotonically, inside the grid
     int32_t guard = g.nx + g.ny + g.nz + 2;
     while (grid_inside(g, vx, vy, vz) && --guard > 0) {
         const int32_t bxi = vx >> 3, byi = vy >> 3, bzi = vz >> 3;
-        const uint32_t e =
-            __ldg(g.dir + ((size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi)));
+        const size_t bidx = (size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi);
+        const uint32_t e = __ldg(g.dir + bidx);
         if (!brick_empty(e)) {
             slot = e;
             const uint64_t* mk = g.masks + (size_t)slot * 8;
@@ -405,10 +446,9 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
             }
             if (hit) break;
         } else {
-            const int32_t D1 = max((int32_t)(e & 0xFFu), 1) - 1;
-            const int32_t lox = max((bxi - D1) * 8, 0), hix = min((bxi + D1 + 1) * 8, g.nx);
-            const int32_t loy = max((byi - D1) * 8, 0), hiy = min((byi + D1 + 1) * 8, g.ny);
-            const int32_t loz = max((bzi - D1) * 8, 0), hiz = min((bzi + D1 + 1) * 8, g.nz);
+            int32_t lox, hix, loy, hiy, loz, hiz;
+            empty_box(g, e, bidx, bxi, byi, bzi, stx, sty, stz, oshift, lox, hix, loy, hiy, loz,
+                      hiz);
             const int32_t nxe = stx > 0 ? hix - vx : vx - lox + 1;
             const int32_t nye = sty > 0 ? hiy - vy : vy - loy + 1;
             const int32_t nze = stz > 0 ? hiz - vz : vz - loz + 1;

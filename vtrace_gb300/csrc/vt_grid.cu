@@ -331,6 +331,97 @@ __global__ void __launch_bounds__(256) brick_distance_kernel(uint32_t* __restric
     }
 }
 
+// Forward (octant) distances: for every brick and each of the 8 sign combinations (sx, sy, sz) of
+// a ray direction, the largest K <= kMaxOctantDistance such that the box of K x K x K bricks
+// starting at the brick and extending in the directions (sx, sy, sz) holds no occupied brick
+// (0 for an occupied brick).  Separable: pass x gives the 1D forward distance for sx = +/-1,
+// pass y takes min_j max(j, pass_x(b + j*sy)) for the four (sx, sy), pass z likewise for all
+// eight.  Packed 4 bits per octant, octant index (sx<0) | (sy<0)<<1 | (sz<0)<<2.
+constexpr int kMaxOctantDistance = 15;
+
+__global__ void __launch_bounds__(256) brick_octant_x_kernel(const uint32_t* __restrict__ dir,
+                                                             uint8_t* __restrict__ out,
+                                                             int32_t bx, int32_t by,
+                                                             uint64_t bricks) {
+    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= bricks) return;
+    const BrickCoord c = brick_coord(b, bx, by);
+    uint32_t packed = 0;
+#pragma unroll
+    for (int neg = 0; neg < 2; ++neg) {
+        const int32_t sx = neg ? -1 : 1;
+        int32_t best = kMaxOctantDistance;
+        for (int32_t k = 0; k < kMaxOctantDistance; ++k) {
+            const int32_t x = c.bxi + k * sx;
+            if (x < 0 || x >= bx) break;
+            if (!brick_empty(__ldg(dir + (int64_t)b + (int64_t)k * sx))) {
+                best = k;
+                break;
+            }
+        }
+        packed |= (uint32_t)best << (4 * neg);
+    }
+    out[b] = (uint8_t)packed;
+}
+
+__global__ void __launch_bounds__(256) brick_octant_y_kernel(const uint8_t* __restrict__ in,
+                                                             uint16_t* __restrict__ out,
+                                                             int32_t bx, int32_t by,
+                                                             uint64_t bricks) {
+    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= bricks) return;
+    const BrickCoord c = brick_coord(b, bx, by);
+    uint32_t packed = 0;
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {  // o = (sx<0) | (sy<0)<<1
+        const int32_t sy = (o & 2) ? -1 : 1;
+        int32_t best = kMaxOctantDistance;
+        for (int32_t j = 0; j < best; ++j) {
+            const int32_t y = c.byi + j * sy;
+            if (y < 0 || y >= by) break;
+            const int32_t f = (int32_t)((__ldg(in + (int64_t)b + (int64_t)j * sy * bx) >> (4 * (o & 1))) & 15u);
+            best = min(best, max(j, f));
+        }
+        packed |= (uint32_t)best << (4 * o);
+    }
+    out[b] = (uint16_t)packed;
+}
+
+__global__ void __launch_bounds__(256) brick_octant_z_kernel(const uint16_t* __restrict__ in,
+                                                             uint32_t* __restrict__ out,
+                                                             int32_t bx, int32_t by, int32_t bz,
+                                                             uint64_t bricks) {
+    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= bricks) return;
+    const BrickCoord c = brick_coord(b, bx, by);
+    const int64_t plane = (int64_t)bx * by;
+    uint32_t packed = 0;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {  // o = (sx<0) | (sy<0)<<1 | (sz<0)<<2
+        const int32_t sz = (o & 4) ? -1 : 1;
+        int32_t best = kMaxOctantDistance;
+        for (int32_t l = 0; l < best; ++l) {
+            const int32_t z = c.bzi + l * sz;
+            if (z < 0 || z >= bz) break;
+            const int32_t f = (int32_t)((__ldg(in + (int64_t)b + (int64_t)l * sz * plane) >> (4 * (o & 3))) & 15u);
+            best = min(best, max(l, f));
+        }
+        packed |= (uint32_t)best << (4 * o);
+    }
+    out[b] = packed;
+}
+
+cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* tmp_y,
+                                 uint32_t* oct, int32_t bx, int32_t by, int32_t bz,
+                                 cudaStream_t stream) {
+    const uint64_t bricks = (uint64_t)bx * by * bz;
+    const unsigned blocks = (unsigned)((bricks + 255) / 256);
+    brick_octant_x_kernel<<<blocks, 256, 0, stream>>>(dir, tmp_x, bx, by, bricks);
+    brick_octant_y_kernel<<<blocks, 256, 0, stream>>>(tmp_x, tmp_y, bx, by, bricks);
+    brick_octant_z_kernel<<<blocks, 256, 0, stream>>>(tmp_y, oct, bx, by, bz, bricks);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,
                                   int32_t bz, cudaStream_t stream) {
     const uint64_t bricks = (uint64_t)bx * by * bz;

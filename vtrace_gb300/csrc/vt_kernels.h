@@ -57,6 +57,12 @@ cudaError_t launch_brick_compact(const void* src, uint32_t format, int32_t nx, i
                                  int32_t nz, const BuildScratch& s, uint32_t* dir,
                                  uint64_t* masks, void* payload, cudaStream_t stream);
 
+// Phase 5: forward distances per ray octant (4 bits x 8 per brick) into `oct`; tmp_x holds one
+// byte and tmp_y two bytes per brick.
+cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* tmp_y,
+                                 uint32_t* oct, int32_t bx, int32_t by, int32_t bz,
+                                 cudaStream_t stream);
+
 // Phase 4: Chebyshev distance of every empty brick to the nearest occupied one, into dir.
 cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,
                                   int32_t bz, cudaStream_t stream);

@@ -23,6 +23,7 @@ struct LaneRay {
     float t_entry;
     bool mx, my, mz;     // axes stepped on the final iteration
     uint32_t flags;      // VT_HIT_FLAG_INVALID for rejected input
+    uint32_t oshift;     // nibble of the ray's octant in the octant words
 };
 
 // Validity, slab entry and DDA set-up (trace.frag:68-71).  Returns kRayRunning, or the final
@@ -67,6 +68,7 @@ __device__ __forceinline__ int ray_begin(const GridView& g, const float o[3], co
         return r.hit ? kRayHit : kRayMiss;
     }
     R.guard = g.nx + g.ny + g.nz + 2;
+    R.oshift = octant_shift(R.stx, R.sty, R.stz);
     return grid_inside(g, R.vx, R.vy, R.vz) ? kRayRunning : kRayMiss;
 }
 
@@ -80,8 +82,8 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
     bool mx = R.mx, my = R.my, mz = R.mz;
     int status = kRayRunning;
     const int32_t bxi = vx >> 3, byi = vy >> 3, bzi = vz >> 3;
-    const uint32_t e =
-        __ldg(g.dir + ((size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi)));
+    const size_t bidx = (size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi);
+    const uint32_t e = __ldg(g.dir + bidx);
     if (!brick_empty(e)) {
         const uint64_t* mk = g.masks + (size_t)e * 8;
         const int32_t ex = stx > 0 ? min((bxi << 3) + 8, g.nx) : (stx < 0 ? (bxi << 3) - 1 : INT_MIN);
@@ -99,10 +101,8 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
             if (vx == ex || vy == ey || vz == ez || steps >= 24u) break;
         }
     } else {
-        const int32_t D1 = max((int32_t)(e & 0xFFu), 1) - 1;
-        const int32_t lox = max((bxi - D1) * 8, 0), hix = min((bxi + D1 + 1) * 8, g.nx);
-        const int32_t loy = max((byi - D1) * 8, 0), hiy = min((byi + D1 + 1) * 8, g.ny);
-        const int32_t loz = max((bzi - D1) * 8, 0), hiz = min((bzi + D1 + 1) * 8, g.nz);
+        int32_t lox, hix, loy, hiy, loz, hiz;
+        empty_box(g, e, bidx, bxi, byi, bzi, stx, sty, stz, R.oshift, lox, hix, loy, hiy, loz, hiz);
         const int32_t nxe = stx > 0 ? hix - vx : vx - lox + 1;
         const int32_t nye = sty > 0 ? hiy - vy : vy - loy + 1;
         const int32_t nze = stz > 0 ? hiz - vz : vz - loz + 1;
