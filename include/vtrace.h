@@ -159,6 +159,8 @@ typedef struct vt_tuning {
     uint32_t refill_min;
     int32_t blocks_per_sm;
     uint32_t persistent;
+    uint32_t wavefront; /* VT_KERNEL_RENDER tile launches: trace shadow rays in a second pass over
+                           a compacted queue instead of in the primary ray's thread */
 } vt_tuning;
 
 #define VT_KERNEL_RENDER 1

@@ -348,25 +348,30 @@ def test_empty_space_skipping_is_exact(torch, dims, count):
         g.destroy()
 
 
-@pytest.mark.parametrize("persistent,refill_min", [(0, 16), (1, 1), (1, 8), (1, 32)])
-def test_launch_shapes_agree(torch, persistent, refill_min):
-    """Tile launches and persistent launches at any refill threshold give identical records."""
+@pytest.mark.parametrize("persistent,refill_min,wavefront",
+                         [(0, 16, 0), (0, 16, 1), (1, 1, 0), (1, 8, 0), (1, 32, 0)])
+def test_launch_shapes_agree(torch, persistent, refill_min, wavefront):
+    """Tile launches (shadow rays fused or in a second pass) and persistent launches at any refill
+    threshold give identical records."""
     saved = {k: vt.get_tuning(k) for k in (vt.KERNEL_RENDER, vt.KERNEL_TRACE_RAYS)}
     w = workloads.terrain256(n=192, width=320, height=200)
+    light = workloads.seeded_light(1, shadows=True)
     g = vt.Grid.from_u8(w["voxels"], w["palette"])
     try:
         for k in saved:
-            vt.set_tuning(k, refill_min, 0, persistent)
+            vt.set_tuning(k, refill_min, 0, persistent, wavefront)
         og = po.Grid(w["voxels"], w["palette"])
-        img, _ = device_render(torch, g, w["camera"], w["light"])
-        assert_hits_equal(img, po.render(og, oracle_camera(w["camera"]), oracle_light(w["light"])),
-                          "render persistent=%d refill_min=%d" % (persistent, refill_min))
+        img, _ = device_render(torch, g, w["camera"], light)
+        assert_hits_equal(img, po.render(og, oracle_camera(w["camera"]), oracle_light(light)),
+                          "render persistent=%d refill_min=%d wavefront=%d"
+                          % (persistent, refill_min, wavefront))
+        assert ((img["face"] & vt.FLAG_SHADOW_RAY) != 0).sum() > 1000
         rays = vt.gen_rays_uniform(192, 9, 200000)
         hits, _, _ = device_trace(torch, g, rays)
         assert_hits_equal(hits, po.trace_rays(og, rays), "rays persistent=%d" % persistent)
     finally:
         for k, t in saved.items():
-            vt.set_tuning(k, t["refill_min"], t["blocks_per_sm"], t["persistent"])
+            vt.set_tuning(k, t["refill_min"], t["blocks_per_sm"], t["persistent"], t["wavefront"])
         g.destroy()
 
 

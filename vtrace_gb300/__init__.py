@@ -77,7 +77,7 @@ class TraceStats(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("refill_min", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_int32),
-                ("persistent", ctypes.c_uint32)]
+                ("persistent", ctypes.c_uint32), ("wavefront", ctypes.c_uint32)]
 
 
 KERNEL_RENDER, KERNEL_TRACE_RAYS, KERNEL_BATCH = 1, 2, 3
@@ -257,11 +257,11 @@ def get_tuning(kernel):
     t = Tuning()
     check(lib().vt_get_tuning(kernel, ctypes.byref(t)))
     return {"refill_min": t.refill_min, "blocks_per_sm": t.blocks_per_sm,
-            "persistent": t.persistent}
+            "persistent": t.persistent, "wavefront": t.wavefront}
 
 
-def set_tuning(kernel, refill_min=16, blocks_per_sm=0, persistent=True):
-    t = Tuning(refill_min, blocks_per_sm, 1 if persistent else 0)
+def set_tuning(kernel, refill_min=16, blocks_per_sm=0, persistent=True, wavefront=False):
+    t = Tuning(refill_min, blocks_per_sm, 1 if persistent else 0, 1 if wavefront else 0)
     check(lib().vt_set_tuning(kernel, ctypes.byref(t)))
 
 

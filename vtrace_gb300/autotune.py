@@ -17,10 +17,12 @@ DEFAULT_REFILL = (1, 4, 8, 16, 24, 32)
 DEFAULT_BLOCKS = (0, 2)
 
 
-def candidates(refill=DEFAULT_REFILL, blocks=DEFAULT_BLOCKS, tiles=True):
+def candidates(refill=DEFAULT_REFILL, blocks=DEFAULT_BLOCKS, tiles=True, wavefront=False):
     out = []
     if tiles:
         out.append({"refill_min": 32, "blocks_per_sm": 0, "persistent": False})
+    if wavefront:
+        out.append({"refill_min": 32, "blocks_per_sm": 0, "persistent": False, "wavefront": True})
     for r, b in itertools.product(refill, blocks):
         out.append({"refill_min": r, "blocks_per_sm": b, "persistent": True})
     return out
@@ -57,18 +59,21 @@ def autotune(kernel, run, stream, cands=None, repeats=5, flush=None, prepare=Non
     best, best_ms = None, float("inf")
     try:
         for c in cands:
-            set_tuning(kernel, c["refill_min"], c["blocks_per_sm"], c["persistent"])
+            set_tuning(kernel, c["refill_min"], c["blocks_per_sm"], c["persistent"],
+                       c.get("wavefront", False))
             if prepare is not None:
                 prepare()
             ms = time_ms(run, stream, repeats=repeats, flush=flush)
-            key = "%s_r%d_b%d" % ("persistent" if c["persistent"] else "tiles", c["refill_min"],
-                                  c["blocks_per_sm"])
+            key = "%s_r%d_b%d" % ("persistent" if c["persistent"] else
+                                  ("wavefront" if c.get("wavefront") else "tiles"),
+                                  c["refill_min"], c["blocks_per_sm"])
             results[key] = ms
             if ms < best_ms:
                 best, best_ms = c, ms
     finally:
         chosen = best or saved
-        set_tuning(kernel, chosen["refill_min"], chosen["blocks_per_sm"], chosen["persistent"])
+        set_tuning(kernel, chosen["refill_min"], chosen["blocks_per_sm"], chosen["persistent"],
+                   chosen.get("wavefront", False))
         if prepare is not None:
             prepare()
     return best, results

@@ -66,6 +66,7 @@ cudaError_t launch_frame(const GridView& g, const vt_camera& cam, const LightVie
     if (s.tune_render.persistent)
         return launch_render_persistent(g, cam, light, out, next_counter(), s.tune_render,
                                         s.sm_count, stream);
+    if (s.tune_render.wavefront) return launch_render_wavefront(g, cam, light, out, stream);
     return launch_render(g, cam, light, out, nullptr, stream);
 }
 
@@ -350,6 +351,7 @@ int32_t vt_get_tuning(int32_t kernel, vt_tuning* out) {
     out->refill_min = t->refill_min;
     out->blocks_per_sm = t->blocks_per_sm;
     out->persistent = t->persistent;
+    out->wavefront = t->wavefront;
     return VT_OK;
 }
 
@@ -361,6 +363,7 @@ int32_t vt_set_tuning(int32_t kernel, const vt_tuning* in) {
     t->refill_min = in->refill_min;
     t->blocks_per_sm = in->blocks_per_sm;
     t->persistent = in->persistent ? 1u : 0u;
+    t->wavefront = in->wavefront ? 1u : 0u;
     return VT_OK;
 }
 

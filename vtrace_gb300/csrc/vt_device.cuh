@@ -361,16 +361,16 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
 }
 
 // The empty box of voxels the ray crosses next from the empty brick (bxi, byi, bzi): the forward
-// box of the ray's octant (K bricks along each stepping direction, from the octant word) when it
-// reaches further than the centred cube of bricks within Chebyshev distance D - 1 (from the
-// directory entry), else that cube; clipped to the grid.
-__device__ __forceinline__ void empty_box(const GridView& g, uint32_t e, size_t bidx, int32_t bxi,
+// box of the ray's octant (K bricks along each stepping direction, from the brick's octant word
+// `ow`) when it reaches further than the centred cube of bricks within Chebyshev distance D - 1
+// (from the directory entry `e`), else that cube; clipped to the grid.
+__device__ __forceinline__ void empty_box(const GridView& g, uint32_t e, uint32_t ow, int32_t bxi,
                                           int32_t byi, int32_t bzi, int32_t stx, int32_t sty,
                                           int32_t stz, uint32_t oct_shift, int32_t& lox,
                                           int32_t& hix, int32_t& loy, int32_t& hiy, int32_t& loz,
                                           int32_t& hiz) {
     const int32_t D = max((int32_t)(e & 0xFFu), 1);
-    const int32_t K = g.oct ? (int32_t)((__ldg(g.oct + bidx) >> oct_shift) & 15u) : 0;
+    const int32_t K = (int32_t)((ow >> oct_shift) & 15u);
     if (K > D) {
         lox = stx < 0 ? (bxi - K + 1) * 8 : bxi * 8;
         hix = stx < 0 ? (bxi + 1) * 8 : (bxi + K) * 8;
@@ -393,6 +393,13 @@ __device__ __forceinline__ void empty_box(const GridView& g, uint32_t e, size_t 
     hix = min(hix, g.nx);
     hiy = min(hiy, g.ny);
     hiz = min(hiz, g.nz);
+}
+
+// The octant word of brick `bidx`; 0 (no forward boxes) for a grid built without octant words.
+// Loaded together with the directory entry, before the entry is tested, so that both loads are in
+// flight at once.
+__device__ __forceinline__ uint32_t octant_word(const GridView& g, size_t bidx) {
+    return g.oct ? __ldg(g.oct + bidx) : 0u;
 }
 
 __device__ __forceinline__ uint32_t octant_shift(int32_t stx, int32_t sty, int32_t stz) {
@@ -428,6 +435,7 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
         const int32_t bxi = vx >> 3, byi = vy >> 3, bzi = vz >> 3;
         const size_t bidx = (size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi);
         const uint32_t e = __ldg(g.dir + bidx);
+        const uint32_t ow = octant_word(g, bidx);
         if (!brick_empty(e)) {
             slot = e;
             const uint64_t* mk = g.masks + (size_t)slot * 8;
@@ -447,7 +455,7 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
             if (hit) break;
         } else {
             int32_t lox, hix, loy, hiy, loz, hiz;
-            empty_box(g, e, bidx, bxi, byi, bzi, stx, sty, stz, oshift, lox, hix, loy, hiy, loz,
+            empty_box(g, e, ow, bxi, byi, bzi, stx, sty, stz, oshift, lox, hix, loy, hiy, loz,
                       hiz);
             const int32_t nxe = stx > 0 ? hix - vx : vx - lox + 1;
             const int32_t nye = sty > 0 ? hiy - vy : vy - loy + 1;

@@ -17,7 +17,12 @@ struct TraceTuning {
     uint32_t refill_min = 16;  // refill a warp when at least this many lanes are idle (1..32)
     int blocks_per_sm = 0;     // 0: as many 256-thread blocks as fit on an SM
     uint32_t persistent = 1;   // 0: one thread per ray in 8 x 4 pixel tiles, no refill
+    uint32_t wavefront = 0;    // render only: shadow rays in a second pass over a compacted queue
 };
+
+// Render in two passes (primary rays, then the queued shadow rays); stream-ordered scratch.
+cudaError_t launch_render_wavefront(const GridView& g, const vt_camera& cam,
+                                    const LightView& light, uint4* out, cudaStream_t stream);
 
 cudaError_t launch_render_persistent(const GridView& g, const vt_camera& cam,
                                      const LightView& light, uint4* out,

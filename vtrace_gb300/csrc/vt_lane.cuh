@@ -84,6 +84,7 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
     const int32_t bxi = vx >> 3, byi = vy >> 3, bzi = vz >> 3;
     const size_t bidx = (size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi);
     const uint32_t e = __ldg(g.dir + bidx);
+    const uint32_t ow = octant_word(g, bidx);
     if (!brick_empty(e)) {
         const uint64_t* mk = g.masks + (size_t)e * 8;
         const int32_t ex = stx > 0 ? min((bxi << 3) + 8, g.nx) : (stx < 0 ? (bxi << 3) - 1 : INT_MIN);
@@ -102,7 +103,7 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
         }
     } else {
         int32_t lox, hix, loy, hiy, loz, hiz;
-        empty_box(g, e, bidx, bxi, byi, bzi, stx, sty, stz, R.oshift, lox, hix, loy, hiy, loz, hiz);
+        empty_box(g, e, ow, bxi, byi, bzi, stx, sty, stz, R.oshift, lox, hix, loy, hiy, loz, hiz);
         const int32_t nxe = stx > 0 ? hix - vx : vx - lox + 1;
         const int32_t nye = sty > 0 ? hiy - vy : vy - loy + 1;
         const int32_t nze = stz > 0 ? hiz - vz : vz - loz + 1;

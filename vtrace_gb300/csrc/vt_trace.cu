@@ -257,3 +257,105 @@ cudaError_t launch_trace_rays_persistent(const GridView& g, const vt_ray* rays, 
 }
 
 }  // namespace vt
+
+// ---------------------------------------------------------------------------------------------
+// Two-pass render ("wavefront"): the primary pass shades what it can and appends every needed
+// shadow ray to a compacted queue (one warp-aggregated atomic per warp, queue order = tile
+// order, so neighbouring queue entries are neighbouring pixels); the shadow pass traces full warps
+// of shadow rays, all parallel to the light, and finishes those pixels.  Same records as the
+// fused render_kernel.
+// ---------------------------------------------------------------------------------------------
+namespace vt {
+
+struct ShadowJob {
+    uint32_t pix;
+    float so[3];
+};
+
+__global__ void __launch_bounds__(256) render_primary_kernel(GridView g, vt_camera cam,
+                                                             LightView L,
+                                                             uint4* __restrict__ out,
+                                                             ShadowJob* __restrict__ queue,
+                                                             unsigned int* __restrict__ count) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t px = blockIdx.x * kTileW + (warp & 1u) * 8u + (lane & 7u);
+    const uint32_t py = blockIdx.y * kTileH + (warp >> 1) * 4u + (lane >> 3);
+    const bool inside = px < cam.width && py < cam.height;
+    bool need = false;
+    ShadowJob job;
+    if (inside) {
+        Tally<false> tl;
+        float o[3], d[3];
+        raygen(cam, px, py, 0.5f, 0.5f, o, d);
+        HitRec h = trace_ray<false>(g, o, d, tl);
+        const uint32_t flags = h.w1 >> 24;
+        float ndl;
+        if (!(flags & VT_HIT_FLAG_HIT)) {
+            h.w3 = VT_SKY_RGBA;
+        } else if (L.enabled && face_lit(h, L, ndl)) {
+            if (ndl > 0.0f && L.shadows) {
+                need = true;
+                job.pix = py * cam.width + px;
+                shadow_origin(h, o, d, job.so);
+            } else {
+                h.w3 = shade_rgba(h.w3, ndl, 1.0f, L.ambient);
+            }
+        }
+        out[(size_t)py * cam.width + px] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+    }
+    const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, need);
+    if (ballot) {
+        const int leader = __ffs(ballot) - 1;
+        unsigned int base = 0;
+        if ((int)lane == leader) base = atomicAdd(count, (unsigned int)__popc(ballot));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (need) queue[base + __popc(ballot & ((1u << lane) - 1u))] = job;
+    }
+}
+
+__global__ void __launch_bounds__(256) render_shadow_kernel(GridView g, LightView L,
+                                                            uint4* __restrict__ out,
+                                                            const ShadowJob* __restrict__ queue,
+                                                            const unsigned int* __restrict__ count) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *count) return;
+    const ShadowJob job = queue[i];
+    Tally<false> tl;
+    const float ld[3] = {L.dx, L.dy, L.dz};
+    const HitRec s = trace_ray<false>(g, job.so, ld, tl);
+    const bool shadowed = ((s.w1 >> 24) & VT_HIT_FLAG_HIT) != 0u;
+    uint4 h = out[job.pix];
+    HitRec r;
+    r.w0 = h.x;
+    r.w1 = h.y;
+    r.w2 = h.z;
+    r.w3 = h.w;
+    float ndl = 0.0f;
+    face_lit(r, L, ndl);
+    r.w3 = shade_rgba(r.w3, ndl, shadowed ? 0.0f : 1.0f, L.ambient);
+    r.w1 |= (VT_HIT_FLAG_SHADOW_RAY | (shadowed ? VT_HIT_FLAG_SHADOWED : 0u)) << 24;
+    out[job.pix] = make_uint4(r.w0, r.w1, r.w2, r.w3);
+}
+
+cudaError_t launch_render_wavefront(const GridView& g, const vt_camera& cam,
+                                    const LightView& light, uint4* out, cudaStream_t stream) {
+    const uint64_t npx = (uint64_t)cam.width * cam.height;
+    void* scratch = nullptr;
+    cudaError_t e = cudaMallocAsync(&scratch, 256 + npx * sizeof(ShadowJob), stream);
+    if (e != cudaSuccess) return e;
+    unsigned int* count = (unsigned int*)scratch;
+    ShadowJob* queue = (ShadowJob*)((char*)scratch + 256);
+    e = cudaMemsetAsync(count, 0, sizeof(unsigned int), stream);
+    if (e == cudaSuccess) {
+        dim3 grid((cam.width + kTileW - 1) / kTileW, (cam.height + kTileH - 1) / kTileH);
+        render_primary_kernel<<<grid, 256, 0, stream>>>(g, cam, light, out, queue, count);
+        if (light.enabled && light.shadows)
+            render_shadow_kernel<<<(unsigned)((npx + 255) / 256), 256, 0, stream>>>(g, light, out,
+                                                                                   queue, count);
+        e = cudaGetLastError();
+    }
+    const cudaError_t f = cudaFreeAsync(scratch, stream);
+    return e != cudaSuccess ? e : f;
+}
+
+}  // namespace vt
