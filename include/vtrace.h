@@ -185,6 +185,21 @@ int32_t vt_grid_create_u8_device(const uint8_t* d_voxels, const uint32_t* palett
 /* Build a brick grid from an x-fastest RGBA8 texel array (host), the format of the reference's
  * add_texture (lib/memory.c:286-385).  Occupied iff alpha > 0. */
 int32_t vt_grid_create_rgba8(const uint8_t* rgba, uint32_t nx, uint32_t ny, uint32_t nz);
+
+/* Element orders of a dense input array. */
+#define VT_ORDER_X_FASTEST 0u /* element (x, y, z) at x + nx*(y + ny*z): the order add_texture's
+                                 buffer-to-image copy reads (lib/memory.c:353-366) */
+#define VT_ORDER_Z_FASTEST 1u /* element (x, y, z) at z + nz*(y + ny*x): RawDynamicChunk::at
+                                 (src/voxel/rawchunk.rs:292) and RawStaticChunk's [x][y][z]
+                                 array (src/voxel/rawchunk.rs:19), the chunks the Rust host builds */
+/* Build a grid from a dense host array of u8 palette indices (format VT_PAYLOAD_U8, palette of 256
+ * RGBA8 required) or RGBA8 texels (VT_PAYLOAD_RGBA8, palette ignored) in either order: grid voxel
+ * (x, y, z) is the input's element (x, y, z).  Z-fastest input is reordered on the device.  The
+ * reference itself hands its z-fastest chunks to add_texture, whose copy reads them x-fastest
+ * (the x and z axes of the rendered texture are the chunk's z and x): that behaviour is
+ * add_texture's, and VT_ORDER_Z_FASTEST is the geometrically faithful reading. */
+int32_t vt_grid_create(const void* voxels, uint32_t format, uint32_t order,
+                       const uint32_t* palette, uint32_t nx, uint32_t ny, uint32_t nz);
 int32_t vt_grid_destroy(int32_t grid);
 /* No counterpart in the reference.  Builds the brick layout of an x-fastest u8 grid into buffers
  * the caller owns, allocating nothing, for callers that cannot allocate device memory while they
@@ -338,6 +353,32 @@ int32_t vt_serve_poll(int32_t service, uint64_t request_id, uint32_t timeout_us,
 int32_t vt_serve_get_stats(int32_t service, vt_serve_stats* out);
 /* Finish in-flight launches, cancel pending requests, free everything of the service. */
 int32_t vt_serve_stop(int32_t service);
+
+/* ---------------------------------------------------------------- MagicaVoxel models (host) */
+
+/* src/voxel/magica_voxel.rs:18-44 (dot_vox 4.1.0 for the file format).  `bytes` is a whole .vox
+ * file in host memory; nothing is read from disk. */
+typedef struct vt_vox_info {
+    uint32_t version;     /* the file's version field (150, 200, ...) */
+    uint32_t models;      /* SIZE + XYZI pairs, in file order */
+    uint32_t has_palette; /* 1 if an RGBA chunk is present */
+    uint32_t reserved;
+} vt_vox_info;
+typedef struct vt_vox_model {
+    uint32_t size[3]; /* the model's SIZE chunk: x, y, z (MagicaVoxel's z points up) */
+    uint32_t voxels;  /* voxels in its XYZI chunk */
+} vt_vox_model;
+int32_t vt_vox_inspect(const uint8_t* bytes, uint64_t size, vt_vox_info* info);
+int32_t vt_vox_model_info(const uint8_t* bytes, uint64_t size, uint32_t model, vt_vox_model* out);
+/* The texture load_magica_voxel builds from model `model`: a RawDynamicChunk<Color> of
+ * (size.x, size.y, size.z) voxels, z-fastest (VT_ORDER_Z_FASTEST), 4 bytes per voxel, zero where
+ * empty; voxel (x, y, z, c) lands at chunk coordinate (x, size.y - z - 1, y) with the RGBA chunk's
+ * entry c - 1.  Pass it to add_texture(rgba, size.x, size.y, size.z) for what vtrace renders, or
+ * to vt_grid_create(..., VT_ORDER_Z_FASTEST, ...) for the chunk's own geometry.  VT_EINVAL for a
+ * malformed file, a file without an RGBA chunk, a voxel outside the chunk (where vtrace panics)
+ * or a short buffer; VT_ENOTFOUND for a model index past the last model. */
+int32_t vt_vox_model_chunk(const uint8_t* bytes, uint64_t size, uint32_t model, uint8_t* rgba,
+                           uint64_t capacity_bytes);
 
 /* ---------------------------------------------------------------- scene generators (host) */
 

@@ -112,3 +112,39 @@ def test_reference_call_sequence(lib):
     L.cleanup()
     assert L.render_tick(ctypes.byref(w), ctypes.byref(h), ctypes.byref(info)) == -1
     assert L.add_texture(t0.ctypes.data, 16, 16, 16) == -1
+
+
+@pytest.mark.parametrize("load_dist,size", [(3, (320, 240)), (5, (256, 320))])
+def test_pager_world_with_instance_culling(lib, monkeypatch, load_dist, size):
+    """vtrace's own world shape (src/world.rs:136-190): hundreds of 16^3 terrain chunks around
+    the camera, some straddling it, and 121 entities, drawn through the per-tile instance bins;
+    the frame equals the oracle's loop over every instance."""
+    from vtrace_gb300 import workloads
+    w, h = size
+    world = workloads.pager_world(load_dist=load_dist, width=w, height=h)
+    monkeypatch.setenv("VTRACE_WIDTH", str(w))
+    monkeypatch.setenv("VTRACE_HEIGHT", str(h))
+    L = lib
+    assert L.entry() == 0
+    try:
+        for t in world["textures"]:
+            nz, ny, nx = t.shape
+            assert L.add_texture(t.ctypes.data, nx, ny, nz) >= 0
+        insts = world["instances"]
+        ptr = L.start_update_instances(len(insts))
+        ctypes.memmove(ptr, insts.ctypes.data, insts.nbytes)
+        assert L.end_update_instances(len(insts)) == 0
+        info = vt.RenderTickInfo(world["P"].ctypes.data, world["C"].ctypes.data)
+        ww, hh = ctypes.c_int32(0), ctypes.c_int32(0)
+        assert L.render_tick(ctypes.byref(ww), ctypes.byref(hh), ctypes.byref(info)) == 0
+        assert (ww.value, hh.value) == (w, h)
+        fb = np.zeros((h, w, 4), np.uint8)
+        assert L.vt_framebuffer_download(fb.ctypes.data, fb.nbytes) == 0
+    finally:
+        L.cleanup()
+    grids = [po.Grid(texels=t) for t in world["textures"]]
+    want = po.compat_render(grids, insts, world["P"], world["C"], w, h)
+    diff = np.nonzero((fb != want).any(-1))
+    assert len(diff[0]) == 0, (len(diff[0]), diff[0][:5], diff[1][:5])
+    sky = np.array([0xC0, 0xE8, 0xF6, 0xFF], np.uint8)
+    assert 0.05 < (fb != sky).any(-1).mean() < 0.99

@@ -30,6 +30,8 @@ FLAG_HIT = 0x80
 SKY_RGBA = 0xFFF6E8C0
 PAYLOAD_U8 = 1
 PAYLOAD_RGBA8 = 2
+ORDER_X_FASTEST = 0
+ORDER_Z_FASTEST = 1
 
 
 class VtError(RuntimeError):
@@ -119,6 +121,15 @@ class ServeStats(ctypes.Structure):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
 
 
+class VoxInfo(ctypes.Structure):
+    _fields_ = [("version", ctypes.c_uint32), ("models", ctypes.c_uint32),
+                ("has_palette", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class VoxModel(ctypes.Structure):
+    _fields_ = [("size", ctypes.c_uint32 * 3), ("voxels", ctypes.c_uint32)]
+
+
 class RenderTickInfo(ctypes.Structure):
     _fields_ = [("perspective", ctypes.c_void_p), ("camera", ctypes.c_void_p)]
 
@@ -145,6 +156,7 @@ SIGNATURES = [
     ("vt_grid_create_u8", _i32, [_vp, _vp, _u32, _u32, _u32]),
     ("vt_grid_create_u8_device", _i32, [_vp, _vp, _u32, _u32, _u32, _vp]),
     ("vt_grid_create_rgba8", _i32, [_vp, _u32, _u32, _u32]),
+    ("vt_grid_create", _i32, [_vp, _u32, _u32, _vp, _u32, _u32, _u32]),
     ("vt_grid_destroy", _i32, [_i32]),
     ("vt_grid_build_u8_noalloc", _i32, [_vp, _vp, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp]),
     ("vt_grid_get_info", _i32, [_i32, ctypes.POINTER(GridInfo)]),
@@ -170,6 +182,9 @@ SIGNATURES = [
     ("vt_serve_get_stats", _i32, [_i32, ctypes.POINTER(ServeStats)]),
     ("vt_serve_stop", _i32, [_i32]),
     ("vt_camera_look_at", _i32, [_vp, _vp, _vp, _f32, _u32, _u32, ctypes.POINTER(Camera)]),
+    ("vt_vox_inspect", _i32, [_vp, _u64, ctypes.POINTER(VoxInfo)]),
+    ("vt_vox_model_info", _i32, [_vp, _u64, _u32, ctypes.POINTER(VoxModel)]),
+    ("vt_vox_model_chunk", _i32, [_vp, _u64, _u32, _vp, _u64]),
     ("vt_gen_palette", _i32, [_u32, _vp]),
     ("vt_gen_terrain", _i32, [_u32, _u32, _u32, _u32, _u32, _f32, _vp]),
     ("vt_gen_shapes", _i32, [_u32, _u32, _u32, _u32, _u32, _f32, _f32, _vp]),
@@ -321,6 +336,36 @@ def make_light(direction, ambient=0.25, shadows=True):
     return L
 
 
+# ---------------------------------------------------------------- MagicaVoxel models
+
+def _vox_bytes(src):
+    if isinstance(src, (bytes, bytearray, memoryview)):
+        return np.frombuffer(bytes(src), np.uint8)
+    with open(src, "rb") as f:
+        return np.frombuffer(f.read(), np.uint8)
+
+
+def vox_inspect(src):
+    """src: a path or the bytes of a .vox file -> {"version", "models", "has_palette"}."""
+    b = _vox_bytes(src)
+    info = VoxInfo()
+    check(lib().vt_vox_inspect(b.ctypes.data, b.size, ctypes.byref(info)))
+    return {"version": info.version, "models": info.models, "has_palette": bool(info.has_palette)}
+
+
+def vox_model_chunk(src, model=0):
+    """The RGBA8 texture vtrace builds from a .vox model (src/voxel/magica_voxel.rs:18-44), as a
+    uint8 array indexed [x, y, z, channel] (the chunk's z-fastest order), shape
+    (size.x, size.y, size.z, 4)."""
+    b = _vox_bytes(src)
+    m = VoxModel()
+    check(lib().vt_vox_model_info(b.ctypes.data, b.size, model, ctypes.byref(m)))
+    sx, sy, sz = m.size
+    out = np.zeros((sx, sy, sz, 4), np.uint8)
+    check(lib().vt_vox_model_chunk(b.ctypes.data, b.size, model, out.ctypes.data, out.nbytes))
+    return out
+
+
 # ---------------------------------------------------------------- grids
 
 class Grid:
@@ -356,6 +401,26 @@ class Grid:
             a = a.astype(np.uint8, copy=False)
             nz, ny, nx, _ = a.shape
         return cls(check(lib().vt_grid_create_rgba8(a.ctypes.data, nx, ny, nz)))
+
+    @classmethod
+    def from_chunk(cls, data, palette=None):
+        """A z-fastest chunk (RawDynamicChunk order): numpy array indexed [x, y, z] of u8 palette
+        indices (palette required), or [x, y, z, 4] u8 / [x, y, z] u32 RGBA8 texels.  Grid voxel
+        (x, y, z) is data[x, y, z]."""
+        a = np.ascontiguousarray(data)
+        if palette is not None:
+            a = a.astype(np.uint8, copy=False)
+            nx, ny, nz = a.shape
+            pal = np.ascontiguousarray(palette, np.uint32)
+            return cls(check(lib().vt_grid_create(a.ctypes.data, PAYLOAD_U8, ORDER_Z_FASTEST,
+                                                  pal.ctypes.data, nx, ny, nz)))
+        if a.dtype == np.uint32:
+            nx, ny, nz = a.shape
+        else:
+            a = a.astype(np.uint8, copy=False)
+            nx, ny, nz, _ = a.shape
+        return cls(check(lib().vt_grid_create(a.ctypes.data, PAYLOAD_RGBA8, ORDER_Z_FASTEST, None,
+                                              nx, ny, nz)))
 
     def info(self):
         gi = GridInfo()

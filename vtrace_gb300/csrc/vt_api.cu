@@ -379,22 +379,27 @@ int32_t vt_grid_create_u8_device(const uint8_t* d_voxels, const uint32_t* palett
     return register_grid(std::move(g));
 }
 
-static int32_t create_from_host(const void* data, size_t elem, uint32_t format,
+static int32_t create_from_host(const void* data, size_t elem, uint32_t format, uint32_t order,
                                 const uint32_t* palette, uint32_t nx, uint32_t ny, uint32_t nz) {
     int32_t rc = check_dims(nx, ny, nz);
     if (rc) return rc;
     if ((rc = ensure_init())) return rc;
     const size_t bytes = (size_t)nx * ny * nz * elem;
+    const int nbuf = order == VT_ORDER_Z_FASTEST ? 2 : 1;
     void* d = nullptr;
-    if (cudaMalloc(&d, bytes) != cudaSuccess) {
+    if (cudaMalloc(&d, bytes * nbuf) != cudaSuccess) {
         cudaGetLastError();
         return fail(VT_ENOMEM, "cudaMalloc(dense grid upload) failed");
     }
     cudaStream_t st = state().stream;
-    cudaError_t e = cudaMemcpyAsync(d, data, bytes, cudaMemcpyHostToDevice, st);
+    // z-fastest input lands in the second half and is transposed into the first
+    void* up = (char*)d + bytes * (nbuf - 1);
+    cudaError_t e = cudaMemcpyAsync(up, data, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && nbuf == 2)
+        e = launch_transpose_xz(up, d, elem, (int32_t)nx, (int32_t)ny, (int32_t)nz, st);
     std::unique_ptr<Grid> g;
     if (e != cudaSuccess)
-        rc = cuda_fail(e, "cudaMemcpy(dense grid)");
+        rc = cuda_fail(e, "dense grid upload");
     else
         rc = build_grid(d, format, palette, nx, ny, nz, st, g);
     cudaStreamSynchronize(st);
@@ -403,15 +408,28 @@ static int32_t create_from_host(const void* data, size_t elem, uint32_t format,
     return register_grid(std::move(g));
 }
 
+int32_t vt_grid_create(const void* voxels, uint32_t format, uint32_t order,
+                       const uint32_t* palette, uint32_t nx, uint32_t ny, uint32_t nz) {
+    if (!voxels) return fail(VT_EINVAL, "vt_grid_create: null voxels");
+    if (format != VT_PAYLOAD_U8 && format != VT_PAYLOAD_RGBA8)
+        return fail(VT_EINVAL, "vt_grid_create: format must be VT_PAYLOAD_U8 or VT_PAYLOAD_RGBA8");
+    if (order != VT_ORDER_X_FASTEST && order != VT_ORDER_Z_FASTEST)
+        return fail(VT_EINVAL, "vt_grid_create: order must be VT_ORDER_X_FASTEST or VT_ORDER_Z_FASTEST");
+    if (format == VT_PAYLOAD_U8 && !palette)
+        return fail(VT_EINVAL, "vt_grid_create: a u8 grid needs a palette");
+    return create_from_host(voxels, format == VT_PAYLOAD_U8 ? 1 : 4, format, order,
+                            format == VT_PAYLOAD_U8 ? palette : nullptr, nx, ny, nz);
+}
+
 int32_t vt_grid_create_u8(const uint8_t* voxels, const uint32_t* palette, uint32_t nx,
                           uint32_t ny, uint32_t nz) {
     if (!voxels || !palette) return fail(VT_EINVAL, "vt_grid_create_u8: null pointer");
-    return create_from_host(voxels, 1, VT_PAYLOAD_U8, palette, nx, ny, nz);
+    return create_from_host(voxels, 1, VT_PAYLOAD_U8, VT_ORDER_X_FASTEST, palette, nx, ny, nz);
 }
 
 int32_t vt_grid_create_rgba8(const uint8_t* rgba, uint32_t nx, uint32_t ny, uint32_t nz) {
     if (!rgba) return fail(VT_EINVAL, "vt_grid_create_rgba8: null pointer");
-    return create_from_host(rgba, 4, VT_PAYLOAD_RGBA8, nullptr, nx, ny, nz);
+    return create_from_host(rgba, 4, VT_PAYLOAD_RGBA8, VT_ORDER_X_FASTEST, nullptr, nx, ny, nz);
 }
 
 int32_t vt_grid_destroy(int32_t grid) {

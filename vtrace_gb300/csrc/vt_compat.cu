@@ -34,8 +34,14 @@ constexpr uint32_t kMaxTextures = 65536;  // lib/common.h:35
 struct CompatInstance {
     float minv[12];  // inverse(model), rows 0..2 of the 4x4 (row-major)
     int32_t texture;
-    int32_t pad[3];
+    int32_t tx0, ty0, tx1, ty1;  // 16 x 16-pixel tiles its pixels can fall in (inclusive; empty
+                                 // when tx0 > tx1)
+    int32_t pad[2];
 };
+
+constexpr int32_t kTile = 16;
+// Bitmasks larger than this are not built; every tile then visits every instance.
+constexpr size_t kMaxBinBytes = (size_t)256 << 20;
 
 struct CompatFrame {
     float dirm[12];  // inverse(centered camera) * inverse(projection), rows 0..2
@@ -69,9 +75,56 @@ __device__ __forceinline__ uint32_t srgb_encode(float v) {
     return lo;
 }
 
+// Instance binning: bit i of word w of tile t is set iff instance 32 w + i may cover a pixel of
+// tile t.  One warp per (word, run of 32 tiles): each lane tests one instance's tile rectangle,
+// the ballot is the word.  Every word of every tile is written, so nothing needs clearing.
+__global__ void __launch_bounds__(256) compat_bin_kernel(const CompatInstance* __restrict__ inst,
+                                                         int32_t ninst, int32_t words,
+                                                         int32_t tiles_x, int32_t ntiles,
+                                                         uint32_t* __restrict__ bins) {
+    const int32_t lane = threadIdx.x & 31;
+    const int32_t w = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (w >= words) return;
+    const int32_t i = w * 32 + lane;
+    int32_t x0 = 1, y0 = 1, x1 = 0, y1 = 0;
+    if (i < ninst) {
+        x0 = inst[i].tx0;
+        y0 = inst[i].ty0;
+        x1 = inst[i].tx1;
+        y1 = inst[i].ty1;
+    }
+    const int32_t t_end = min(ntiles, (int32_t)(blockIdx.y + 1) * 32 * 8);
+    for (int32_t t = blockIdx.y * 32 * 8; t < t_end; ++t) {
+        const int32_t tx = t % tiles_x, ty = t / tiles_x;
+        const uint32_t b = __ballot_sync(0xFFFFFFFFu, tx >= x0 && tx <= x1 && ty >= y0 && ty <= y1);
+        if (lane == 0) bins[(size_t)t * words + w] = b;
+    }
+}
+
+// The instances of tile `tile` in draw order: all of them when there are no bins.
+struct InstanceCursor {
+    const uint32_t* bins;
+    int32_t ninst, words, w, i;
+    uint32_t bits;
+    __device__ InstanceCursor(const uint32_t* b, int32_t n, int32_t nw, int32_t tile)
+        : bins(b ? b + (size_t)tile * nw : nullptr), ninst(n), words(nw), w(-1), i(-1), bits(0) {}
+    // next instance index, or -1
+    __device__ __forceinline__ int32_t next() {
+        if (!bins) return ++i < ninst ? i : -1;
+        while (bits == 0) {
+            if (++w >= words) return -1;
+            bits = __ldg(bins + w);
+        }
+        const int32_t b = __ffs(bits) - 1;
+        bits &= bits - 1u;
+        return w * 32 + b;
+    }
+};
+
 __global__ void __launch_bounds__(256) compat_kernel(const GridView* __restrict__ views,
                                                      const CompatInstance* __restrict__ inst,
-                                                     int32_t ninst, CompatFrame f,
+                                                     int32_t ninst, const uint32_t* __restrict__ bins,
+                                                     int32_t words, CompatFrame f,
                                                      uchar4* __restrict__ fb) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const int32_t px = (int32_t)(blockIdx.x * 16 + (warp & 1u) * 8u + (lane & 7u));
@@ -93,7 +146,8 @@ __global__ void __launch_bounds__(256) compat_kernel(const GridView* __restrict_
     uint32_t cr = VT_SKY_RGBA & 0xFFu, cg = (VT_SKY_RGBA >> 8) & 0xFFu,
              cb = (VT_SKY_RGBA >> 16) & 0xFFu, ca = VT_SKY_RGBA >> 24;
     float depth = INFINITY;
-    for (int32_t i = 0; i < ninst; ++i) {
+    InstanceCursor cur(bins, ninst, words, (int32_t)(blockIdx.y * gridDim.x + blockIdx.x));
+    for (int32_t i = cur.next(); i >= 0; i = cur.next()) {
         const CompatInstance& I = inst[i];
         const GridView g = views[I.texture];
         float om[3], dm[3];
@@ -171,6 +225,8 @@ struct Compat {
     uint32_t views_capacity = 0;
     CompatInstance* d_inst = nullptr;
     uint32_t inst_capacity = 0;
+    uint32_t* d_bins = nullptr;  // per-tile instance bitmasks
+    size_t bins_capacity = 0;
     user_input input;
 };
 
@@ -222,6 +278,141 @@ static void mul4(const double* a, const double* b, double* c) {
         }
 }
 
+// Screen-space culling of instances.  The kernel's view ray of pixel (px, py) runs from the
+// camera `cam` along A (xn, yn) + c with xn = (px + 0.5) 2 / width - 1 and yn likewise (the
+// viewport is width x width, lib/command.c:81), where A's columns and c come from the direction
+// matrix.  A world point X lies on that ray at t > 0 iff B q = X - cam with B = [A c] has q.z > 0
+// and (q.x, q.y) / q.z = (xn, yn).  The cube's hit points therefore project into the projection
+// of the cube clipped to q.z >= eps, for any eps no larger than the nearest hit's q.z: every hit
+// is at least the cube's distance delta from the camera, and q.z = |X - cam| / |A (xn, yn) + c|,
+// so eps = delta / (largest ray length over the screen) loses nothing.  delta is bounded below by
+// the model-space distance of the camera to the unit cube over the Frobenius norm of the inverse
+// model matrix.  The clipped cube's vertices (corners with q.z >= eps, and edge crossings of
+// q.z = eps) give a pixel rectangle, widened by two pixels for the FP32 rounding of the kernel's
+// rays, in double precision throughout.
+struct CullFrame {
+    double binv[9];  // inverse of B, row-major
+    double cam[3];
+    double len_max;
+    int32_t width, height;
+    bool ok;
+};
+
+static bool invert3(const double* m, double* r) {
+    const double c00 = m[4] * m[8] - m[5] * m[7], c01 = m[5] * m[6] - m[3] * m[8],
+                 c02 = m[3] * m[7] - m[4] * m[6];
+    const double det = m[0] * c00 + m[1] * c01 + m[2] * c02;
+    if (!(det != 0.0) || !isfinite(det)) return false;
+    r[0] = c00 / det;
+    r[1] = (m[2] * m[7] - m[1] * m[8]) / det;
+    r[2] = (m[1] * m[5] - m[2] * m[4]) / det;
+    r[3] = c01 / det;
+    r[4] = (m[0] * m[8] - m[2] * m[6]) / det;
+    r[5] = (m[2] * m[3] - m[0] * m[5]) / det;
+    r[6] = c02 / det;
+    r[7] = (m[1] * m[6] - m[0] * m[7]) / det;
+    r[8] = (m[0] * m[4] - m[1] * m[3]) / det;
+    return true;
+}
+
+static CullFrame cull_frame(const double* dm, const double* cam, int32_t width, int32_t height) {
+    CullFrame cf;
+    cf.width = width;
+    cf.height = height;
+    double b[9];
+    for (int r = 0; r < 3; ++r) {
+        b[3 * r + 0] = dm[0 * 4 + r];
+        b[3 * r + 1] = dm[1 * 4 + r];
+        b[3 * r + 2] = dm[2 * 4 + r] + dm[3 * 4 + r];
+    }
+    cf.ok = invert3(b, cf.binv);
+    for (int r = 0; r < 3; ++r) cf.cam[r] = cam[r];
+    // |A (xn, yn) + c| is convex in (xn, yn): its maximum over the screen is at a corner
+    const double yn_max = 2.0 * height / width - 1.0;
+    cf.len_max = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        const double xn = (k & 1) ? 1.0 : -1.0, yn = (k & 2) ? yn_max : -1.0;
+        double l2 = 0.0;
+        for (int r = 0; r < 3; ++r) {
+            const double v = b[3 * r] * xn + b[3 * r + 1] * yn + b[3 * r + 2];
+            l2 += v * v;
+        }
+        cf.len_max = fmax(cf.len_max, sqrt(l2));
+    }
+    cf.ok = cf.ok && isfinite(cf.len_max) && cf.len_max > 0.0;
+    return cf;
+}
+
+// Tile rectangle of an instance (model matrix md, column-major; its inverse mi).  Returns false
+// when no pixel can see it.
+static bool instance_tiles(const CullFrame& cf, const double* md, const double* mi, int32_t& tx0,
+                           int32_t& ty0, int32_t& tx1, int32_t& ty1) {
+    const int32_t ntx = (cf.width + kTile - 1) / kTile, nty = (cf.height + kTile - 1) / kTile;
+    tx0 = 0;
+    ty0 = 0;
+    tx1 = ntx - 1;
+    ty1 = nty - 1;
+    if (!cf.ok) return true;
+    // camera in model space and its distance to the unit cube
+    double om[3], d2 = 0.0, fro = 0.0;
+    for (int r = 0; r < 3; ++r) {
+        om[r] = mi[0 * 4 + r] * cf.cam[0] + mi[1 * 4 + r] * cf.cam[1] + mi[2 * 4 + r] * cf.cam[2] +
+                mi[3 * 4 + r];
+        const double e = fmax(fabs(om[r]) - 0.5, 0.0);
+        d2 += e * e;
+        for (int k = 0; k < 3; ++k) fro += mi[k * 4 + r] * mi[k * 4 + r];
+    }
+    if (!(d2 > 0.0) || !isfinite(d2) || !(fro > 0.0) || !isfinite(fro)) return true;
+    const double eps = 0.5 * sqrt(d2) / sqrt(fro) / cf.len_max;
+    // corners in q space
+    double q[8][3];
+    for (int k = 0; k < 8; ++k) {
+        const double m[3] = {(k & 1) ? 0.5 : -0.5, (k & 2) ? 0.5 : -0.5, (k & 4) ? 0.5 : -0.5};
+        double x[3];
+        for (int r = 0; r < 3; ++r)
+            x[r] = md[0 * 4 + r] * m[0] + md[1 * 4 + r] * m[1] + md[2 * 4 + r] * m[2] +
+                   md[3 * 4 + r] - cf.cam[r];
+        for (int r = 0; r < 3; ++r)
+            q[k][r] = cf.binv[3 * r] * x[0] + cf.binv[3 * r + 1] * x[1] + cf.binv[3 * r + 2] * x[2];
+    }
+    double xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
+    int used = 0;
+    auto take = [&](const double* p) {
+        const double xn = p[0] / p[2], yn = p[1] / p[2];
+        xmin = fmin(xmin, xn);
+        xmax = fmax(xmax, xn);
+        ymin = fmin(ymin, yn);
+        ymax = fmax(ymax, yn);
+        ++used;
+    };
+    for (int k = 0; k < 8; ++k)
+        if (q[k][2] >= eps) take(q[k]);
+    for (int k = 0; k < 8; ++k)
+        for (int a = 0; a < 3; ++a) {
+            const int j = k | (1 << a);
+            if (j == k) continue;  // each edge once, from its lower corner
+            const double sa = q[k][2] - eps, sb = q[j][2] - eps;
+            if ((sa < 0.0) == (sb < 0.0)) continue;
+            const double u = sa / (sa - sb);
+            double p[3];
+            for (int r = 0; r < 3; ++r) p[r] = q[k][r] + u * (q[j][r] - q[k][r]);
+            p[2] = eps;
+            take(p);
+        }
+    if (used == 0) return false;  // the whole cube is behind the camera
+    if (!(isfinite(xmin) && isfinite(xmax) && isfinite(ymin) && isfinite(ymax))) return true;
+    // xn -> px: px = (xn + 1) width / 2 - 0.5, and yn -> py with the same width
+    const double hw = 0.5 * cf.width;
+    const double px0 = floor((xmin + 1.0) * hw - 0.5) - 2.0, px1 = ceil((xmax + 1.0) * hw - 0.5) + 2.0;
+    const double py0 = floor((ymin + 1.0) * hw - 0.5) - 2.0, py1 = ceil((ymax + 1.0) * hw - 0.5) + 2.0;
+    if (px1 < 0.0 || py1 < 0.0 || px0 > cf.width - 1 || py0 > cf.height - 1) return false;
+    tx0 = (int32_t)(fmax(px0, 0.0) / kTile);
+    tx1 = (int32_t)(fmin(px1, cf.width - 1.0) / kTile);
+    ty0 = (int32_t)(fmax(py0, 0.0) / kTile);
+    ty1 = (int32_t)(fmin(py1, cf.height - 1.0) / kTile);
+    return true;
+}
+
 static int32_t compat_upload_tables() {
     SrgbTables t;
     for (int i = 0; i < 256; ++i) t.decode[i] = (float)srgb_to_linear(i / 255.0);
@@ -237,12 +428,15 @@ static void compat_release_locked(Compat& c) {
     cudaFree(c.fb);
     cudaFree(c.d_views);
     cudaFree(c.d_inst);
+    cudaFree(c.d_bins);
     cudaFreeHost(c.host_instances);
     for (int32_t g : c.textures) vt_grid_destroy(g);
     c.textures.clear();
     c.fb = nullptr;
     c.d_views = nullptr;
     c.d_inst = nullptr;
+    c.d_bins = nullptr;
+    c.bins_capacity = 0;
     c.host_instances = nullptr;
     c.capacity = c.count = c.views_capacity = c.inst_capacity = 0;
     c.mapped = false;
@@ -354,6 +548,7 @@ int32_t render_tick(int32_t* window_width, int32_t* window_height, const render_
     for (int r = 0; r < 3; ++r) f.cam[r] = (float)ic[12 + r];  // inverse(camera) * (0,0,0,1)
     f.width = c.width;
     f.height = c.height;
+    const CullFrame cf = cull_frame(dm, ic + 12, c.width, c.height);
 
     // instances -> device records (texture id in the bits of element [3][3], trace.vert:38-40)
     std::vector<CompatInstance> recs;
@@ -373,6 +568,10 @@ int32_t render_tick(int32_t* window_width, int32_t* window_height, const render_
         for (int r = 0; r < 3; ++r)
             for (int k = 0; k < 4; ++k) ci.minv[4 * r + k] = (float)mi[k * 4 + r];
         ci.texture = tid;
+        if (!instance_tiles(cf, md, mi, ci.tx0, ci.ty0, ci.tx1, ci.ty1)) {
+            ci.tx0 = 1;  // empty rectangle: in no tile
+            ci.tx1 = 0;
+        }
         recs.push_back(ci);
     }
     cudaStream_t st = state().stream;
@@ -403,8 +602,25 @@ int32_t render_tick(int32_t* window_width, int32_t* window_height, const render_
     if (e == cudaSuccess && !recs.empty())
         e = cudaMemcpyAsync(c.d_inst, recs.data(), recs.size() * sizeof(CompatInstance), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return -1;
-    dim3 grid((c.width + 15) / 16, (c.height + 15) / 16);
-    compat_kernel<<<grid, 256, 0, st>>>(c.d_views, c.d_inst, (int32_t)recs.size(), f, c.fb);
+    dim3 grid((c.width + kTile - 1) / kTile, (c.height + kTile - 1) / kTile);
+    const int32_t ninst = (int32_t)recs.size();
+    const int32_t words = (ninst + 31) / 32, ntiles = (int32_t)(grid.x * grid.y);
+    const size_t bin_bytes = (size_t)ntiles * words * 4;
+    uint32_t* bins = nullptr;
+    if (ninst > 0 && bin_bytes <= kMaxBinBytes) {
+        if (bin_bytes > c.bins_capacity) {
+            cudaFree(c.d_bins);
+            c.d_bins = nullptr;
+            c.bins_capacity = 0;
+            if (cudaMalloc(&c.d_bins, bin_bytes) != cudaSuccess) return -1;
+            c.bins_capacity = bin_bytes;
+        }
+        bins = c.d_bins;
+        const dim3 bgrid((words + 7) / 8, (ntiles + 255) / 256);
+        compat_bin_kernel<<<bgrid, 256, 0, st>>>(c.d_inst, ninst, words, (int32_t)grid.x, ntiles,
+                                                 bins);
+    }
+    compat_kernel<<<grid, 256, 0, st>>>(c.d_views, c.d_inst, ninst, bins, words, f, c.fb);
     if (cudaGetLastError() != cudaSuccess) return -1;
     // the host vectors above are staged by the copies: wait before they go out of scope
     if (cudaStreamSynchronize(st) != cudaSuccess) return -1;

@@ -433,3 +433,46 @@ cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t 
 }
 
 }  // namespace vt
+
+// ---------------------------------------------------------------------------------------------
+// Order conversion of dense input: z-fastest (src/voxel/rawchunk.rs:292, element (x, y, z) at
+// z + nz * (y + ny * x)) to the x-fastest order the brick build reads.  Each y-plane is an
+// nx x nz matrix stored row-major by x; 32 x 32 tiles are staged through shared memory so that
+// both the reads (along z) and the writes (along x) are contiguous per warp.
+// ---------------------------------------------------------------------------------------------
+namespace vt {
+
+template <typename T>
+__global__ void __launch_bounds__(256) transpose_xz_kernel(const T* __restrict__ src,
+                                                           T* __restrict__ dst, int32_t nx,
+                                                           int32_t ny, int32_t nz) {
+    __shared__ T tile[32][33];
+    const int32_t z0 = blockIdx.x * 32, x0 = blockIdx.y * 32;
+    const size_t y = blockIdx.z;
+    const int32_t tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+#pragma unroll
+    for (int32_t r = ty; r < 32; r += 8) {
+        const int32_t x = x0 + r, z = z0 + tx;
+        if (x < nx && z < nz) tile[r][tx] = src[(size_t)z + (size_t)nz * (y + (size_t)ny * x)];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int32_t r = ty; r < 32; r += 8) {
+        const int32_t z = z0 + r, x = x0 + tx;
+        if (x < nx && z < nz) dst[(size_t)x + (size_t)nx * (y + (size_t)ny * z)] = tile[tx][r];
+    }
+}
+
+cudaError_t launch_transpose_xz(const void* src, void* dst, size_t elem, int32_t nx, int32_t ny,
+                                int32_t nz, cudaStream_t stream) {
+    const dim3 grid((nz + 31) / 32, (nx + 31) / 32, ny);
+    if (elem == 1)
+        transpose_xz_kernel<uint8_t><<<grid, 256, 0, stream>>>((const uint8_t*)src, (uint8_t*)dst,
+                                                               nx, ny, nz);
+    else
+        transpose_xz_kernel<uint32_t><<<grid, 256, 0, stream>>>((const uint32_t*)src,
+                                                                (uint32_t*)dst, nx, ny, nz);
+    return cudaGetLastError();
+}
+
+}  // namespace vt

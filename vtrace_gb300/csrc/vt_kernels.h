@@ -57,6 +57,10 @@ cudaError_t launch_brick_words(const void* src, uint32_t format, const uint32_t*
                                int32_t nx, int32_t ny, int32_t nz, const BuildScratch& s,
                                cudaStream_t stream);
 cudaError_t launch_brick_scan(const BuildScratch& s, uint64_t bricks, cudaStream_t stream);
+// Dense z-fastest input (element size 1 or 4) to x-fastest; y-planes are transposed in place of
+// the x and z axes.  grid.y = ceil(nx / 32) and grid.z = ny must stay within 65535.
+cudaError_t launch_transpose_xz(const void* src, void* dst, size_t elem, int32_t nx, int32_t ny,
+                                int32_t nz, cudaStream_t stream);
 // Phase 3: directory, compacted masks and payloads.
 cudaError_t launch_brick_compact(const void* src, uint32_t format, int32_t nx, int32_t ny,
                                  int32_t nz, const BuildScratch& s, uint32_t* dir,

@@ -152,3 +152,93 @@ def serving_requests(scenes, count, rate=2000.0, seed=6, min_px=320 * 240, max_p
                      "spp": int(rng.integers(1, max_spp + 1)), "seed": k, "view_id": k,
                      "light": seeded_light(seed * 100000 + k, shadows=False)})
     return reqs
+
+
+def _value_noise2(x, z, seed, cell):
+    """Smooth 2D value noise in [0, 1) at integer coordinates (numpy arrays), lattice spacing
+    `cell`, from a seeded integer hash."""
+    def h(ix, iz):
+        v = (ix.astype(np.int64) * 374761393 + iz.astype(np.int64) * 668265263 + seed * 2246822519)
+        v = (v ^ (v >> 13)) * 1274126177
+        return ((v ^ (v >> 16)) & 0xFFFF).astype(np.float64) / 65536.0
+    fx, fz = x / cell, z / cell
+    ix, iz = np.floor(fx).astype(np.int64), np.floor(fz).astype(np.int64)
+    ux, uz = fx - ix, fz - iz
+    ux, uz = ux * ux * (3 - 2 * ux), uz * uz * (3 - 2 * uz)
+    a, b = h(ix, iz), h(ix + 1, iz)
+    c, d = h(ix, iz + 1), h(ix + 1, iz + 1)
+    return (a + (b - a) * ux) + ((c + (d - c) * ux) - (a + (b - a) * ux)) * uz
+
+
+def pager_world(load_dist=10, chunk=16, seed=7, entity_sizes=(40, 50), width=1000, height=1000):
+    """The shape of vtrace's own world (src/world.rs:136-190, src/gen/pager.rs): terrain chunks of
+    chunk^3 voxels on a 2-unit lattice within `load_dist` chunks of the camera's chunk, one texture
+    and one instance (translate * scale 2) per chunk holding any voxel, and 11 x 11 entity
+    instances (unit cubes at (1.5 x, -5, 1.5 z)) alternating two voxel models.  Terrain is a
+    seeded value-noise heightfield (the build's own content).  Returns textures (x-fastest RGBA8
+    [z, y, x] uint32 arrays), instances (column-major float32 [n, 16] with the texture index in
+    the bits of element 15), and the perspective and camera matrices of src/render.rs:190-214."""
+    rng = np.random.default_rng(seed)
+    pal = gen_palette(seed)
+    R = load_dist
+    textures, instances = [], []
+
+    def inst(tx, ty, tz, s, tid):
+        m = np.zeros(16, np.float32)
+        m[0] = m[5] = m[10] = s
+        m[12], m[13], m[14] = tx, ty, tz
+        m[15] = np.array([tid], np.int32).view(np.float32)[0]
+        return m
+
+    # entity models: random blobs of boxes (stand-ins for the .vox assets, 40^3 and 50^3)
+    ent = []
+    for n in entity_sizes:
+        t = np.zeros((n, n, n), np.uint32)
+        for _ in range(12):
+            lo = rng.integers(0, n - 4, 3)
+            hi = np.minimum(lo + rng.integers(3, max(4, n // 3), 3), n)
+            t[lo[2]:hi[2], lo[1]:hi[1], lo[0]:hi[0]] = pal[int(rng.integers(1, 256))] | 0xFF000000
+        ent.append(len(textures))
+        textures.append(t)
+    for x in range(-5, 6):
+        for z in range(-5, 6):
+            instances.append(inst(x * 1.5, -5.0, z * 1.5, 1.0, ent[0] if (x + z + 10) % 2 == 0 else ent[1]))
+    # terrain: height in voxels over the world's voxel columns (8 voxels per world unit)
+    vox_per_unit = chunk / 2.0
+    span = np.arange(-R * chunk, (R + 1) * chunk)
+    gx, gz = np.meshgrid(span, span, indexing="xy")  # [z, x]
+    hgt = (-8.0 + 40.0 * _value_noise2(gx, gz, seed, 48.0) + 10.0 * _value_noise2(gx, gz, seed + 1, 13.0))
+    ys = np.arange(chunk)
+    for cz in range(-R, R + 1):
+        for cy in range(-R, R + 1):
+            for cx in range(-R, R + 1):
+                h = hgt[(cz + R) * chunk:(cz + R + 1) * chunk, (cx + R) * chunk:(cx + R + 1) * chunk]
+                vy = cy * chunk + ys
+                solid = vy[:, None, None] < h[None, :, :]          # [y, z, x]
+                if not solid.any():
+                    continue
+                depth = h[None, :, :] - vy[:, None, None]
+                idx = np.clip((depth * 3).astype(np.int64) % 255 + 1, 1, 255)
+                t = np.where(solid, pal[idx] | np.uint32(0xFF000000), 0).astype(np.uint32)
+                textures.append(np.ascontiguousarray(t.transpose(1, 0, 2)))  # [z, y, x]
+                instances.append(inst(cx * 2.0, cy * 2.0, cz * 2.0, 2.0, len(textures) - 1))
+    from math import tan
+    fov = 80.0 / 180.0 * 3.1415926
+    f = 1.0 / tan(fov / 2.0)
+    near, far = 0.01, 10000.0
+    P = np.zeros(16, np.float32)
+    P[0], P[5] = f / (width / height), f
+    P[10], P[11], P[14] = (far + near) / (near - far), -1.0, 2.0 * far * near / (near - far)
+    eye = np.array([0.3, float(hgt[R * chunk, R * chunk]) / vox_per_unit + 2.5, 0.2])
+    d = np.array([0.8, -0.35, 0.45])
+    d /= np.linalg.norm(d)
+    s = np.cross(d, [0.0, 1.0, 0.0])
+    s /= np.linalg.norm(s)
+    u = np.cross(s, d)
+    C = np.eye(4)
+    C[0, :3], C[1, :3], C[2, :3] = s, u, -d
+    C[:3, 3] = [-s @ eye, -u @ eye, d @ eye]
+    C = np.ascontiguousarray(C.T, np.float32).reshape(16)
+    return {"name": "pager_world_r%d" % R, "textures": textures,
+            "instances": np.stack(instances).astype(np.float32), "P": P, "C": C,
+            "width": width, "height": height}
