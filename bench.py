@@ -45,7 +45,8 @@ def parse_args():
     p.add_argument("--steps", type=int, default=50)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--config", choices=["shapes1024", "terrain256", "cave512", "multiview", "serve"],
+    p.add_argument("--config", choices=["shapes1024", "terrain256", "cave512", "multiview", "serve",
+                                        "pager_world"],
                    default="shapes1024")
     p.add_argument("--serve-requests", type=int, default=1000,
                    help="requests of the serving comparison added to the headline run (0: skip)")
@@ -451,6 +452,57 @@ def run_config(args):
             x.destroy()
         for gr in grids:
             gr.destroy()
+    elif args.config == "pager_world":
+        # the reference-compatible frame (render_tick) over vtrace's own world shape
+        import ctypes
+        world = workloads.pager_world()
+        os.environ["VTRACE_WIDTH"], os.environ["VTRACE_HEIGHT"] = (str(world["width"]),
+                                                                  str(world["height"]))
+        L = vt.lib()
+        assert L.entry() == 0
+        t0 = time.perf_counter()
+        for t in world["textures"]:
+            nz, ny, nx = t.shape
+            vt.check(L.add_texture(t.ctypes.data, nx, ny, nz))
+        upload_s = time.perf_counter() - t0
+        insts = world["instances"]
+        ptr = L.start_update_instances(len(insts))
+        ctypes.memmove(ptr, insts.ctypes.data, insts.nbytes)
+        vt.check(L.end_update_instances(len(insts)))
+        info = vt.RenderTickInfo(world["P"].ctypes.data, world["C"].ctypes.data)
+        ww, hh = ctypes.c_int32(0), ctypes.c_int32(0)
+        lib_stream = torch.cuda.ExternalStream(L.vt_get_stream())
+        tick = lambda: vt.check(L.render_tick(ctypes.byref(ww), ctypes.byref(hh), ctypes.byref(info)))
+        # device time of the frame's launches (binning + per-pixel kernel) on the library stream
+        ms = autotune.time_ms(tick, lib_stream, repeats=args.steps, warmup=args.warmup, flush=flush)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            tick()
+        e2e_ms = (time.perf_counter() - t0) / args.steps * 1e3
+        fb = np.zeros((hh.value, ww.value, 4), np.uint8)
+        vt.check(L.vt_framebuffer_download(fb.ctypes.data, fb.nbytes))
+        L.cleanup()
+        px = world["width"] * world["height"]
+        line.update(metric="Mpixels/s (render_tick, %dx%d, %d instances)" % (
+                        world["width"], world["height"], len(insts)),
+                    value=px / ms / 1e3, unit="Mpixels/s", ms_per_step=ms,
+                    config={"workload": world["name"], "textures": len(world["textures"]),
+                            "instances": len(insts), "texture_upload_s": upload_s},
+                    e2e={"value": px / e2e_ms / 1e3, "unit": "Mpixels/s",
+                         "h2d_bytes_per_step": int(insts.nbytes) + 128, "d2h_bytes_per_step": 0,
+                         "path": "render_tick (C ABI), host wall clock"},
+                    gpu_launches=2 * args.steps)
+        if not args.no_cpu_baseline:
+            from oracle import pyoracle as po
+            grids = [po.Grid(texels=t) for t in world["textures"]]
+            t0 = time.perf_counter()
+            want = po.compat_render(grids, insts, world["P"], world["C"], world["width"],
+                                    world["height"])
+            cpu_s = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": px / cpu_s / 1e6, "unit": "Mpixels/s",
+                                    "cores": po.hardware_threads(), "kind": "port",
+                                    "sample": "the whole frame, every instance per pixel"}
+            line["parity"] = {"pixels_differing_from_oracle": int((fb != want).any(-1).sum())}
     else:  # serve
         r = serve_compare(max(args.serve_requests, 2000))
         line.update(metric="serve p50/p99 latency and Msamples/s vs plain per-request launches",
@@ -465,7 +517,7 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.config in ("cave512", "multiview", "serve"):
+    if args.config in ("cave512", "multiview", "serve", "pager_world"):
         return run_config(args)
     return run_ours(args)
 

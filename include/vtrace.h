@@ -149,6 +149,10 @@ const char* vt_last_error(void);
 uint32_t vt_version(void);
 /* Device the library runs on and its SM count; for sizing persistent launches. */
 int32_t vt_device_info(int32_t* device, int32_t* sm_count, uint64_t* free_bytes, uint64_t* total_bytes);
+/* The library's own stream (a cudaStream_t): the stream of calls given a NULL stream and of the
+ * reference-compatible entry points.  Callers order their own work after the library's on it.
+ * Initialises the library; NULL if that fails. */
+void* vt_get_stream(void);
 
 /* Launch shape of a tracing entry point.  persistent = 0: one thread per ray, rays packed in
  * 8 x 4 pixel tiles per warp.  persistent = 1: resident warps keep one ray per lane and refill

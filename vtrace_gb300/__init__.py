@@ -151,6 +151,7 @@ SIGNATURES = [
     ("vt_last_error", ctypes.c_char_p, []),
     ("vt_version", _u32, []),
     ("vt_device_info", _i32, [_vp, _vp, _vp, _vp]),
+    ("vt_get_stream", _vp, []),
     ("vt_get_tuning", _i32, [_i32, ctypes.POINTER(Tuning)]),
     ("vt_set_tuning", _i32, [_i32, ctypes.POINTER(Tuning)]),
     ("vt_grid_create_u8", _i32, [_vp, _vp, _u32, _u32, _u32]),

@@ -320,6 +320,11 @@ const char* vt_last_error(void) { return g_last_error.c_str(); }
 
 uint32_t vt_version(void) { return (1u << 16) | 0u; }
 
+void* vt_get_stream(void) {
+    if (ensure_init()) return nullptr;
+    return (void*)state().stream;
+}
+
 int32_t vt_device_info(int32_t* device, int32_t* sm_count, uint64_t* free_bytes,
                        uint64_t* total_bytes) {
     int32_t rc = ensure_init();
