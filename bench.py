@@ -46,7 +46,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", choices=["shapes1024", "terrain256", "cave512", "multiview", "serve",
-                                        "pager_world"],
+                                        "pager_world", "pathtrace"],
                    default="shapes1024")
     p.add_argument("--serve-requests", type=int, default=1000,
                    help="requests of the serving comparison added to the headline run (0: skip)")
@@ -452,6 +452,49 @@ def run_config(args):
             x.destroy()
         for gr in grids:
             gr.destroy()
+    elif args.config == "pathtrace":
+        # multi-bounce diffuse path tracing over the 1024^3 shapes grid at 1080p
+        w = workloads.shapes1024()
+        g = vt.Grid.from_u8(w["voxels"], w["palette"])
+        cam = w["camera"]
+        p = vt.make_path_params(spp=2, max_bounces=3, seed=1, sun_dir=tuple(w["light"].dir))
+        d_out = torch.empty(cam.width * cam.height * 16, dtype=torch.uint8, device="cuda")
+        d_rays = torch.zeros(1, dtype=torch.int64, device="cuda")
+        vt.path_trace(g, cam, p, d_out, d_rays, stream)
+        torch.cuda.synchronize()
+        rays = int(d_rays.item())
+        ms = autotune.time_ms(lambda: vt.path_trace(g, cam, p, d_out, None, stream), stream,
+                              repeats=args.steps, warmup=args.warmup, flush=flush)
+        p8 = vt.make_path_params(spp=2, max_bounces=3, seed=1, sun_dir=tuple(w["light"].dir),
+                                 out_format=vt.PATH_OUT_RGBA8)
+        vt.path_trace_host(g, cam, p8)
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps // 4)):
+            vt.path_trace_host(g, cam, p8)
+        e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 4)
+        line.update(metric="Mrays/s (path tracing, 1080p, 1024^3 grid, 2 spp, 3 bounces + sun)",
+                    value=rays / ms / 1e3, unit="Mrays/s", ms_per_step=ms,
+                    config={"workload": w["name"] + "_pt_spp2_b3", "rays_per_frame": rays,
+                            "samples_per_frame": cam.width * cam.height * 2},
+                    e2e={"value": rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 96,
+                         "d2h_bytes_per_step": cam.width * cam.height * 4,
+                         "path": "vt_path_trace_host (C ABI), RGBA8 out"},
+                    gpu_launches=args.steps)
+        if not args.no_cpu_baseline:
+            from oracle import pyoracle as po
+            og = po.Grid(w["voxels"], w["palette"])
+            op = po.make_path_params(2, 3, 1, list(p.sky), list(p.sun_dir), list(p.sun))
+            rows = (cam.height // 2 - 4, cam.height // 2 + 4)
+            t0 = time.perf_counter()
+            band, band_rays = po.path_trace(og, po.make_camera(cam.as_dict()), op, rows=rows)
+            cpu_s = time.perf_counter() - t0
+            got = d_out.cpu().numpy().view(np.float32).reshape(cam.height, cam.width, 4)
+            line["cpu_baseline"] = {"value": band_rays / cpu_s / 1e6, "unit": "Mrays/s",
+                                    "cores": po.hardware_threads(), "kind": "port",
+                                    "sample": "rows %d-%d of the frame (%d rays)" % (rows[0], rows[1] - 1, band_rays)}
+            line["parity"] = {"band_pixels_differing_from_oracle":
+                              int((got[rows[0]:rows[1]] != band).any(-1).sum())}
+        g.destroy()
     elif args.config == "pager_world":
         # the reference-compatible frame (render_tick) over vtrace's own world shape
         import ctypes
@@ -517,7 +560,7 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.config in ("cave512", "multiview", "serve", "pager_world"):
+    if args.config in ("cave512", "multiview", "serve", "pager_world", "pathtrace"):
         return run_config(args)
     return run_ours(args)
 

@@ -264,6 +264,34 @@ int32_t vt_trace_rays_stats(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_h
 int32_t vt_camera_look_at(const float eye[3], const float target[3], const float up[3],
                           float vfov_degrees, uint32_t width, uint32_t height, vt_camera* out);
 
+/* ---------------------------------------------------------------- path tracing */
+
+/* Multi-bounce diffuse path tracing on the same traversal (vtrace's stated goal, README.md:2; no
+ * counterpart in the reference's code).  Per sample: a Philox-jittered camera ray; at every hit
+ * the throughput takes the voxel colour (byte / 255), a next-event ray toward the sun adds
+ * throughput * sun * n.l when unblocked, and the path continues along a cosine-weighted
+ * direction about the face normal, for at most max_bounces bounces; rays leaving the grid add
+ * throughput * sky.  Radiance is averaged over spp samples in sample order.  Deterministic for a
+ * given seed and bit-identical to the library's CPU restatement. */
+#define VT_PATH_OUT_F32X4 0u /* float4 (r, g, b, 1) per pixel, linear radiance */
+#define VT_PATH_OUT_RGBA8 1u /* u32 per pixel: clamp(c, 0, 1) * 255 rounded half up, alpha 255 */
+typedef struct vt_path_params {
+    uint32_t spp;         /* samples per pixel, 1..65536 */
+    uint32_t max_bounces; /* bounces after the camera ray's hit, 0..64 */
+    uint32_t seed;
+    uint32_t out_format;  /* VT_PATH_OUT_* */
+    float sky[3];         /* radiance of rays that leave the grid */
+    float sun_dir[3];     /* unit direction toward the sun */
+    float sun[3];         /* sun irradiance; all zero: no next-event rays */
+} vt_path_params;
+/* d_out: width*height pixels of the chosen format (device, 16-byte aligned).  d_rays_traced:
+ * NULL or a device u64 the launch adds the number of rays it traced to. */
+int32_t vt_path_trace(int32_t grid, const vt_camera* camera, const vt_path_params* params,
+                      void* d_out, uint64_t* d_rays_traced, void* stream);
+/* Synchronous, host output; rays_traced may be NULL. */
+int32_t vt_path_trace_host(int32_t grid, const vt_camera* camera, const vt_path_params* params,
+                           void* out, uint64_t* rays_traced);
+
 /* ---------------------------------------------------------------- batched multi-view */
 
 /* One view of a batch: a camera over a grid with `spp` jittered samples per pixel.  Sample s of

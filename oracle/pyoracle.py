@@ -274,3 +274,42 @@ def compat_render(grids, instances, P, C, width, height, threads=0):
     if rc != 0:
         raise ValueError("singular projection or camera matrix")
     return out
+
+
+class PathParams(ctypes.Structure):
+    _fields_ = [("spp", ctypes.c_uint32), ("max_bounces", ctypes.c_uint32),
+                ("seed", ctypes.c_uint32), ("out_format", ctypes.c_uint32),
+                ("sky", ctypes.c_float * 3), ("sun_dir", ctypes.c_float * 3),
+                ("sun", ctypes.c_float * 3)]
+
+
+def make_path_params(spp, max_bounces, seed, sky, sun_dir, sun):
+    p = PathParams()
+    p.spp, p.max_bounces, p.seed, p.out_format = spp, max_bounces, seed, 0
+    p.sky[:], p.sun_dir[:], p.sun[:] = list(sky), list(sun_dir), list(sun)
+    return p
+
+
+def path_trace(grid, camera, params, threads=0, rows=None):
+    """The path-tracing estimator restated: (float32 [rows, width, 4], rays traced) for the rows
+    (row0, row1) of the image (all by default)."""
+    L = lib()
+    r0, r1 = rows if rows is not None else (0, camera.height)
+    out = np.zeros((r1 - r0, camera.width, 4), np.float32)
+    rays = ctypes.c_uint64(0)
+    L.vto_path_trace.argtypes = [ctypes.POINTER(_Grid), ctypes.POINTER(Camera),
+                                 ctypes.POINTER(PathParams), ctypes.c_uint32, ctypes.c_uint32,
+                                 ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
+    L.vto_path_trace.restype = None
+    L.vto_path_trace(ctypes.byref(grid._g), ctypes.byref(camera), ctypes.byref(params), r0, r1,
+                     _ptr(out), threads, ctypes.byref(rays))
+    return out, rays.value
+
+
+def path_rgba8(img):
+    """VT_PATH_OUT_RGBA8 of a float image: clamp to [0, 1], x 255 + 0.5 truncated, alpha 255."""
+    c = np.clip(img[..., :3], np.float32(0), np.float32(1)).astype(np.float32)
+    q = (c * np.float32(255.0) + np.float32(0.5)).astype(np.uint32)
+    out = np.full(img.shape[:2] + (4,), 255, np.uint8)
+    out[..., :3] = q.astype(np.uint8)
+    return out

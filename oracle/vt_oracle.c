@@ -411,6 +411,91 @@ void vto_shade_sample(const vto_grid* g, const vto_camera* cam, const vto_light*
     shade_from_ray(g, light, o, d, out, stats);
 }
 
+/* ------------------------------------------------------------------ path tracing */
+
+/* The library's path-tracing estimator (vt_path.cu's header states it; vtrace itself has none). */
+static int sphere_sample(uint32_t seed, uint32_t px, uint32_t py, uint32_t s, uint32_t bounce,
+                         float u[3]) {
+    for (uint32_t t = 0; t < 16; ++t) {
+        const uint32_t ctr[4] = {px, py, s, (bounce << 8) | t};
+        const uint32_t key[2] = {seed, 0x50415448u};
+        uint32_t r[4];
+        vto_philox4x32_10(ctr, key, r);
+        float p[3];
+        for (int k = 0; k < 3; ++k) p[k] = (float)(r[k] >> 8) * 0x1p-23f - 1.0f;
+        const float r2 = (p[0] * p[0] + p[1] * p[1]) + p[2] * p[2];
+        if (r2 <= 1.0f && r2 > 0x1p-20f) {
+            const float l = sqrtf(r2);
+            for (int k = 0; k < 3; ++k) u[k] = p[k] / l;
+            return 1;
+        }
+    }
+    return 0;
+}
+
+void vto_path_pixel(const vto_grid* g, const vto_camera* cam, const vto_path_params* P,
+                    uint32_t px, uint32_t py, float out[3], uint64_t* rays) {
+    int sun_on = 0;
+    for (int c = 0; c < 3; ++c)
+        if (P->sun[c] > 0.0f) sun_on = 1;
+    float sum[3] = {0.0f, 0.0f, 0.0f};
+    for (uint32_t s = 0; s < P->spp; ++s) {
+        float jx, jy, o[3], d[3];
+        vto_jitter(P->seed, 0u, px, py, s, &jx, &jy);
+        vto_raygen(cam, px, py, jx, jy, o, d);
+        float T[3] = {1.0f, 1.0f, 1.0f}, L[3] = {0.0f, 0.0f, 0.0f};
+        for (uint32_t b = 0;; ++b) {
+            vto_hit h;
+            vto_trace_ray_f32(g, o, d, &h, NULL);
+            ++*rays;
+            if (!(h.face & VTO_FLAG_HIT)) {
+                for (int c = 0; c < 3; ++c) L[c] = L[c] + T[c] * P->sky[c];
+                break;
+            }
+            const int face = h.face & 7;
+            if (face == 0) break;
+            for (int c = 0; c < 3; ++c) T[c] = T[c] * ((float)((h.rgba >> (8 * c)) & 0xFFu) / 255.0f);
+            const int a = (face - 1) / 2;
+            const int npos = (face & 1) != 0;
+            const int32_t hv[3] = {h.x, h.y, h.z};
+            const float plane = (float)(npos ? hv[a] + 1 : hv[a]);
+            float so[3];
+            for (int k = 0; k < 3; ++k) so[k] = o[k] + h.t * d[k];
+            so[a] = npos ? plane + 0.015625f : plane - 0.015625f;
+            if (sun_on) {
+                const float ndl = npos ? P->sun_dir[a] : -P->sun_dir[a];
+                if (ndl > 0.0f) {
+                    vto_hit sh;
+                    vto_trace_ray_f32(g, so, P->sun_dir, &sh, NULL);
+                    ++*rays;
+                    if (!(sh.face & VTO_FLAG_HIT))
+                        for (int c = 0; c < 3; ++c) L[c] = L[c] + (T[c] * P->sun[c]) * ndl;
+                }
+            }
+            if (b >= P->max_bounces) break;
+            float n[3] = {0.0f, 0.0f, 0.0f}, u[3], nd[3];
+            n[a] = npos ? 1.0f : -1.0f;
+            if (sphere_sample(P->seed, px, py, s, b, u)) {
+                for (int k = 0; k < 3; ++k) nd[k] = n[k] + u[k];
+                const float l = sqrtf((nd[0] * nd[0] + nd[1] * nd[1]) + nd[2] * nd[2]);
+                if (l > 1e-6f)
+                    for (int k = 0; k < 3; ++k) nd[k] = nd[k] / l;
+                else
+                    for (int k = 0; k < 3; ++k) nd[k] = n[k];
+            } else {
+                for (int k = 0; k < 3; ++k) nd[k] = n[k];
+            }
+            for (int k = 0; k < 3; ++k) {
+                o[k] = so[k];
+                d[k] = nd[k];
+            }
+        }
+        for (int c = 0; c < 3; ++c) sum[c] = sum[c] + L[c];
+    }
+    const float n = (float)P->spp;
+    for (int c = 0; c < 3; ++c) out[c] = sum[c] / n;
+}
+
 /* ------------------------------------------------------------------ threading */
 
 int vto_hardware_threads(void) {
@@ -431,6 +516,9 @@ typedef struct job {
     uint32_t row_offset;
     vto_stats stats;
     int want_stats;
+    const vto_path_params* path;
+    float* path_out; /* width * height * 4 floats */
+    uint64_t path_rays;
 } job;
 
 static void* run_job(void* arg) {
@@ -452,6 +540,14 @@ static void* run_job(void* arg) {
         for (uint64_t i = j->begin; i < j->end; ++i) {
             const float* r = j->rays + 6 * i;
             vto_trace_ray_f64(j->g, r, r + 3, &j->hits64[i]);
+        }
+    } else if (j->kind == 4) { /* path tracing, begin/end: pixel indices */
+        const uint32_t w = j->cam->width;
+        for (uint64_t p = j->begin; p < j->end; ++p) {
+            const uint32_t y = (uint32_t)(p / w), x = (uint32_t)(p % w);
+            float* o = j->path_out + 4 * p;
+            vto_path_pixel(j->g, j->cam, j->path, x, y, o, &j->path_rays);
+            o[3] = 1.0f;
         }
     } else { /* begin/end: pixel indices */
         const uint32_t w = j->cam->width;
@@ -525,6 +621,8 @@ static void run_parallel(job* proto, uint64_t begin, uint64_t end, int threads, 
     }
     free(lanes);
     free(tids);
+    proto->path_rays = 0;
+    for (uint64_t c = 0; c < nchunks; ++c) proto->path_rays += jobs[c].path_rays;
     free(jobs);
 }
 
@@ -792,4 +890,17 @@ int vto_compat_render(const vto_grid* grids, uint32_t ngrids, const float* insta
     free(jobs);
     free(inst);
     return 0;
+}
+
+void vto_path_trace(const vto_grid* g, const vto_camera* cam, const vto_path_params* params,
+                    uint32_t row0, uint32_t row1, float* out, int threads, uint64_t* rays) {
+    job p;
+    memset(&p, 0, sizeof(p));
+    p.kind = 4;
+    p.g = g;
+    p.cam = cam;
+    p.path = params;
+    p.path_out = out - 4 * (uint64_t)row0 * cam->width; /* out holds rows row0..row1-1 */
+    run_parallel(&p, (uint64_t)row0 * cam->width, (uint64_t)row1 * cam->width, threads, NULL);
+    if (rays) *rays = p.path_rays;
 }

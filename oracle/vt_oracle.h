@@ -160,6 +160,18 @@ int vto_compat_render(const vto_grid* grids, uint32_t ngrids, const float* insta
 
 int vto_hardware_threads(void);
 
+/* Path tracing: the library's estimator (vt_path.cu), restated. */
+typedef struct vto_path_params { /* layout identical to vt_path_params */
+    uint32_t spp, max_bounces, seed, out_format;
+    float sky[3], sun_dir[3], sun[3];
+} vto_path_params;
+void vto_path_pixel(const vto_grid* g, const vto_camera* cam, const vto_path_params* p,
+                    uint32_t px, uint32_t py, float out[3], uint64_t* rays);
+/* Rows row0..row1-1 of the image into out ((row1 - row0) * width * 4 floats: r, g, b, 1); rays
+ * may be NULL. */
+void vto_path_trace(const vto_grid* g, const vto_camera* cam, const vto_path_params* params,
+                    uint32_t row0, uint32_t row1, float* out, int threads, uint64_t* rays);
+
 #ifdef __cplusplus
 }
 #endif

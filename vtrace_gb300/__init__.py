@@ -121,6 +121,28 @@ class ServeStats(ctypes.Structure):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
 
 
+class PathParams(ctypes.Structure):
+    _fields_ = [("spp", ctypes.c_uint32), ("max_bounces", ctypes.c_uint32),
+                ("seed", ctypes.c_uint32), ("out_format", ctypes.c_uint32),
+                ("sky", ctypes.c_float * 3), ("sun_dir", ctypes.c_float * 3),
+                ("sun", ctypes.c_float * 3)]
+
+
+PATH_OUT_F32X4 = 0
+PATH_OUT_RGBA8 = 1
+
+
+def make_path_params(spp=4, max_bounces=3, seed=0, out_format=PATH_OUT_F32X4,
+                     sky=(0.6, 0.75, 1.0), sun_dir=(0.3, 0.8, 0.52), sun=(2.5, 2.3, 2.0)):
+    p = PathParams()
+    p.spp, p.max_bounces, p.seed, p.out_format = spp, max_bounces, seed, out_format
+    p.sky[:] = [float(x) for x in sky]
+    n = float(np.sqrt(np.sum(np.square(np.asarray(sun_dir, np.float64)))))
+    p.sun_dir[:] = [float(np.float32(x / n)) for x in sun_dir]
+    p.sun[:] = [float(x) for x in sun]
+    return p
+
+
 class VoxInfo(ctypes.Structure):
     _fields_ = [("version", ctypes.c_uint32), ("models", ctypes.c_uint32),
                 ("has_palette", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
@@ -170,6 +192,10 @@ SIGNATURES = [
     ("vt_render_stats", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp,
                                ctypes.POINTER(TraceStats)]),
     ("vt_trace_rays_stats", _i32, [_i32, _vp, _u64, _vp, ctypes.POINTER(TraceStats)]),
+    ("vt_path_trace", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(PathParams), _vp, _vp,
+                             _vp]),
+    ("vt_path_trace_host", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(PathParams), _vp,
+                                  ctypes.POINTER(ctypes.c_uint64)]),
     ("vt_batch_create", _i32, [ctypes.POINTER(View), _u32, ctypes.POINTER(ctypes.c_int32)]),
     ("vt_batch_run", _i32, [_i32, _vp]),
     ("vt_batch_run_direct", _i32, [_i32, _vp]),
@@ -479,6 +505,25 @@ def render_host(grid, camera, light=None, out=None):
                                ctypes.byref(light) if light is not None else None,
                                _ptr(hits)))
     return hits.reshape(camera.height, camera.width) if out is None else hits
+
+
+def path_trace(grid, camera, params, d_out, d_rays=None, stream=None):
+    """Asynchronous: width*height pixels (float4 or RGBA8 per params.out_format) into d_out
+    (device); d_rays (device u64) accumulates the rays traced."""
+    check(lib().vt_path_trace(grid.id, ctypes.byref(camera), ctypes.byref(params), _ptr(d_out),
+                              _ptr(d_rays), _stream(stream)))
+
+
+def path_trace_host(grid, camera, params):
+    """-> (image [height, width, 4] float32 or uint8, rays traced)."""
+    if params.out_format == PATH_OUT_F32X4:
+        out = np.zeros((camera.height, camera.width, 4), np.float32)
+    else:
+        out = np.zeros((camera.height, camera.width, 4), np.uint8)
+    rays = ctypes.c_uint64(0)
+    check(lib().vt_path_trace_host(grid.id, ctypes.byref(camera), ctypes.byref(params),
+                                   out.ctypes.data, ctypes.byref(rays)))
+    return out, rays.value
 
 
 def render_stats(grid, camera, light, d_hits):

@@ -1,0 +1,248 @@
+// vt_path.cu — multi-bounce diffuse path tracing on the traversal kernel (vtrace's stated goal,
+// README.md:2; the reference has no path tracer, so the estimator is this library's own
+// specification, restated operation for operation by the oracle's vto_path_pixel).
+//
+// Per pixel, for each of `spp` samples: a jittered camera ray (Philox4x32-10, as the batched
+// renderer), then up to max_bounces + 1 path vertices.  At a vertex the throughput takes the
+// voxel's colour (byte / 255 per channel); with a sun, a Lambert next-event ray from the hit point
+// (1/64 voxel off the entered face) toward the sun adds throughput x sun x n.l when it leaves the
+// grid unblocked; the path continues along n + u, u uniform on the unit sphere (rejection
+// sampling in the cube, 16 tries, Philox counters (px, py, sample, bounce << 8 | try)), which is
+// cosine-weighted about n, so that the Lambert BRDF and the sampling density cancel.  A ray that
+// leaves the grid adds throughput x sky.  A hit without a face (origin inside an occupied voxel)
+// ends the path.  The samples' radiances are summed in order and divided by spp; the output is
+// float RGBA (alpha 1) or RGBA8 (clamped to [0, 1], x 255, rounded half up, alpha 255).
+//
+// All arithmetic is IEEE binary32 round-to-nearest without contraction (explicit intrinsics), so
+// the result is bit-identical to the oracle.  One thread traces one pixel's samples in 8 x 4
+// pixel tiles.
+#include <cuda_runtime.h>
+
+#include "vt_api_internal.h"
+#include "vt_device.cuh"
+#include "vt_internal.h"
+
+namespace vt {
+
+struct PathParams {
+    uint32_t spp, max_bounces, seed, out_format;
+    float sky[3], sun_dir[3], sun[3];
+    bool sun_on;
+};
+
+constexpr uint32_t kPathKey = 0x50415448u;  // "PATH"
+constexpr int kSphereTries = 16;
+
+// A unit vector uniform on the sphere, or false after kSphereTries rejected cube samples.
+__device__ __forceinline__ bool sphere_sample(uint32_t seed, uint32_t px, uint32_t py, uint32_t s,
+                                              uint32_t bounce, float u[3]) {
+    for (int t = 0; t < kSphereTries; ++t) {
+        uint32_t r[4];
+        philox4x32_10(px, py, s, (bounce << 8) | (uint32_t)t, seed, kPathKey, r);
+        float p[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)  // (r >> 8) 2^-23 - 1: exact, in [-1, 1)
+            p[k] = __fsub_rn(__fmul_rn(__uint2float_rn(r[k] >> 8), 0x1p-23f), 1.0f);
+        const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(p[0], p[0]), __fmul_rn(p[1], p[1])),
+                                   __fmul_rn(p[2], p[2]));
+        if (r2 <= 1.0f && r2 > 0x1p-20f) {
+            const float l = __fsqrt_rn(r2);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) u[k] = __fdiv_rn(p[k], l);
+            return true;
+        }
+    }
+    return false;
+}
+
+__device__ __forceinline__ void path_pixel(const GridView& g, const vt_camera& cam,
+                                           const PathParams& P, uint32_t px, uint32_t py,
+                                           float sum[3], uint32_t& rays) {
+    Tally<false> tl;
+    sum[0] = sum[1] = sum[2] = 0.0f;
+    for (uint32_t s = 0; s < P.spp; ++s) {
+        float jx, jy, o[3], d[3];
+        jitter(P.seed, 0u, px, py, s, jx, jy);
+        raygen(cam, px, py, jx, jy, o, d);
+        float T[3] = {1.0f, 1.0f, 1.0f}, L[3] = {0.0f, 0.0f, 0.0f};
+        for (uint32_t b = 0;; ++b) {
+            const HitRec h = trace_ray<false>(g, o, d, tl);
+            ++rays;
+            const uint32_t flags = h.w1 >> 24;
+            if (!(flags & VT_HIT_FLAG_HIT)) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) L[c] = __fadd_rn(L[c], __fmul_rn(T[c], P.sky[c]));
+                break;
+            }
+            const uint32_t face = flags & VT_FACE_MASK;
+            if (face == 0) break;
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                T[c] = __fmul_rn(T[c], __fdiv_rn(__uint2float_rn((h.w3 >> (8 * c)) & 0xFFu), 255.0f));
+            const int a = (int)(face - 1) / 2;
+            const bool npos = (face & 1u) != 0u;
+            float so[3];
+            shadow_origin(h, o, d, so);
+            if (P.sun_on) {
+                const float la = a == 0 ? P.sun_dir[0] : (a == 1 ? P.sun_dir[1] : P.sun_dir[2]);
+                const float ndl = npos ? la : -la;
+                if (ndl > 0.0f) {
+                    const HitRec sh = trace_ray<false>(g, so, P.sun_dir, tl);
+                    ++rays;
+                    if (!((sh.w1 >> 24) & VT_HIT_FLAG_HIT)) {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c)
+                            L[c] = __fadd_rn(L[c], __fmul_rn(__fmul_rn(T[c], P.sun[c]), ndl));
+                    }
+                }
+            }
+            if (b >= P.max_bounces) break;
+            float n[3] = {0.0f, 0.0f, 0.0f};
+            n[a] = npos ? 1.0f : -1.0f;
+            float u[3], nd[3];
+            if (sphere_sample(P.seed, px, py, s, b, u)) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) nd[k] = __fadd_rn(n[k], u[k]);
+                const float l = __fsqrt_rn(__fadd_rn(
+                    __fadd_rn(__fmul_rn(nd[0], nd[0]), __fmul_rn(nd[1], nd[1])), __fmul_rn(nd[2], nd[2])));
+                if (l > 1e-6f) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) nd[k] = __fdiv_rn(nd[k], l);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) nd[k] = n[k];
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) nd[k] = n[k];
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                o[k] = so[k];
+                d[k] = nd[k];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) sum[c] = __fadd_rn(sum[c], L[c]);
+    }
+    const float n = __uint2float_rn(P.spp);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) sum[c] = __fdiv_rn(sum[c], n);
+}
+
+__global__ void __launch_bounds__(256) path_kernel(GridView g, vt_camera cam, PathParams P,
+                                                   void* __restrict__ out,
+                                                   unsigned long long* __restrict__ rays_out) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t px = blockIdx.x * 16 + (warp & 1u) * 8u + (lane & 7u);
+    const uint32_t py = blockIdx.y * 16 + (warp >> 1) * 4u + (lane >> 3);
+    uint32_t rays = 0;
+    if (px < cam.width && py < cam.height) {
+        float v[3];
+        path_pixel(g, cam, P, px, py, v, rays);
+        const size_t i = (size_t)py * cam.width + px;
+        if (P.out_format == VT_PATH_OUT_F32X4) {
+            ((float4*)out)[i] = make_float4(v[0], v[1], v[2], 1.0f);
+        } else {
+            uint32_t q = 0xFF000000u;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float x = v[c] > 1.0f ? 1.0f : (v[c] > 0.0f ? v[c] : 0.0f);
+                q |= __float2uint_rz(__fadd_rn(__fmul_rn(x, 255.0f), 0.5f)) << (8 * c);
+            }
+            ((uint32_t*)out)[i] = q;
+        }
+    }
+    if (rays_out) {
+        // one atomic per warp
+        unsigned long long r = rays;
+#pragma unroll
+        for (int k = 16; k > 0; k >>= 1) r += __shfl_down_sync(0xFFFFFFFFu, r, k);
+        if (lane == 0 && r) atomicAdd(rays_out, r);
+    }
+}
+
+static int32_t path_params(const vt_path_params* in, PathParams& P) {
+    if (!in) return fail(VT_EINVAL, "vt_path_trace: null params");
+    if (in->spp < 1 || in->spp > 65536) return fail(VT_EINVAL, "vt_path_trace: spp must be 1..65536");
+    if (in->max_bounces > 64) return fail(VT_EINVAL, "vt_path_trace: max_bounces must be 0..64");
+    if (in->out_format != VT_PATH_OUT_F32X4 && in->out_format != VT_PATH_OUT_RGBA8)
+        return fail(VT_EINVAL, "vt_path_trace: bad out_format");
+    P.spp = in->spp;
+    P.max_bounces = in->max_bounces;
+    P.seed = in->seed;
+    P.out_format = in->out_format;
+    P.sun_on = false;
+    for (int c = 0; c < 3; ++c) {
+        if (!isfinite(in->sky[c]) || !isfinite(in->sun[c]) || !isfinite(in->sun_dir[c]))
+            return fail(VT_EINVAL, "vt_path_trace: non-finite sky, sun or sun direction");
+        P.sky[c] = in->sky[c];
+        P.sun[c] = in->sun[c];
+        P.sun_dir[c] = in->sun_dir[c];
+        if (in->sun[c] > 0.0f) P.sun_on = true;
+    }
+    return VT_OK;
+}
+
+static cudaError_t launch_path(const GridView& g, const vt_camera& cam, const PathParams& P,
+                               void* out, unsigned long long* rays, cudaStream_t st) {
+    const dim3 grid((cam.width + 15) / 16, (cam.height + 15) / 16);
+    path_kernel<<<grid, 256, 0, st>>>(g, cam, P, out, rays);
+    return cudaGetLastError();
+}
+
+static size_t out_bytes(const vt_camera& cam, uint32_t fmt) {
+    return (size_t)cam.width * cam.height * (fmt == VT_PATH_OUT_F32X4 ? 16 : 4);
+}
+
+}  // namespace vt
+
+using namespace vt;
+
+extern "C" {
+
+int32_t vt_path_trace(int32_t grid, const vt_camera* camera, const vt_path_params* params,
+                      void* d_out, uint64_t* d_rays_traced, void* stream) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_path_trace: unknown grid");
+    int32_t rc = check_camera(camera);
+    if (rc) return rc;
+    PathParams P;
+    if ((rc = path_params(params, P))) return rc;
+    if (!d_out || ((uintptr_t)d_out & 15u)) return fail(VT_EINVAL, "vt_path_trace: output must be 16-byte aligned");
+    if ((uintptr_t)d_rays_traced & 7u) return fail(VT_EINVAL, "vt_path_trace: misaligned ray counter");
+    cudaError_t e = launch_path(g->view(), *camera, P, d_out, (unsigned long long*)d_rays_traced,
+                                pick_stream(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "vt_path_trace launch");
+    return VT_OK;
+}
+
+int32_t vt_path_trace_host(int32_t grid, const vt_camera* camera, const vt_path_params* params,
+                           void* out, uint64_t* rays_traced) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_path_trace_host: unknown grid");
+    int32_t rc = check_camera(camera);
+    if (rc) return rc;
+    PathParams P;
+    if ((rc = path_params(params, P))) return rc;
+    if (!out) return fail(VT_EINVAL, "vt_path_trace_host: null output");
+    const size_t bytes = out_bytes(*camera, P.out_format);
+    State& s = state();
+    cudaStream_t st = s.stream;
+    void* d = nullptr;
+    cudaError_t e = cudaMallocAsync(&d, bytes + 256, st);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_path_trace_host: cudaMallocAsync");
+    unsigned long long* dr = (unsigned long long*)((char*)d + ((bytes + 15) / 16) * 16);
+    unsigned long long hr = 0;
+    e = cudaMemsetAsync(dr, 0, 8, st);
+    if (e == cudaSuccess) e = launch_path(g->view(), *camera, P, d, dr, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hr, dr, 8, cudaMemcpyDeviceToHost, st);
+    cudaFreeAsync(d, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_path_trace_host");
+    if (rays_traced) *rays_traced = hr;
+    return VT_OK;
+}
+
+}  // extern "C"
