@@ -117,7 +117,8 @@ typedef struct vt_grid_info {
     uint64_t voxels_occupied;
     uint64_t device_bytes; /* directory + masks + payloads + palette */
     uint32_t payload_format; /* VT_PAYLOAD_* */
-    uint32_t reserved;
+    uint32_t slots;          /* brick slots in use (the masks vt_grid_download_bricks copies):
+                                bricks_nonempty, plus slots vt_grid_update freed and not reused */
 } vt_grid_info;
 
 #define VT_PAYLOAD_U8 1    /* palette index per voxel + 256-entry RGBA8 palette */
@@ -205,6 +206,16 @@ int32_t vt_grid_create_rgba8(const uint8_t* rgba, uint32_t nx, uint32_t ny, uint
 int32_t vt_grid_create(const void* voxels, uint32_t format, uint32_t order,
                        const uint32_t* palette, uint32_t nx, uint32_t ny, uint32_t nz);
 int32_t vt_grid_destroy(int32_t grid);
+/* Chunk paging (src/gen/pager.rs:52-78, one chunk per frame at src/render.rs:246-261): write a
+ * w x h x d box of voxels (host memory, `order`; u8 palette indices for VT_PAYLOAD_U8 grids,
+ * RGBA8 texels for VT_PAYLOAD_RGBA8 grids) into the grid at (x0, y0, z0), in place.  Bricks
+ * that become occupied take freed or new slots (the slot arrays grow by doubling), bricks that
+ * become empty give theirs back, and the empty-space distances are recomputed, so that the grid
+ * traverses exactly as one built from the updated array.  Synchronous on the library stream; not
+ * concurrent with launches that read the grid, nor with other calls on the same grid.
+ * VT_EBUSY while a batch or a service references the grid. */
+int32_t vt_grid_update(int32_t grid, const void* voxels, uint32_t order, uint32_t x0, uint32_t y0,
+                       uint32_t z0, uint32_t w, uint32_t h, uint32_t d);
 /* No counterpart in the reference.  Builds the brick layout of an x-fastest u8 grid into buffers
  * the caller owns, allocating nothing, for callers that cannot allocate device memory while they
  * run (a pager rebuilding chunks inside a real-time frame loop, where cudaMalloc/cudaFree would
@@ -228,8 +239,8 @@ int32_t vt_grid_get_info(int32_t grid, vt_grid_info* info);
 /* Copy the grid's brick directory and occupancy masks to host memory; either may be NULL.
  * directory: bricks_total u32, x-fastest over bricks; an occupied brick's entry is its slot
  * (bit 31 clear); an empty brick's entry is 0x80000000 | d, d = Chebyshev distance in bricks to
- * the nearest occupied brick (1..31, saturating).  masks: bricks_nonempty * 8 u64 by slot, word
- * lz holding bit (ly * 8 + lx) of z-slice lz. */
+ * the nearest occupied brick (1..31, saturating).  masks: vt_grid_info.slots * 8 u64 by slot,
+ * word lz holding bit (ly * 8 + lx) of z-slice lz. */
 int32_t vt_grid_download_bricks(int32_t grid, uint32_t* directory, uint64_t* masks);
 /* Copy the grid's forward-distance words (bricks_total u32): for a ray octant
  * o = (dx<0) | (dy<0)<<1 | (dz<0)<<2, nibble o holds the largest K <= 15 such that the K x K x K

@@ -62,7 +62,7 @@ class GridInfo(ctypes.Structure):
                 ("bricks_z", ctypes.c_uint32), ("bricks_total", ctypes.c_uint64),
                 ("bricks_nonempty", ctypes.c_uint64), ("voxels_occupied", ctypes.c_uint64),
                 ("device_bytes", ctypes.c_uint64), ("payload_format", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("slots", ctypes.c_uint32)]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -181,6 +181,7 @@ SIGNATURES = [
     ("vt_grid_create_rgba8", _i32, [_vp, _u32, _u32, _u32]),
     ("vt_grid_create", _i32, [_vp, _u32, _u32, _vp, _u32, _u32, _u32]),
     ("vt_grid_destroy", _i32, [_i32]),
+    ("vt_grid_update", _i32, [_i32, _vp, _u32, _u32, _u32, _u32, _u32, _u32, _u32]),
     ("vt_grid_build_u8_noalloc", _i32, [_vp, _vp, _u32, _u32, _u32, _vp, _vp, _vp, _vp, _vp]),
     ("vt_grid_get_info", _i32, [_i32, ctypes.POINTER(GridInfo)]),
     ("vt_grid_download_bricks", _i32, [_i32, _vp, _vp]),
@@ -449,6 +450,18 @@ class Grid:
         return cls(check(lib().vt_grid_create(a.ctypes.data, PAYLOAD_RGBA8, ORDER_Z_FASTEST, None,
                                               nx, ny, nz)))
 
+    def update(self, origin, voxels, order=ORDER_X_FASTEST):
+        """Write a box of voxels at origin (x0, y0, z0): x-fastest arrays are indexed [z, y, x]
+        (u8 indices, or [z, y, x, 4] u8 / [z, y, x] u32 texels for RGBA8 grids), z-fastest
+        arrays [x, y, z]."""
+        a = np.ascontiguousarray(voxels)
+        if a.dtype != np.uint32 and a.ndim == 4:
+            a = a.astype(np.uint8, copy=False).view(np.uint32)[..., 0]
+        shape = a.shape if order == ORDER_Z_FASTEST else a.shape[::-1]
+        w, h, d = shape
+        x0, y0, z0 = origin
+        check(lib().vt_grid_update(self.id, a.ctypes.data, order, x0, y0, z0, w, h, d))
+
     def info(self):
         gi = GridInfo()
         check(lib().vt_grid_get_info(self.id, ctypes.byref(gi)))
@@ -457,9 +470,9 @@ class Grid:
     def bricks(self):
         inf = self.info()
         d = np.zeros(inf["bricks_total"], np.uint32)
-        m = np.zeros(max(1, inf["bricks_nonempty"]) * 8, np.uint64)
+        m = np.zeros(max(1, inf["slots"]) * 8, np.uint64)
         check(lib().vt_grid_download_bricks(self.id, d.ctypes.data, m.ctypes.data))
-        return d, m[: inf["bricks_nonempty"] * 8].reshape(-1, 8)
+        return d, m[: inf["slots"] * 8].reshape(-1, 8)
 
     def octants(self):
         out = np.zeros(self.info()["bricks_total"], np.uint32)

@@ -198,6 +198,8 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
         e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick build"); break; }
         g->bytes = g->bricks * 8 + slots * 64 + slots * psize + (g->palette ? 1024 : 0);
+        g->slot_capacity = slots;
+        g->slots_used = g->nonempty;
     } while (0);
     cudaFree(scratch);
     if (rc != VT_OK) {
@@ -464,7 +466,7 @@ int32_t vt_grid_get_info(int32_t grid, vt_grid_info* info) {
     info->voxels_occupied = g->occupied;
     info->device_bytes = g->bytes;
     info->payload_format = g->format;
-    info->reserved = 0;
+    info->slots = (uint32_t)g->slots_used;
     return VT_OK;
 }
 
@@ -474,8 +476,8 @@ int32_t vt_grid_download_bricks(int32_t grid, uint32_t* directory, uint64_t* mas
     cudaStream_t st = state().stream;
     cudaError_t e = cudaSuccess;
     if (directory) e = cudaMemcpyAsync(directory, g->dir, g->bricks * 4, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess && masks && g->nonempty)
-        e = cudaMemcpyAsync(masks, g->masks, g->nonempty * 64, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && masks && g->slots_used)
+        e = cudaMemcpyAsync(masks, g->masks, g->slots_used * 64, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_grid_download_bricks");
     return VT_OK;

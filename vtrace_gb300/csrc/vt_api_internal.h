@@ -32,6 +32,9 @@ struct Grid {
     void* payload = nullptr;
     uint32_t* palette = nullptr;
     size_t bytes = 0;
+    // slots of masks/payload: allocated, handed out (high-water mark), and freed by updates
+    uint64_t slot_capacity = 0, slots_used = 0;
+    std::vector<uint32_t> free_slots;
     std::atomic<int32_t> refs{0};  // in-flight batches / serving requests using the grid
     GridView view() const;
     void release();
