@@ -46,7 +46,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--config", choices=["shapes1024", "terrain256", "cave512", "multiview", "serve",
-                                        "pager_world", "pathtrace"],
+                                        "pager_world", "pathtrace", "paging"],
                    default="shapes1024")
     p.add_argument("--serve-requests", type=int, default=1000,
                    help="requests of the serving comparison added to the headline run (0: skip)")
@@ -495,6 +495,37 @@ def run_config(args):
             line["parity"] = {"band_pixels_differing_from_oracle":
                               int((got[rows[0]:rows[1]] != band).any(-1).sum())}
         g.destroy()
+    elif args.config == "paging":
+        # chunk streaming into the resident 1024^3 grid: 16^3 chunks written in place
+        w = workloads.shapes1024()
+        g = vt.Grid.from_u8(w["voxels"], w["palette"])
+        rng = np.random.default_rng(9)
+        n = w["voxels"].shape[0]
+        chunks = []
+        for k in range(args.steps + args.warmup):
+            org = tuple(int(rng.integers(0, n // 16)) * 16 for _ in range(3))
+            fill = k % 2 == 0
+            c = np.where(rng.random((16, 16, 16)) < 0.3, rng.integers(1, 256, (16, 16, 16)), 0) if fill else np.zeros((16, 16, 16))
+            chunks.append((org, np.ascontiguousarray(c.astype(np.uint8))))
+        for org, c in chunks[:args.warmup]:
+            g.update(org, c)
+        t0 = time.perf_counter()
+        for org, c in chunks[args.warmup:]:
+            g.update(org, c)
+        ms = (time.perf_counter() - t0) / args.steps * 1e3
+        cam, light = w["camera"], w["light"]
+        d_hits = torch.empty(cam.width * cam.height * 16, dtype=torch.uint8, device="cuda")
+        frame_ms = autotune.time_ms(lambda: vt.render(g, cam, light, d_hits, stream), stream,
+                                    repeats=10, warmup=2, flush=flush)
+        line.update(metric="chunk updates/s (16^3 chunks written into a resident 1024^3 grid)",
+                    value=1e3 / ms, unit="chunks/s", ms_per_step=ms,
+                    config={"workload": "shapes1024_paging_16cube", "chunk_bytes": 4096,
+                            "bricks_total": g.info()["bricks_total"]},
+                    e2e={"value": 1e3 / ms, "unit": "chunks/s", "h2d_bytes_per_step": 4096,
+                         "d2h_bytes_per_step": 8 * 2 * 8 + 8,
+                         "path": "vt_grid_update (C ABI), synchronous, host wall clock"},
+                    frame_after_updates_ms=frame_ms, gpu_launches=9 * args.steps)
+        g.destroy()
     elif args.config == "pager_world":
         # the reference-compatible frame (render_tick) over vtrace's own world shape
         import ctypes
@@ -560,7 +591,7 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.config in ("cave512", "multiview", "serve", "pager_world", "pathtrace"):
+    if args.config in ("cave512", "multiview", "serve", "pager_world", "pathtrace", "paging"):
         return run_config(args)
     return run_ours(args)
 

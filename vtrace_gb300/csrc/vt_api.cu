@@ -162,8 +162,11 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
     uint32_t last_off = 0, last_flag = 0;
     unsigned long long occ = 0;
     do {
+        // u8 palettes whose only transparent entry is index 0: occupancy is "index != 0"
+        bool nonzero = format == VT_PAYLOAD_U8 && (palette_host[0] >> 24) == 0u;
+        for (int i = 1; nonzero && i < 256; ++i) nonzero = (palette_host[i] >> 24) != 0u;
         e = launch_brick_words(d_src, format, g->palette, (int32_t)nx, (int32_t)ny, (int32_t)nz, s,
-                               stream);
+                               stream, nonzero);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick words kernel"); break; }
         e = launch_brick_scan(s, g->bricks, stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick scan kernel"); break; }

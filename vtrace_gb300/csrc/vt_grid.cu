@@ -69,21 +69,33 @@ __device__ __forceinline__ BrickCoord brick_coord(uint64_t brick, int32_t bx, in
     return c;
 }
 
+// Occupancy bits of 8 u8 voxels packed in a u64 when "occupied" means "nonzero index": the high
+// bit of each byte of ((v & 0x7F..) + 0x7F..) | v is set iff the byte is nonzero; the multiply
+// gathers the eight high bits into the top byte (bit k from byte k).
+__device__ __forceinline__ uint32_t nonzero_bytes(uint64_t v) {
+    const uint64_t hi = (((v & 0x7F7F7F7F7F7F7F7Full) + 0x7F7F7F7F7F7F7F7Full) | v) & 0x8080808080808080ull;
+    return (uint32_t)(((hi >> 7) * 0x0102040810204080ull) >> 56);
+}
+
 // Occupancy bits of one 8-voxel row: bit lx set iff voxel x0+lx is inside the grid and occupied.
 template <uint32_t FMT>
 __device__ __forceinline__ uint32_t row_bits(const void* src, const uint8_t* lut, size_t row_base,
-                                             int32_t x0, int32_t nx) {
+                                             int32_t x0, int32_t nx, bool nz = false) {
     uint32_t bits = 0;
     if (FMT == VT_PAYLOAD_U8) {
         const uint8_t* row = (const uint8_t*)src + row_base + x0;
         if (x0 + 8 <= nx && (((uintptr_t)row) & 7u) == 0) {
             const uint2 v = __ldg((const uint2*)row);
+            if (nz) return nonzero_bytes(((uint64_t)v.y << 32) | v.x);
 #pragma unroll
             for (int k = 0; k < 4; ++k) bits |= (uint32_t)lut[(v.x >> (8 * k)) & 0xFFu] << k;
 #pragma unroll
             for (int k = 0; k < 4; ++k) bits |= (uint32_t)lut[(v.y >> (8 * k)) & 0xFFu] << (k + 4);
         } else {
-            for (int k = 0; k < 8 && x0 + k < nx; ++k) bits |= (uint32_t)lut[__ldg(row + k)] << k;
+            for (int k = 0; k < 8 && x0 + k < nx; ++k) {
+                const uint8_t b = __ldg(row + k);
+                bits |= (uint32_t)(nz ? b != 0 : lut[b]) << k;
+            }
         }
     } else {
         const uint32_t* row = (const uint32_t*)src + row_base + x0;
@@ -100,7 +112,9 @@ __device__ __forceinline__ uint32_t row_bits(const void* src, const uint8_t* lut
     return bits;
 }
 
-template <uint32_t FMT>
+// NZ: u8 grid whose palette has alpha 0 at index 0 only, so that occupancy is "index != 0" and the
+// row bits come from byte arithmetic instead of palette lookups.
+template <uint32_t FMT, bool NZ>
 __global__ void __launch_bounds__(256) brick_words_kernel(const void* __restrict__ src,
                                                           const uint32_t* __restrict__ palette,
                                                           int32_t nx, int32_t ny, int32_t nz,
@@ -109,7 +123,7 @@ __global__ void __launch_bounds__(256) brick_words_kernel(const void* __restrict
                                                           uint32_t* __restrict__ flags,
                                                           unsigned long long* occupied) {
     __shared__ uint8_t lut[256];
-    if (FMT == VT_PAYLOAD_U8) {
+    if (FMT == VT_PAYLOAD_U8 && !NZ) {
         for (int i = threadIdx.x; i < 256; i += blockDim.x)
             lut[i] = (uint8_t)((__ldg(palette + i) >> 24) != 0u);
         __syncthreads();
@@ -123,11 +137,22 @@ __global__ void __launch_bounds__(256) brick_words_kernel(const void* __restrict
         const BrickCoord c = brick_coord(brick, bx, by);
         const int32_t z = c.bzi * 8 + (int32_t)lz, x0 = c.bxi * 8;
         if (z < nz) {
-            for (int ly = 0; ly < 8; ++ly) {
-                const int32_t y = c.byi * 8 + ly;
-                if (y >= ny) break;
-                const size_t row_base = (size_t)nx * ((size_t)y + (size_t)ny * (size_t)z);
-                w |= (uint64_t)row_bits<FMT>(src, lut, row_base, x0, nx) << (8 * ly);
+            const size_t plane = (size_t)nx * (size_t)ny * (size_t)z;
+            if (NZ && x0 + 8 <= nx && (nx & 7) == 0 && c.byi * 8 + 8 <= ny) {
+                // whole rows, 8-byte aligned: issue the eight loads before using any
+                const uint8_t* base = (const uint8_t*)src + plane + (size_t)nx * (size_t)(c.byi * 8) + x0;
+                uint64_t r[8];
+#pragma unroll
+                for (int ly = 0; ly < 8; ++ly) r[ly] = __ldg((const unsigned long long*)(base + (size_t)nx * ly));
+#pragma unroll
+                for (int ly = 0; ly < 8; ++ly) w |= (uint64_t)nonzero_bytes(r[ly]) << (8 * ly);
+            } else {
+                for (int ly = 0; ly < 8; ++ly) {
+                    const int32_t y = c.byi * 8 + ly;
+                    if (y >= ny) break;
+                    const size_t row_base = plane + (size_t)nx * (size_t)y;
+                    w |= (uint64_t)row_bits<FMT>(src, NZ ? nullptr : lut, row_base, x0, nx, NZ) << (8 * ly);
+                }
             }
         }
     }
@@ -212,18 +237,21 @@ cudaError_t launch_brick_scan(const BuildScratch& s, uint64_t bricks, cudaStream
 
 cudaError_t launch_brick_words(const void* src, uint32_t format, const uint32_t* d_palette,
                                int32_t nx, int32_t ny, int32_t nz, const BuildScratch& s,
-                               cudaStream_t stream) {
+                               cudaStream_t stream, bool nonzero_occupancy) {
     const int32_t bx = (nx + 7) / 8, by = (ny + 7) / 8, bz = (nz + 7) / 8;
     const uint64_t bricks = (uint64_t)bx * by * bz;
     const uint64_t threads = bricks * 8;
     const unsigned blocks = (unsigned)((threads + 255) / 256);
     cudaError_t e = cudaMemsetAsync(s.occupied, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
-    if (format == VT_PAYLOAD_U8)
-        brick_words_kernel<VT_PAYLOAD_U8><<<blocks, 256, 0, stream>>>(
+    if (format == VT_PAYLOAD_U8 && nonzero_occupancy)
+        brick_words_kernel<VT_PAYLOAD_U8, true><<<blocks, 256, 0, stream>>>(
+            src, d_palette, nx, ny, nz, bx, by, bricks, s.words, s.flags, s.occupied);
+    else if (format == VT_PAYLOAD_U8)
+        brick_words_kernel<VT_PAYLOAD_U8, false><<<blocks, 256, 0, stream>>>(
             src, d_palette, nx, ny, nz, bx, by, bricks, s.words, s.flags, s.occupied);
     else
-        brick_words_kernel<VT_PAYLOAD_RGBA8><<<blocks, 256, 0, stream>>>(
+        brick_words_kernel<VT_PAYLOAD_RGBA8, false><<<blocks, 256, 0, stream>>>(
             src, nullptr, nx, ny, nz, bx, by, bricks, s.words, s.flags, s.occupied);
     return cudaGetLastError();
 }
@@ -317,12 +345,19 @@ __global__ void __launch_bounds__(256) brick_distance_kernel(uint32_t* __restric
     const int32_t n = AXIS == 0 ? bx : (AXIS == 1 ? by : bz);
     const int64_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? (int64_t)bx : (int64_t)bx * by);
     const int32_t cap = (int32_t)kMaxBrickDistance;
-    const int32_t lo = max(pos - cap, 0), hi = min(pos + cap, n - 1);
+    // min over offsets j of max(|j|, val(pos + j)), visiting |j| = 0, 1, 2, ... and stopping once
+    // |j| reaches the best value found (no farther offset can improve it)
     int32_t best = cap;
-    for (int32_t p = lo; p <= hi; ++p) {
-        const int64_t idx = (int64_t)b + (int64_t)(p - pos) * stride;
-        const int32_t val = AXIS == 0 ? (brick_empty(__ldg(dir + idx)) ? cap : 0) : (int32_t)__ldg(in + idx);
-        best = min(best, max(abs(p - pos), val));
+    for (int32_t r = 0; r < best; ++r) {
+#pragma unroll
+        for (int sgn = 0; sgn < 2; ++sgn) {
+            if (r == 0 && sgn) continue;
+            const int32_t p = sgn ? pos - r : pos + r;
+            if (p < 0 || p >= n) continue;
+            const int64_t idx = (int64_t)b + (int64_t)(p - pos) * stride;
+            const int32_t val = AXIS == 0 ? (brick_empty(__ldg(dir + idx)) ? cap : 0) : (int32_t)__ldg(in + idx);
+            best = min(best, max(r, val));
+        }
     }
     if (AXIS < 2) {
         out[b] = (uint8_t)best;
@@ -373,16 +408,18 @@ __global__ void __launch_bounds__(256) brick_octant_y_kernel(const uint8_t* __re
     const BrickCoord c = brick_coord(b, bx, by);
     uint32_t packed = 0;
 #pragma unroll
-    for (int o = 0; o < 4; ++o) {  // o = (sx<0) | (sy<0)<<1
-        const int32_t sy = (o & 2) ? -1 : 1;
-        int32_t best = kMaxOctantDistance;
-        for (int32_t j = 0; j < best; ++j) {
+    for (int ny = 0; ny < 2; ++ny) {  // one walk per sy serves both sx
+        const int32_t sy = ny ? -1 : 1;
+        int32_t best[2] = {(int32_t)kMaxOctantDistance, (int32_t)kMaxOctantDistance};
+        for (int32_t j = 0; j < max(best[0], best[1]); ++j) {
             const int32_t y = c.byi + j * sy;
             if (y < 0 || y >= by) break;
-            const int32_t f = (int32_t)((__ldg(in + (int64_t)b + (int64_t)j * sy * bx) >> (4 * (o & 1))) & 15u);
-            best = min(best, max(j, f));
+            const uint32_t f = __ldg(in + (int64_t)b + (int64_t)j * sy * bx);
+#pragma unroll
+            for (int nx = 0; nx < 2; ++nx) best[nx] = min(best[nx], max(j, (int32_t)((f >> (4 * nx)) & 15u)));
         }
-        packed |= (uint32_t)best << (4 * o);
+#pragma unroll
+        for (int nx = 0; nx < 2; ++nx) packed |= (uint32_t)best[nx] << (4 * (nx | (ny << 1)));
     }
     out[b] = (uint16_t)packed;
 }
@@ -397,16 +434,25 @@ __global__ void __launch_bounds__(256) brick_octant_z_kernel(const uint16_t* __r
     const int64_t plane = (int64_t)bx * by;
     uint32_t packed = 0;
 #pragma unroll
-    for (int o = 0; o < 8; ++o) {  // o = (sx<0) | (sy<0)<<1 | (sz<0)<<2
-        const int32_t sz = (o & 4) ? -1 : 1;
-        int32_t best = kMaxOctantDistance;
-        for (int32_t l = 0; l < best; ++l) {
+    for (int nz = 0; nz < 2; ++nz) {  // one walk per sz serves the four (sx, sy)
+        const int32_t sz = nz ? -1 : 1;
+        int32_t best[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) best[q] = (int32_t)kMaxOctantDistance;
+        int32_t lim = (int32_t)kMaxOctantDistance;
+        for (int32_t l = 0; l < lim; ++l) {
             const int32_t z = c.bzi + l * sz;
             if (z < 0 || z >= bz) break;
-            const int32_t f = (int32_t)((__ldg(in + (int64_t)b + (int64_t)l * sz * plane) >> (4 * (o & 3))) & 15u);
-            best = min(best, max(l, f));
+            const uint32_t f = __ldg(in + (int64_t)b + (int64_t)l * sz * plane);
+            lim = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                best[q] = min(best[q], max(l, (int32_t)((f >> (4 * q)) & 15u)));
+                lim = max(lim, best[q]);
+            }
         }
-        packed |= (uint32_t)best << (4 * o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) packed |= (uint32_t)best[q] << (4 * (q | (nz << 2)));
     }
     out[b] = packed;
 }

@@ -55,7 +55,7 @@ BuildScratch carve_build_scratch(void* base, uint64_t bricks);
 // Phase 1: occupancy words, brick flags and the occupied-voxel count; phase 2: slots.
 cudaError_t launch_brick_words(const void* src, uint32_t format, const uint32_t* d_palette,
                                int32_t nx, int32_t ny, int32_t nz, const BuildScratch& s,
-                               cudaStream_t stream);
+                               cudaStream_t stream, bool nonzero_occupancy = false);
 cudaError_t launch_brick_scan(const BuildScratch& s, uint64_t bricks, cudaStream_t stream);
 // Dense z-fastest input (element size 1 or 4) to x-fastest; y-planes are transposed in place of
 // the x and z axes.  grid.y = ceil(nx / 32) and grid.z = ny must stay within 65535.
