@@ -135,8 +135,10 @@ class ClockSampler:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_sample(w, seconds, threads=0):
-    """The CPU oracle on bands of 8 rows spread over the frame until `seconds` of wall time."""
+def cpu_sample(w, seconds, threads=0, frame=None):
+    """The CPU oracle on bands of 8 rows spread over the frame until `seconds` of wall time; with
+    the GPU's `frame` (hit records [H, W]) also the number of records of those bands that differ
+    from the oracle's."""
     from oracle import pyoracle as po
     og = po.Grid(w["voxels"], w["palette"])
     cam = po.make_camera(w["camera"].as_dict())
@@ -148,18 +150,55 @@ def cpu_sample(w, seconds, threads=0):
     order = np.random.default_rng(0).permutation(H // band)
     rays = 0
     rows = 0
+    differ = 0
     t0 = time.perf_counter()
     for b in order:
         r0 = int(b) * band
-        _, st = po.render(og, cam, light, threads=threads, stats=True, rows=(r0, r0 + band))
+        hits, st = po.render(og, cam, light, threads=threads, stats=True, rows=(r0, r0 + band))
         rays += st["rays"]
         rows += band
+        if frame is not None:
+            got = frame[r0:r0 + band].view(np.uint8).reshape(-1, 16)
+            differ += int((got != hits.view(np.uint8).reshape(-1, 16)).any(1).sum())
         if time.perf_counter() - t0 >= seconds:
             break
     dt = time.perf_counter() - t0
-    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": "%d of %d rows of the %dx%d frame in 8-row bands (%d rays incl. shadow "
-                      "rays), %.1f s wall" % (rows, H, cam.width, H, rays, dt)}
+    out = {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+           "sample": "%d of %d rows of the %dx%d frame in 8-row bands (%d rays incl. shadow "
+                     "rays), %.1f s wall" % (rows, H, cam.width, H, rays, dt)}
+    if frame is not None:
+        out["records_differing_from_gpu"] = differ
+    return out
+
+
+def tie_divergence(w, grid, n=1 << 18):
+    """Seeded uniform rays in the grid, traced on the GPU and by the oracle in binary32 and
+    binary64: binary32 records that differ (must be 0), rays whose binary32 and binary64 hits
+    differ, and those of them that pass an exact binary32 tie (an iteration stepping two or three
+    axes at once)."""
+    import torch
+    import vtrace_gb300 as vt
+    from oracle import pyoracle as po
+    nx = w["voxels"].shape[::-1]
+    rays = vt.gen_rays_uniform(nx, 77, n)
+    d_rays = torch.from_numpy(rays.view(np.uint8).reshape(-1)).cuda()
+    d_hits = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    vt.trace_rays(grid, d_rays, n, d_hits)
+    torch.cuda.synchronize()
+    got = d_hits.cpu().numpy().view(vt.HIT_DTYPE)
+    og = po.Grid(w["voxels"], w["palette"])
+    h32 = po.trace_rays(og, rays)
+    h64 = po.trace_rays_f64(og, rays)
+    hit = (h32["face"] & po.FLAG_HIT) != 0
+    same = hit & (h64["hit"] == 1) & (h32["x"] == h64["v"][:, 0]) & (h32["y"] == h64["v"][:, 1]) & \
+        (h32["z"] == h64["v"][:, 2]) & ((h32["face"] & 7) == h64["face"])
+    div = np.nonzero((hit != (h64["hit"] == 1)) | (hit & ~same))[0]
+    tie_div = sum(1 for i in div if po.trace_rays(og, rays[i:i + 1], stats=True)[1]["ties"] > 0)
+    return {"rays": n, "gpu_records_differing_from_oracle":
+            int((got.view(np.uint8).reshape(-1, 16) != h32.view(np.uint8).reshape(-1, 16)).any(1).sum()),
+            "fp64_divergent_rate": len(div) / n, "tie_divergent_rate": tie_div / n,
+            "note": "uniform rays in the benchmark grid; divergence from binary64 is the binary32 "
+                    "recurrence resolving near-ties (within rounding of an edge) differently"}
 
 
 def run_reference(args):
@@ -316,7 +355,9 @@ def run_ours(args):
         "grid_info": grid.info(),
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_sample(w, args.cpu_seconds)
+        frame = d_hits.cpu().numpy().view(vt.HIT_DTYPE).reshape(cam.height, cam.width)
+        line["cpu_baseline"] = cpu_sample(w, args.cpu_seconds, frame=frame)
+        line["parity"] = tie_divergence(w, grid)
     grid.destroy()
     del d_hits
     if rank == 0 and args.serve_requests > 0 and world == 1:
