@@ -171,6 +171,7 @@ typedef struct vt_tuning {
 #define VT_KERNEL_RENDER 1
 #define VT_KERNEL_TRACE_RAYS 2
 #define VT_KERNEL_BATCH 3
+#define VT_KERNEL_PATH 4 /* vt_path_trace: persistent = paths refilled per lane, else a thread per pixel */
 
 int32_t vt_get_tuning(int32_t kernel, vt_tuning* out);
 int32_t vt_set_tuning(int32_t kernel, const vt_tuning* in);

@@ -23,8 +23,16 @@ def oracle_params(p):
                                list(p.sun))
 
 
+@pytest.fixture(params=[(1, 32), (1, 4), (0, 32)], ids=["persistent", "refill4", "per_pixel"])
+def form(request, torch):
+    saved = vt.get_tuning(vt.KERNEL_PATH)
+    vt.set_tuning(vt.KERNEL_PATH, request.param[1], 0, bool(request.param[0]))
+    yield request.param
+    vt.set_tuning(vt.KERNEL_PATH, saved["refill_min"], saved["blocks_per_sm"], saved["persistent"])
+
+
 @pytest.mark.parametrize("case", ["terrain", "shapes", "nosun", "deep"])
-def test_path_trace_matches_oracle(torch, case):
+def test_path_trace_matches_oracle(torch, form, case):
     if case == "shapes":
         w = workloads.shapes1024(n=128, width=80, height=60, count=60)
         p = vt.make_path_params(spp=3, max_bounces=3, seed=5)
@@ -61,7 +69,7 @@ def test_path_trace_matches_oracle(torch, case):
         g.destroy()
 
 
-def test_path_trace_rgba8_grid_and_determinism(torch):
+def test_path_trace_rgba8_grid_and_determinism(torch, form):
     rng = np.random.default_rng(8)
     n = 40
     tex = np.zeros((n, n, n), np.uint32)
@@ -82,6 +90,12 @@ def test_path_trace_rgba8_grid_and_determinism(torch):
         p.seed = 2
         c, _ = vt.path_trace_host(g, cam, p)
         assert (c != a).any()
+        # more samples than one chunk of the persistent form's sample buffer holds per pixel
+        p.seed, p.spp, p.max_bounces = 3, 37, 1
+        big, rb = vt.path_trace_host(g, cam, p)
+        want, rays = po.path_trace(po.Grid(texels=tex), po.make_camera(cam.as_dict()), oracle_params(p))
+        np.testing.assert_array_equal(big, want)
+        assert rb == rays
         with pytest.raises(vt.VtError):
             p.spp = 0
             vt.path_trace_host(g, cam, p)

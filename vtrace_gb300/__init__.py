@@ -82,7 +82,7 @@ class Tuning(ctypes.Structure):
                 ("persistent", ctypes.c_uint32), ("wavefront", ctypes.c_uint32)]
 
 
-KERNEL_RENDER, KERNEL_TRACE_RAYS, KERNEL_BATCH = 1, 2, 3
+KERNEL_RENDER, KERNEL_TRACE_RAYS, KERNEL_BATCH, KERNEL_PATH = 1, 2, 3, 4
 
 
 class View(ctypes.Structure):

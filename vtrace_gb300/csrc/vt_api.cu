@@ -351,6 +351,7 @@ static TraceTuning* tuning_of(int32_t kernel) {
         case VT_KERNEL_RENDER: return &s.tune_render;
         case VT_KERNEL_TRACE_RAYS: return &s.tune_rays;
         case VT_KERNEL_BATCH: return &s.tune_batch;
+        case VT_KERNEL_PATH: return &s.tune_path;
         default: return nullptr;
     }
 }

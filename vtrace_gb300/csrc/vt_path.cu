@@ -18,9 +18,12 @@
 // pixel tiles.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "vt_api_internal.h"
 #include "vt_device.cuh"
 #include "vt_internal.h"
+#include "vt_lane.cuh"
 
 namespace vt {
 
@@ -162,6 +165,273 @@ __global__ void __launch_bounds__(256) path_kernel(GridView g, vt_camera cam, Pa
     }
 }
 
+
+// ---------------------------------------------------------------------------------------------
+// Persistent form: paths end after very different numbers of rays (escape at the first hit, or
+// bounces plus sun rays), so one thread per pixel leaves most lanes idle.  Here resident warps
+// hold one path per lane and advance every live lane by one traversal unit (vt_lane.cuh); a lane
+// whose path ended takes the next path from a work counter (warp-aggregated).  Paths are numbered
+// tile by tile (8 x 4 pixels), sample-major inside a tile, so a refill hands a warp one tile's
+// rays for one sample.  Each path's radiance goes to a per-sample buffer; the resolve sums the
+// samples of a pixel in sample order, so the image is identical to path_kernel's.
+// ---------------------------------------------------------------------------------------------
+
+struct PathLane {
+    LaneRay R;
+    float T[3], L[3];
+    float so[3];      // origin of the pending bounce (hit point off the face)
+    uint32_t item;    // path index
+    uint32_t px, py, s;
+    uint32_t b;       // vertex index
+    uint32_t face;    // face of the current vertex (for the bounce after a sun ray)
+    int mode;         // 0 idle, 1 path ray, 2 sun ray
+};
+
+// Starts the ray after the current vertex (bounce) or ends the path; returns the new status of
+// the lane's ray (kRayRunning while a ray is under way).
+__device__ __forceinline__ int path_continue(const GridView& g, const PathParams& P, PathLane& s,
+                                             float4* __restrict__ samples, uint32_t spp) {
+    if (s.b >= P.max_bounces) {
+        samples[s.item] = make_float4(s.L[0], s.L[1], s.L[2], 0.0f);
+        s.mode = 0;
+        return kRayMiss;
+    }
+    const int a = (int)(s.face - 1) / 2;
+    const bool npos = (s.face & 1u) != 0u;
+    float n[3] = {0.0f, 0.0f, 0.0f};
+    n[a] = npos ? 1.0f : -1.0f;
+    float u[3], nd[3];
+    if (sphere_sample(P.seed, s.px, s.py, s.s, s.b, u)) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) nd[k] = __fadd_rn(n[k], u[k]);
+        const float l = __fsqrt_rn(__fadd_rn(
+            __fadd_rn(__fmul_rn(nd[0], nd[0]), __fmul_rn(nd[1], nd[1])), __fmul_rn(nd[2], nd[2])));
+        if (l > 1e-6f) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) nd[k] = __fdiv_rn(nd[k], l);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) nd[k] = n[k];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) nd[k] = n[k];
+    }
+    ++s.b;
+    s.mode = 1;
+    return ray_begin(g, s.so, nd, s.R);
+}
+
+// A ray of the lane ended with status `st`: shade the vertex and start the next ray, or end the
+// path.  Same arithmetic, in the same order, as path_pixel.
+__device__ __forceinline__ int path_finish(const GridView& g, const PathParams& P, PathLane& s,
+                                           int st, float4* __restrict__ samples, uint32_t spp) {
+    if (s.mode == 2) {  // sun ray of vertex b
+        if (st != kRayHit) {
+            const int a = (int)(s.face - 1) / 2;
+            const bool npos = (s.face & 1u) != 0u;
+            const float la = a == 0 ? P.sun_dir[0] : (a == 1 ? P.sun_dir[1] : P.sun_dir[2]);
+            const float ndl = npos ? la : -la;
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                s.L[c] = __fadd_rn(s.L[c], __fmul_rn(__fmul_rn(s.T[c], P.sun[c]), ndl));
+        }
+        return path_continue(g, P, s, samples, spp);
+    }
+    // path ray of vertex b
+    const HitRec h = ray_record(g, s.R, st, 0u);
+    const uint32_t flags = h.w1 >> 24;
+    if (!(flags & VT_HIT_FLAG_HIT)) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) s.L[c] = __fadd_rn(s.L[c], __fmul_rn(s.T[c], P.sky[c]));
+        samples[s.item] = make_float4(s.L[0], s.L[1], s.L[2], 0.0f);
+        s.mode = 0;
+        return kRayMiss;
+    }
+    const uint32_t face = flags & VT_FACE_MASK;
+    if (face == 0) {
+        samples[s.item] = make_float4(s.L[0], s.L[1], s.L[2], 0.0f);
+        s.mode = 0;
+        return kRayMiss;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        s.T[c] = __fmul_rn(s.T[c], __fdiv_rn(__uint2float_rn((h.w3 >> (8 * c)) & 0xFFu), 255.0f));
+    s.face = face;
+    shadow_origin(h, s.R.o, s.R.d, s.so);
+    if (P.sun_on) {
+        const int a = (int)(face - 1) / 2;
+        const bool npos = (face & 1u) != 0u;
+        const float la = a == 0 ? P.sun_dir[0] : (a == 1 ? P.sun_dir[1] : P.sun_dir[2]);
+        const float ndl = npos ? la : -la;
+        if (ndl > 0.0f) {
+            s.mode = 2;
+            return ray_begin(g, s.so, P.sun_dir, s.R);
+        }
+    }
+    return path_continue(g, P, s, samples, spp);
+}
+
+__global__ void __launch_bounds__(256) path_persistent_kernel(
+    GridView g, vt_camera cam, PathParams P, uint32_t s0, uint32_t sn, float4* __restrict__ samples,
+    unsigned long long* __restrict__ counter, uint32_t tiles_x, uint64_t total,
+    uint32_t refill_min, unsigned long long* __restrict__ rays_out) {
+    const uint32_t lane = threadIdx.x & 31u;
+    PathLane s;
+    s.mode = 0;
+    uint32_t rays = 0;
+    bool more = true;  // warp-uniform
+    for (;;) {
+        uint32_t idle = __ballot_sync(0xFFFFFFFFu, s.mode == 0);
+        while (more && __popc(idle) >= (int)refill_min) {
+            uint64_t item;
+            const uint64_t base = warp_fetch(counter, idle, lane, item);
+            if (base + __popc(idle) >= total) more = false;
+            if (s.mode == 0 && item < total) {
+                // item = (tile * sn + sample) * 32 + pixel of the tile
+                const uint32_t l = (uint32_t)(item & 31u);
+                const uint64_t ts = item >> 5;
+                const uint32_t smp = (uint32_t)(ts % sn);
+                const uint64_t tile = ts / sn;
+                const uint32_t px = (uint32_t)(tile % tiles_x) * 8u + (l & 7u);
+                const uint32_t py = (uint32_t)(tile / tiles_x) * 4u + (l >> 3);
+                if (px < cam.width && py < cam.height) {
+                    s.px = px;
+                    s.py = py;
+                    s.s = s0 + smp;
+                    s.item = (uint32_t)(((size_t)py * cam.width + px) * sn + smp);
+                    s.b = 0;
+                    s.T[0] = s.T[1] = s.T[2] = 1.0f;
+                    s.L[0] = s.L[1] = s.L[2] = 0.0f;
+                    float jx, jy, o[3], d[3];
+                    jitter(P.seed, 0u, px, py, s.s, jx, jy);
+                    raygen(cam, px, py, jx, jy, o, d);
+                    s.mode = 1;
+                    ++rays;
+                    int st = ray_begin(g, o, d, s.R);
+                    while (s.mode != 0 && st != kRayRunning) {
+                        st = path_finish(g, P, s, st, samples, sn);
+                        if (s.mode != 0) ++rays;
+                    }
+                }
+            }
+            idle = __ballot_sync(0xFFFFFFFFu, s.mode == 0);
+        }
+        if (!more && idle == 0xFFFFFFFFu) break;
+        if (s.mode != 0) {
+            int st = ray_unit(g, s.R);
+            while (s.mode != 0 && st != kRayRunning) {
+                st = path_finish(g, P, s, st, samples, sn);
+                if (s.mode != 0) ++rays;
+            }
+        }
+    }
+    if (rays_out) {
+        unsigned long long r = rays;
+#pragma unroll
+        for (int k = 16; k > 0; k >>= 1) r += __shfl_down_sync(0xFFFFFFFFu, r, k);
+        if (lane == 0 && r) atomicAdd(rays_out, r);
+    }
+}
+
+// Adds samples s0 .. s0 + sn - 1 of every pixel to its running sum in sample order; the last
+// chunk divides by spp and writes the pixel.
+__global__ void __launch_bounds__(256) path_resolve_kernel(const float4* __restrict__ samples,
+                                                           float4* __restrict__ sums, uint32_t npx,
+                                                           uint32_t sn, bool first, bool last,
+                                                           uint32_t spp, uint32_t out_format,
+                                                           void* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npx) return;
+    float v[3] = {0.0f, 0.0f, 0.0f};
+    if (!first) {
+        const float4 q = sums[i];
+        v[0] = q.x;
+        v[1] = q.y;
+        v[2] = q.z;
+    }
+    for (uint32_t k = 0; k < sn; ++k) {
+        const float4 q = samples[(size_t)i * sn + k];
+        v[0] = __fadd_rn(v[0], q.x);
+        v[1] = __fadd_rn(v[1], q.y);
+        v[2] = __fadd_rn(v[2], q.z);
+    }
+    if (!last) {
+        sums[i] = make_float4(v[0], v[1], v[2], 0.0f);
+        return;
+    }
+    const float n = __uint2float_rn(spp);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] = __fdiv_rn(v[c], n);
+    if (out_format == VT_PATH_OUT_F32X4) {
+        ((float4*)out)[i] = make_float4(v[0], v[1], v[2], 1.0f);
+    } else {
+        uint32_t q = 0xFF000000u;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float x = v[c] > 1.0f ? 1.0f : (v[c] > 0.0f ? v[c] : 0.0f);
+            q |= __float2uint_rz(__fadd_rn(__fmul_rn(x, 255.0f), 0.5f)) << (8 * c);
+        }
+        ((uint32_t*)out)[i] = q;
+    }
+}
+
+// Sample buffer of one chunk of samples: at most 16 samples per pixel and 64 Mi entries (1 GiB).
+constexpr uint32_t kPathChunkSamples = 64u << 20, kPathChunkSpp = 16;
+
+static int path_resident_blocks() {
+    static int n = -1;
+    if (n < 0) {
+        int k = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, (const void*)path_persistent_kernel,
+                                                          256, 0) != cudaSuccess) {
+            cudaGetLastError();
+            k = 1;
+        }
+        n = k < 1 ? 1 : k;
+    }
+    return n;
+}
+
+static cudaError_t launch_path_persistent(const GridView& g, const vt_camera& cam,
+                                          const PathParams& P, void* out,
+                                          unsigned long long* rays, const TraceTuning& tune,
+                                          int sm_count, cudaStream_t st) {
+    const uint32_t npx = cam.width * cam.height;
+    const uint32_t tiles_x = (cam.width + 7) / 8, tiles_y = (cam.height + 3) / 4;
+    // samples per chunk: as many as fit the sample buffer
+    uint32_t sn = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>(std::min(P.spp, kPathChunkSpp), kPathChunkSamples / npx));
+    const size_t sbytes = (size_t)npx * sn * sizeof(float4);
+    const size_t sums_off = (sbytes + 255) / 256 * 256;
+    const size_t total_bytes = sums_off + (size_t)npx * sizeof(float4) + 256;
+    char* buf = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&buf, total_bytes, st);
+    if (e != cudaSuccess) return e;
+    float4* samples = (float4*)buf;
+    float4* sums = (float4*)(buf + sums_off);
+    const int bps = tune.blocks_per_sm > 0 ? min(tune.blocks_per_sm, path_resident_blocks())
+                                           : path_resident_blocks();
+    for (uint32_t s0 = 0; s0 < P.spp && e == cudaSuccess; s0 += sn) {
+        const uint32_t n = std::min(sn, P.spp - s0);
+        const uint64_t total = (uint64_t)tiles_x * tiles_y * n * 32;
+        unsigned long long* counter = next_counter();
+        e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+        if (e != cudaSuccess) break;
+        const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)sm_count * bps, (total + 255) / 256);
+        path_persistent_kernel<<<blocks, 256, 0, st>>>(g, cam, P, s0, n, samples, counter, tiles_x,
+                                                       total, tune.refill_min, rays);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) break;
+        path_resolve_kernel<<<(npx + 255) / 256, 256, 0, st>>>(samples, sums, npx, n, s0 == 0,
+                                                               s0 + n >= P.spp, P.spp,
+                                                               P.out_format, out);
+        e = cudaGetLastError();
+    }
+    const cudaError_t f = cudaFreeAsync(buf, st);
+    return e != cudaSuccess ? e : f;
+}
+
 static int32_t path_params(const vt_path_params* in, PathParams& P) {
     if (!in) return fail(VT_EINVAL, "vt_path_trace: null params");
     if (in->spp < 1 || in->spp > 65536) return fail(VT_EINVAL, "vt_path_trace: spp must be 1..65536");
@@ -186,6 +456,9 @@ static int32_t path_params(const vt_path_params* in, PathParams& P) {
 
 static cudaError_t launch_path(const GridView& g, const vt_camera& cam, const PathParams& P,
                                void* out, unsigned long long* rays, cudaStream_t st) {
+    State& S = state();
+    if (S.tune_path.persistent)
+        return launch_path_persistent(g, cam, P, out, rays, S.tune_path, S.sm_count, st);
     const dim3 grid((cam.width + 15) / 16, (cam.height + 15) / 16);
     path_kernel<<<grid, 256, 0, st>>>(g, cam, P, out, rays);
     return cudaGetLastError();
