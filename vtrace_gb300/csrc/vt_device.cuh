@@ -360,45 +360,29 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
     }
 }
 
-// The empty box of voxels the ray crosses next from the empty brick (bxi, byi, bzi): the forward
-// box of the ray's octant (K bricks along each stepping direction, from the brick's octant word
-// `ow`) when it reaches further than the centred cube of bricks within Chebyshev distance D - 1
-// (from the directory entry `e`), else that cube; clipped to the grid.
-__device__ __forceinline__ void empty_box(const GridView& g, uint32_t e, uint32_t ow, int32_t bxi,
-                                          int32_t byi, int32_t bzi, int32_t stx, int32_t sty,
-                                          int32_t stz, uint32_t oct_shift, int32_t& lox,
-                                          int32_t& hix, int32_t& loy, int32_t& hiy, int32_t& loz,
-                                          int32_t& hiz) {
+// Voxel moves to the far face, along each stepping axis, of the empty box the ray crosses next
+// from the empty brick (bxi, byi, bzi).  Two boxes are known empty: the cube of bricks within
+// Chebyshev distance D - 1 (D from the directory entry `e`) and the box of K bricks from this
+// brick toward the ray's octant (K from the octant word `ow`).  Both reach R bricks forward
+// along every stepping direction (R = D for the cube, K for the forward box), and the ray only
+// moves forward, so the crossing uses R = max(D, K), clipped to the grid.  Axes with no step get
+// 1 (unused by cross_region).
+__device__ __forceinline__ void empty_moves(const GridView& g, uint32_t e, uint32_t ow,
+                                            int32_t bxi, int32_t byi, int32_t bzi, int32_t vx,
+                                            int32_t vy, int32_t vz, int32_t stx, int32_t sty,
+                                            int32_t stz, uint32_t oct_shift, int32_t& nxe,
+                                            int32_t& nye, int32_t& nze) {
     const int32_t D = max((int32_t)(e & 0xFFu), 1);
-    const int32_t K = (int32_t)((ow >> oct_shift) & 15u);
-    if (K > D) {
-        lox = stx < 0 ? (bxi - K + 1) * 8 : bxi * 8;
-        hix = stx < 0 ? (bxi + 1) * 8 : (bxi + K) * 8;
-        loy = sty < 0 ? (byi - K + 1) * 8 : byi * 8;
-        hiy = sty < 0 ? (byi + 1) * 8 : (byi + K) * 8;
-        loz = stz < 0 ? (bzi - K + 1) * 8 : bzi * 8;
-        hiz = stz < 0 ? (bzi + 1) * 8 : (bzi + K) * 8;
-    } else {
-        const int32_t D1 = D - 1;
-        lox = (bxi - D1) * 8;
-        hix = (bxi + D1 + 1) * 8;
-        loy = (byi - D1) * 8;
-        hiy = (byi + D1 + 1) * 8;
-        loz = (bzi - D1) * 8;
-        hiz = (bzi + D1 + 1) * 8;
-    }
-    lox = max(lox, 0);
-    loy = max(loy, 0);
-    loz = max(loz, 0);
-    hix = min(hix, g.nx);
-    hiy = min(hiy, g.ny);
-    hiz = min(hiz, g.nz);
+    const int32_t R = max(D, (int32_t)((ow >> oct_shift) & 15u));
+    nxe = stx > 0 ? min((bxi + R) << 3, g.nx) - vx : (stx < 0 ? vx - max((bxi - R + 1) << 3, 0) + 1 : 1);
+    nye = sty > 0 ? min((byi + R) << 3, g.ny) - vy : (sty < 0 ? vy - max((byi - R + 1) << 3, 0) + 1 : 1);
+    nze = stz > 0 ? min((bzi + R) << 3, g.nz) - vz : (stz < 0 ? vz - max((bzi - R + 1) << 3, 0) + 1 : 1);
 }
 
 // The octant word of brick `bidx`; 0 (no forward boxes) for a grid built without octant words.
 // Loaded together with the directory entry, before the entry is tested, so that both loads are in
 // flight at once.
-__device__ __forceinline__ uint32_t octant_word(const GridView& g, size_t bidx) {
+__device__ __forceinline__ uint32_t octant_word(const GridView& g, uint32_t bidx) {
     return g.oct ? __ldg(g.oct + bidx) : 0u;
 }
 
@@ -407,10 +391,9 @@ __device__ __forceinline__ uint32_t octant_shift(int32_t stx, int32_t sty, int32
 }
 
 // Same result as dda() (hit, voxel, slot, final mask), organised for speed: occupied bricks are
-// walked voxel by voxel against their occupancy bits; an empty brick at Chebyshev distance D from
-// the nearest occupied brick is part of an empty cube of (2D-1)^3 bricks, and of the forward box
-// of the ray's octant (empty_box); the ray crosses the larger in one cross_region().  The step count and tie flag of the literal loop are not
-// tracked here (the counting kernels use dda()).
+// walked voxel by voxel against their occupancy bits; from an empty brick the ray crosses the
+// empty box of empty_moves() in one cross_region().  The step count and tie flag of the literal
+// loop are not tracked here (the counting kernels use dda()).
 __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, float pz,
                                          float dx, float dy, float dz, DDAResult& r) {
     const float len = __fsqrt_rn(
@@ -433,7 +416,8 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
     int32_t guard = g.nx + g.ny + g.nz + 2;
     while (grid_inside(g, vx, vy, vz) && --guard > 0) {
         const int32_t bxi = vx >> 3, byi = vy >> 3, bzi = vz >> 3;
-        const size_t bidx = (size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi);
+        // fewer than 2^31 bricks (vt_grid_create checks): the index fits 32 bits
+        const uint32_t bidx = (uint32_t)bxi + (uint32_t)g.bx * ((uint32_t)byi + (uint32_t)g.by * (uint32_t)bzi);
         const uint32_t e = __ldg(g.dir + bidx);
         const uint32_t ow = octant_word(g, bidx);
         if (!brick_empty(e)) {
@@ -454,12 +438,8 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
             }
             if (hit) break;
         } else {
-            int32_t lox, hix, loy, hiy, loz, hiz;
-            empty_box(g, e, ow, bxi, byi, bzi, stx, sty, stz, oshift, lox, hix, loy, hiy, loz,
-                      hiz);
-            const int32_t nxe = stx > 0 ? hix - vx : vx - lox + 1;
-            const int32_t nye = sty > 0 ? hiy - vy : vy - loy + 1;
-            const int32_t nze = stz > 0 ? hiz - vz : vz - loz + 1;
+            int32_t nxe, nye, nze;
+            empty_moves(g, e, ow, bxi, byi, bzi, vx, vy, vz, stx, sty, stz, oshift, nxe, nye, nze);
             cross_region(sx, sy, sz, vx, vy, vz, dlx, dly, dlz, stx, sty, stz, nxe, nye, nze, mx,
                          my, mz);
         }

@@ -82,7 +82,7 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
     bool mx = R.mx, my = R.my, mz = R.mz;
     int status = kRayRunning;
     const int32_t bxi = vx >> 3, byi = vy >> 3, bzi = vz >> 3;
-    const size_t bidx = (size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi);
+    const uint32_t bidx = (uint32_t)bxi + (uint32_t)g.bx * ((uint32_t)byi + (uint32_t)g.by * (uint32_t)bzi);
     const uint32_t e = __ldg(g.dir + bidx);
     const uint32_t ow = octant_word(g, bidx);
     if (!brick_empty(e)) {
@@ -102,11 +102,8 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
             if (vx == ex || vy == ey || vz == ez || steps >= 24u) break;
         }
     } else {
-        int32_t lox, hix, loy, hiy, loz, hiz;
-        empty_box(g, e, ow, bxi, byi, bzi, stx, sty, stz, R.oshift, lox, hix, loy, hiy, loz, hiz);
-        const int32_t nxe = stx > 0 ? hix - vx : vx - lox + 1;
-        const int32_t nye = sty > 0 ? hiy - vy : vy - loy + 1;
-        const int32_t nze = stz > 0 ? hiz - vz : vz - loz + 1;
+        int32_t nxe, nye, nze;
+        empty_moves(g, e, ow, bxi, byi, bzi, vx, vy, vz, stx, sty, stz, R.oshift, nxe, nye, nze);
         cross_region(sx, sy, sz, vx, vy, vz, dlx, dly, dlz, stx, sty, stz, nxe, nye, nze, mx, my,
                      mz);
     }
