@@ -408,3 +408,20 @@ def test_batched_multiview_matches_oracle(torch):
         for g in grids:
             if g.id is not None:
                 g.destroy()
+
+
+def test_host_forms_split_into_pieces_agree(torch):
+    """vt_render_host renders in row bands and vt_trace_rays_host in chunks of 4 Mi rays on
+    helper streams; both equal the device forms."""
+    w = workloads.terrain256(n=128, width=640, height=477)
+    g = vt.Grid.from_u8(w["voxels"], w["palette"])
+    try:
+        light = workloads.seeded_light(1, shadows=True)
+        img, _ = device_render(torch, g, w["camera"], light)
+        assert_hits_equal(vt.render_host(g, w["camera"], light), img, "render_host bands")
+        n = (1 << 22) + 12345
+        rays = vt.gen_rays_uniform(128, 4, n)
+        hits, _, _ = device_trace(torch, g, rays)
+        assert_hits_equal(vt.trace_rays_host(g, rays), hits, "trace_rays_host chunks")
+    finally:
+        g.destroy()

@@ -1,5 +1,7 @@
 // vt_api.cu — C ABI of libvtrace: library state, grid table, tracing and rendering calls.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <stdio.h>
 #include <string.h>
 
@@ -40,6 +42,12 @@ int32_t ensure_init_locked(int32_t device) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+    for (int k = 0; k < State::kAux; ++k) {
+        e = cudaStreamCreateWithFlags(&s.aux[k], cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate(aux)");
+    }
+    e = cudaEventCreateWithFlags(&s.aux_start, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     e = cudaDeviceGetAttribute(&s.sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
     e = cudaMalloc(&s.counters, kCounterRing * sizeof(unsigned long long));
@@ -316,6 +324,13 @@ void vt_shutdown(void) {
     s.staging_bytes = 0;
     cudaFree(s.counters);
     s.counters = nullptr;
+    for (int k = 0; k < State::kAux; ++k) {
+        cudaStreamSynchronize(s.aux[k]);
+        cudaStreamDestroy(s.aux[k]);
+        s.aux[k] = nullptr;
+    }
+    cudaEventDestroy(s.aux_start);
+    s.aux_start = nullptr;
     cudaStreamDestroy(s.stream);
     s.stream = nullptr;
     s.inited = false;
@@ -534,6 +549,27 @@ int32_t vt_trace_rays_stats(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_h
     return VT_OK;
 }
 
+// Host-buffer forms: the work is split into pieces (ray chunks, row bands) issued round-robin on
+// the helper streams, each piece's upload, traversal and download in order on its stream, so that
+// the copies of one piece overlap the traversal of the next.  Both helper streams first wait for
+// the library stream's earlier work.
+static cudaError_t aux_begin(State& s) {
+    cudaError_t e = cudaEventRecord(s.aux_start, s.stream);
+    for (int k = 0; e == cudaSuccess && k < State::kAux; ++k)
+        e = cudaStreamWaitEvent(s.aux[k], s.aux_start, 0);
+    return e;
+}
+
+static cudaError_t aux_end(State& s, cudaError_t e) {
+    for (int k = 0; k < State::kAux; ++k) {
+        const cudaError_t f = cudaStreamSynchronize(s.aux[k]);
+        if (e == cudaSuccess) e = f;
+    }
+    return e;
+}
+
+constexpr uint64_t kHostRayChunk = 1u << 22;  // rays per piece of vt_trace_rays_host
+
 int32_t vt_trace_rays_host(int32_t grid, const vt_ray* rays, uint64_t n, vt_hit* hits) {
     Grid* g = lookup_grid(grid);
     if (!g) return fail(VT_ENOTFOUND, "vt_trace_rays_host: unknown grid");
@@ -548,11 +584,17 @@ int32_t vt_trace_rays_host(int32_t grid, const vt_ray* rays, uint64_t n, vt_hit*
     if (rc) return rc;
     vt_hit* dh = (vt_hit*)buf;
     vt_ray* dr = (vt_ray*)((char*)buf + roff);
-    cudaStream_t st = s.stream;
-    cudaError_t e = cudaMemcpyAsync(dr, rays, rb, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = launch_rays(g->view(), dr, n, (uint4*)dh, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(hits, dh, hb, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    const GridView v = g->view();
+    cudaError_t e = aux_begin(s);
+    for (uint64_t i = 0, k = 0; e == cudaSuccess && i < n; i += kHostRayChunk, ++k) {
+        const uint64_t m = std::min<uint64_t>(kHostRayChunk, n - i);
+        cudaStream_t st = s.aux[k % State::kAux];
+        e = cudaMemcpyAsync(dr + i, rays + i, m * sizeof(vt_ray), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = launch_rays(v, dr + i, m, (uint4*)(dh + i), st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(hits + i, dh + i, m * sizeof(vt_hit), cudaMemcpyDeviceToHost, st);
+    }
+    e = aux_end(s, e);
     if (e != cudaSuccess) return cuda_fail(e, "vt_trace_rays_host");
     return VT_OK;
 }
@@ -603,13 +645,32 @@ int32_t vt_render_host(int32_t grid, const vt_camera* camera, const vt_light* li
     if (!hits) return fail(VT_EINVAL, "vt_render_host: null output");
     State& s = state();
     std::lock_guard<std::mutex> lk(s.host_mu);
-    const size_t hb = (size_t)camera->width * camera->height * sizeof(vt_hit);
+    const uint32_t W = camera->width, H = camera->height;
+    const size_t hb = (size_t)W * H * sizeof(vt_hit);
     void* buf;
     if ((rc = staging(hb, &buf))) return rc;
-    cudaStream_t st = s.stream;
-    cudaError_t e = launch_frame(g->view(), *camera, light_view(light), (uint4*)buf, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(hits, buf, hb, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    const GridView v = g->view();
+    const LightView L = light_view(light);
+    cudaError_t e;
+    if (s.tune_render.persistent || s.tune_render.wavefront || H < 64) {
+        cudaStream_t st = s.stream;
+        e = launch_frame(v, *camera, L, (uint4*)buf, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hits, buf, hb, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    } else {
+        // four row bands of whole 16-row tiles
+        const uint32_t band = (H / 4 + 15) / 16 * 16;
+        e = aux_begin(s);
+        for (uint32_t r0 = 0, k = 0; e == cudaSuccess && r0 < H; r0 += band, ++k) {
+            const uint32_t r1 = std::min(H, r0 + band);
+            cudaStream_t st = s.aux[k % State::kAux];
+            e = launch_render(v, *camera, L, (uint4*)buf, nullptr, st, r0, r1);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(hits + (size_t)r0 * W, (vt_hit*)buf + (size_t)r0 * W,
+                                    (size_t)(r1 - r0) * W * sizeof(vt_hit), cudaMemcpyDeviceToHost, st);
+        }
+        e = aux_end(s, e);
+    }
     if (e != cudaSuccess) return cuda_fail(e, "vt_render_host");
     return VT_OK;
 }

@@ -47,6 +47,10 @@ struct State {
     int32_t device = 0;
     int32_t sm_count = 0;
     cudaStream_t stream = nullptr;
+    // helper streams of the host-buffer calls: copies of one band overlap the next band's work
+    static constexpr int kAux = 2;
+    cudaStream_t aux[kAux] = {nullptr, nullptr};
+    cudaEvent_t aux_start = nullptr;
     std::vector<std::unique_ptr<Grid>> grids;
     void* staging = nullptr;
     size_t staging_bytes = 0;

@@ -34,7 +34,8 @@ cudaError_t launch_trace_rays_persistent(const GridView& g, const vt_ray* rays, 
                                          cudaStream_t stream);
 
 cudaError_t launch_render(const GridView& g, const vt_camera& cam, const LightView& light,
-                          uint4* out, Counters* counters, cudaStream_t stream);
+                          uint4* out, Counters* counters, cudaStream_t stream, uint32_t row0 = 0,
+                          uint32_t row1 = 0);
 cudaError_t launch_trace_rays(const GridView& g, const vt_ray* rays, uint64_t n, uint4* out,
                               Counters* counters, cudaStream_t stream);
 

@@ -12,14 +12,16 @@ namespace vt {
 // A 256-thread block covers 16 x 16 pixels (2 x 4 warps).
 constexpr int kTileW = 16, kTileH = 16;
 
+// Rows row0 .. row1 - 1 of the image (a band; the whole image when 0 .. height).
 template <bool STATS>
 __global__ void __launch_bounds__(256) render_kernel(GridView g, vt_camera cam, LightView light,
                                                      uint4* __restrict__ out,
-                                                     Counters* __restrict__ counters) {
+                                                     Counters* __restrict__ counters,
+                                                     uint32_t row0, uint32_t row1) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t px = blockIdx.x * kTileW + (warp & 1u) * 8u + (lane & 7u);
-    const uint32_t py = blockIdx.y * kTileH + (warp >> 1) * 4u + (lane >> 3);
-    if (px >= cam.width || py >= cam.height) return;
+    const uint32_t py = row0 + blockIdx.y * kTileH + (warp >> 1) * 4u + (lane >> 3);
+    if (px >= cam.width || py >= row1) return;
     Tally<STATS> tl;
     float o[3], d[3];
     raygen(cam, px, py, 0.5f, 0.5f, o, d);
@@ -45,12 +47,15 @@ __global__ void __launch_bounds__(256) trace_rays_kernel(GridView g,
 }
 
 cudaError_t launch_render(const GridView& g, const vt_camera& cam, const LightView& light,
-                          uint4* out, Counters* counters, cudaStream_t stream) {
-    dim3 grid((cam.width + kTileW - 1) / kTileW, (cam.height + kTileH - 1) / kTileH);
+                          uint4* out, Counters* counters, cudaStream_t stream, uint32_t row0,
+                          uint32_t row1) {
+    if (row1 == 0 || row1 > cam.height) row1 = cam.height;
+    if (row0 >= row1) return cudaSuccess;
+    dim3 grid((cam.width + kTileW - 1) / kTileW, (row1 - row0 + kTileH - 1) / kTileH);
     if (counters)
-        render_kernel<true><<<grid, 256, 0, stream>>>(g, cam, light, out, counters);
+        render_kernel<true><<<grid, 256, 0, stream>>>(g, cam, light, out, counters, row0, row1);
     else
-        render_kernel<false><<<grid, 256, 0, stream>>>(g, cam, light, out, nullptr);
+        render_kernel<false><<<grid, 256, 0, stream>>>(g, cam, light, out, nullptr, row0, row1);
     return cudaGetLastError();
 }
 
