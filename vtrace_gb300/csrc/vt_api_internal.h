@@ -58,10 +58,9 @@ struct State {
     unsigned long long* counters = nullptr;
     std::atomic<uint32_t> counter_next{0};
     // defaults from sweeps on GB300: coherent camera rays keep their 8 x 4 tiles (refills would
-    // mix tiles), incoherent ray buffers refill a warp once 8 lanes are idle, path tracing takes a
-    // new tile-sample of paths when the whole warp is idle (per-lane refills mixed tiles)
+    // mix tiles), incoherent ray buffers and path tracing refill a warp once 8 lanes are idle
     TraceTuning tune_render{16, 0, 0, 0}, tune_rays{8, 0, 1, 0}, tune_batch{16, 0, 0, 0},
-        tune_path{32, 0, 1, 0};
+        tune_path{8, 0, 1, 0};
 };
 
 constexpr uint32_t kCounterRing = 4096;

@@ -179,53 +179,55 @@ __global__ void __launch_bounds__(256) path_kernel(GridView g, vt_camera cam, Pa
 struct PathLane {
     LaneRay R;
     float T[3], L[3];
-    float so[3];      // origin of the pending bounce (hit point off the face)
+    float so[3];      // origin of the next ray (hit point off the face)
+    float nd[3];      // direction of a pending bounce ray
     uint32_t item;    // path index
     uint32_t px, py, s;
     uint32_t b;       // vertex index
     uint32_t face;    // face of the current vertex (for the bounce after a sun ray)
     int mode;         // 0 idle, 1 path ray, 2 sun ray
+    int pend;         // ray to start: 0 none, 1 camera, 2 sun, 3 bounce
 };
 
-// Starts the ray after the current vertex (bounce) or ends the path; returns the new status of
-// the lane's ray (kRayRunning while a ray is under way).
-__device__ __forceinline__ int path_continue(const GridView& g, const PathParams& P, PathLane& s,
-                                             float4* __restrict__ samples, uint32_t spp) {
+// A path vertex after the sun ray (or with none): queue the bounce ray, or end the path.
+__device__ __forceinline__ void path_continue(const PathParams& P, PathLane& s,
+                                              float4* __restrict__ samples) {
     if (s.b >= P.max_bounces) {
         samples[s.item] = make_float4(s.L[0], s.L[1], s.L[2], 0.0f);
         s.mode = 0;
-        return kRayMiss;
+        return;
     }
     const int a = (int)(s.face - 1) / 2;
     const bool npos = (s.face & 1u) != 0u;
     float n[3] = {0.0f, 0.0f, 0.0f};
     n[a] = npos ? 1.0f : -1.0f;
-    float u[3], nd[3];
+    float u[3];
     if (sphere_sample(P.seed, s.px, s.py, s.s, s.b, u)) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) nd[k] = __fadd_rn(n[k], u[k]);
-        const float l = __fsqrt_rn(__fadd_rn(
-            __fadd_rn(__fmul_rn(nd[0], nd[0]), __fmul_rn(nd[1], nd[1])), __fmul_rn(nd[2], nd[2])));
+        for (int k = 0; k < 3; ++k) s.nd[k] = __fadd_rn(n[k], u[k]);
+        const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(s.nd[0], s.nd[0]),
+                                                       __fmul_rn(s.nd[1], s.nd[1])),
+                                             __fmul_rn(s.nd[2], s.nd[2])));
         if (l > 1e-6f) {
 #pragma unroll
-            for (int k = 0; k < 3; ++k) nd[k] = __fdiv_rn(nd[k], l);
+            for (int k = 0; k < 3; ++k) s.nd[k] = __fdiv_rn(s.nd[k], l);
         } else {
 #pragma unroll
-            for (int k = 0; k < 3; ++k) nd[k] = n[k];
+            for (int k = 0; k < 3; ++k) s.nd[k] = n[k];
         }
     } else {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) nd[k] = n[k];
+        for (int k = 0; k < 3; ++k) s.nd[k] = n[k];
     }
     ++s.b;
     s.mode = 1;
-    return ray_begin(g, s.so, nd, s.R);
+    s.pend = 3;
 }
 
-// A ray of the lane ended with status `st`: shade the vertex and start the next ray, or end the
+// The lane's ray ended with status `st`: shade the vertex and queue the next ray, or end the
 // path.  Same arithmetic, in the same order, as path_pixel.
-__device__ __forceinline__ int path_finish(const GridView& g, const PathParams& P, PathLane& s,
-                                           int st, float4* __restrict__ samples, uint32_t spp) {
+__device__ __forceinline__ void path_finish(const GridView& g, const PathParams& P, PathLane& s,
+                                            int st, float4* __restrict__ samples) {
     if (s.mode == 2) {  // sun ray of vertex b
         if (st != kRayHit) {
             const int a = (int)(s.face - 1) / 2;
@@ -236,23 +238,21 @@ __device__ __forceinline__ int path_finish(const GridView& g, const PathParams& 
             for (int c = 0; c < 3; ++c)
                 s.L[c] = __fadd_rn(s.L[c], __fmul_rn(__fmul_rn(s.T[c], P.sun[c]), ndl));
         }
-        return path_continue(g, P, s, samples, spp);
+        path_continue(P, s, samples);
+        return;
     }
     // path ray of vertex b
     const HitRec h = ray_record(g, s.R, st, 0u);
     const uint32_t flags = h.w1 >> 24;
-    if (!(flags & VT_HIT_FLAG_HIT)) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) s.L[c] = __fadd_rn(s.L[c], __fmul_rn(s.T[c], P.sky[c]));
-        samples[s.item] = make_float4(s.L[0], s.L[1], s.L[2], 0.0f);
-        s.mode = 0;
-        return kRayMiss;
-    }
     const uint32_t face = flags & VT_FACE_MASK;
-    if (face == 0) {
+    if (!(flags & VT_HIT_FLAG_HIT) || face == 0) {
+        if (!(flags & VT_HIT_FLAG_HIT)) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) s.L[c] = __fadd_rn(s.L[c], __fmul_rn(s.T[c], P.sky[c]));
+        }
         samples[s.item] = make_float4(s.L[0], s.L[1], s.L[2], 0.0f);
         s.mode = 0;
-        return kRayMiss;
+        return;
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -263,22 +263,30 @@ __device__ __forceinline__ int path_finish(const GridView& g, const PathParams& 
         const int a = (int)(face - 1) / 2;
         const bool npos = (face & 1u) != 0u;
         const float la = a == 0 ? P.sun_dir[0] : (a == 1 ? P.sun_dir[1] : P.sun_dir[2]);
-        const float ndl = npos ? la : -la;
-        if (ndl > 0.0f) {
+        if ((npos ? la : -la) > 0.0f) {
             s.mode = 2;
-            return ray_begin(g, s.so, P.sun_dir, s.R);
+            s.pend = 2;
+            return;
         }
     }
-    return path_continue(g, P, s, samples, spp);
+    path_continue(P, s, samples);
 }
 
-__global__ void __launch_bounds__(256) path_persistent_kernel(
+constexpr int kRayPending = 3;  // the lane has a ray queued in PathLane::pend
+
+// ray_begin, the vertex shading and ray_unit each have one call site: lanes that start rays do so
+// together, and the kernel stays small.  Four blocks of 256 per SM (64 registers; a few bytes of
+// spill) measured faster than three without spill.
+
+__global__ void __launch_bounds__(256, 4) path_persistent_kernel(
     GridView g, vt_camera cam, PathParams P, uint32_t s0, uint32_t sn, float4* __restrict__ samples,
     unsigned long long* __restrict__ counter, uint32_t tiles_x, uint64_t total,
     uint32_t refill_min, unsigned long long* __restrict__ rays_out) {
     const uint32_t lane = threadIdx.x & 31u;
     PathLane s;
     s.mode = 0;
+    s.pend = 0;
+    int st = kRayMiss;
     uint32_t rays = 0;
     bool more = true;  // warp-uniform
     for (;;) {
@@ -303,28 +311,38 @@ __global__ void __launch_bounds__(256) path_persistent_kernel(
                     s.b = 0;
                     s.T[0] = s.T[1] = s.T[2] = 1.0f;
                     s.L[0] = s.L[1] = s.L[2] = 0.0f;
-                    float jx, jy, o[3], d[3];
-                    jitter(P.seed, 0u, px, py, s.s, jx, jy);
-                    raygen(cam, px, py, jx, jy, o, d);
                     s.mode = 1;
-                    ++rays;
-                    int st = ray_begin(g, o, d, s.R);
-                    while (s.mode != 0 && st != kRayRunning) {
-                        st = path_finish(g, P, s, st, samples, sn);
-                        if (s.mode != 0) ++rays;
-                    }
+                    s.pend = 1;
+                    st = kRayPending;
                 }
             }
             idle = __ballot_sync(0xFFFFFFFFu, s.mode == 0);
         }
         if (!more && idle == 0xFFFFFFFFu) break;
-        if (s.mode != 0) {
-            int st = ray_unit(g, s.R);
-            while (s.mode != 0 && st != kRayRunning) {
-                st = path_finish(g, P, s, st, samples, sn);
-                if (s.mode != 0) ++rays;
+        // start queued rays and shade ended ones until every live lane has a running ray
+        while (s.mode != 0 && st != kRayRunning) {
+            if (s.pend != 0) {
+                float o[3], d[3];
+                if (s.pend == 1) {
+                    float jx, jy;
+                    jitter(P.seed, 0u, s.px, s.py, s.s, jx, jy);
+                    raygen(cam, s.px, s.py, jx, jy, o, d);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        o[k] = s.so[k];
+                        d[k] = s.pend == 2 ? P.sun_dir[k] : s.nd[k];
+                    }
+                }
+                s.pend = 0;
+                ++rays;
+                st = ray_begin(g, o, d, s.R);
+            } else {
+                path_finish(g, P, s, st, samples);
+                st = kRayPending;
             }
         }
+        if (s.mode != 0) st = ray_unit(g, s.R);
     }
     if (rays_out) {
         unsigned long long r = rays;
