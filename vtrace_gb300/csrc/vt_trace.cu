@@ -96,40 +96,42 @@ __device__ __forceinline__ bool item_pixel(uint64_t item, uint32_t tiles_x, cons
     return px < cam.width && py < cam.height;
 }
 
-// Render state of one lane: 0 idle, 1 primary ray, 2 shadow ray of `prim`.
+// Render state of one lane: kind 0 idle, 1 primary ray, 2 shadow ray of `prim`; pend 1 or 2
+// when that ray is queued but not started.
 struct RenderLane {
     LaneRay R;
-    int kind;
+    int kind, pend;
     uint32_t pix;
     HitRec prim;
     float ndl;
+    float so[3];  // origin of the queued shadow ray
 };
 
-// A ray of the lane ended with `st`; writes the pixel or starts the shadow ray.  Returns the
-// status of the lane's ray afterwards (kRayRunning while a shadow ray is under way).
-__device__ __forceinline__ int render_finish(const GridView& g, const LightView& L, RenderLane& s,
-                                             int st, uint4* out) {
+constexpr int kRayQueued = 3;  // the lane's next ray is queued in RenderLane::pend
+
+// A ray of the lane ended with `st`: write the pixel, or queue the shadow ray.
+__device__ __forceinline__ void render_finish(const GridView& g, const LightView& L, RenderLane& s,
+                                              int st, uint4* out) {
     if (s.kind == 1) {
         HitRec h = ray_record(g, s.R, st, VT_SKY_RGBA);
         float nd;
         if (st != kRayHit || !L.enabled || !face_lit(h, L, nd)) {
             out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
             s.kind = 0;
-            return kRayMiss;
+            return;
         }
         if (nd > 0.0f && L.shadows) {
-            float so[3];
-            shadow_origin(h, s.R.o, s.R.d, so);
+            shadow_origin(h, s.R.o, s.R.d, s.so);
             s.prim = h;
             s.ndl = nd;
             s.kind = 2;
-            const float ld[3] = {L.dx, L.dy, L.dz};
-            return ray_begin(g, so, ld, s.R);
+            s.pend = 2;
+            return;
         }
         h.w3 = shade_rgba(h.w3, nd, 1.0f, L.ambient);
         out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
         s.kind = 0;
-        return kRayMiss;
+        return;
     }
     // shadow ray
     const bool shadowed = st == kRayHit;
@@ -138,9 +140,10 @@ __device__ __forceinline__ int render_finish(const GridView& g, const LightView&
     h.w1 |= (VT_HIT_FLAG_SHADOW_RAY | (shadowed ? VT_HIT_FLAG_SHADOWED : 0u)) << 24;
     out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
     s.kind = 0;
-    return kRayMiss;
 }
 
+// ray_begin, render_finish and ray_unit each have one call site (lanes starting rays do so
+// together; small code).
 __global__ void __launch_bounds__(256) render_persistent_kernel(
     GridView g, vt_camera cam, LightView L, uint4* __restrict__ out,
     unsigned long long* __restrict__ counter, uint32_t tiles_x, uint64_t total,
@@ -148,8 +151,10 @@ __global__ void __launch_bounds__(256) render_persistent_kernel(
     const uint32_t lane = threadIdx.x & 31u;
     RenderLane s;
     s.kind = 0;
+    s.pend = 0;
     s.pix = 0;
     s.ndl = 0.0f;
+    int st = kRayMiss;
     bool more = true;  // warp-uniform
     for (;;) {
         uint32_t idle = __ballot_sync(0xFFFFFFFFu, s.kind == 0);
@@ -161,20 +166,34 @@ __global__ void __launch_bounds__(256) render_persistent_kernel(
                 uint32_t px, py;
                 if (item_pixel(item, tiles_x, cam, px, py)) {
                     s.pix = py * cam.width + px;
-                    float o[3], d[3];
-                    raygen(cam, px, py, 0.5f, 0.5f, o, d);
                     s.kind = 1;
-                    int st = ray_begin(g, o, d, s.R);
-                    while (s.kind != 0 && st != kRayRunning) st = render_finish(g, L, s, st, out);
+                    s.pend = 1;
+                    st = kRayQueued;
                 }
             }
             idle = __ballot_sync(0xFFFFFFFFu, s.kind == 0);
         }
         if (!more && idle == 0xFFFFFFFFu) break;
-        if (s.kind != 0) {
-            int st = ray_unit(g, s.R);
-            while (s.kind != 0 && st != kRayRunning) st = render_finish(g, L, s, st, out);
+        while (s.kind != 0 && st != kRayRunning) {
+            if (s.pend != 0) {
+                float o[3], d[3];
+                if (s.pend == 1) {
+                    raygen(cam, s.pix % cam.width, s.pix / cam.width, 0.5f, 0.5f, o, d);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) o[k] = s.so[k];
+                    d[0] = L.dx;
+                    d[1] = L.dy;
+                    d[2] = L.dz;
+                }
+                s.pend = 0;
+                st = ray_begin(g, o, d, s.R);
+            } else {
+                render_finish(g, L, s, st, out);
+                st = kRayQueued;
+            }
         }
+        if (s.kind != 0) st = ray_unit(g, s.R);
     }
 }
 
