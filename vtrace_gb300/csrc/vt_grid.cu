@@ -69,6 +69,19 @@ __device__ __forceinline__ BrickCoord brick_coord(uint64_t brick, int32_t bx, in
     return c;
 }
 
+// Brick of thread (blockIdx.x * blockDim.x + threadIdx.x) in `box`; false past its end.
+__device__ __forceinline__ bool box_brick(const BrickBox& box, int32_t bx, int32_t by,
+                                          BrickCoord& c, uint64_t& b) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)box.nx * box.ny * box.nz) return false;
+    c.bxi = box.x0 + (int32_t)(t % (uint64_t)box.nx);
+    const uint64_t r = t / (uint64_t)box.nx;
+    c.byi = box.y0 + (int32_t)(r % (uint64_t)box.ny);
+    c.bzi = box.z0 + (int32_t)(r / (uint64_t)box.ny);
+    b = (uint64_t)c.bxi + (uint64_t)bx * ((uint64_t)c.byi + (uint64_t)by * (uint64_t)c.bzi);
+    return true;
+}
+
 // Occupancy bits of 8 u8 voxels packed in a u64 when "occupied" means "nonzero index": the high
 // bit of each byte of ((v & 0x7F..) + 0x7F..) | v is set iff the byte is nonzero; the multiply
 // gathers the eight high bits into the top byte (bit k from byte k).
@@ -337,10 +350,10 @@ __global__ void __launch_bounds__(256) brick_distance_kernel(uint32_t* __restric
                                                              const uint8_t* __restrict__ in,
                                                              uint8_t* __restrict__ out,
                                                              int32_t bx, int32_t by, int32_t bz,
-                                                             uint64_t bricks) {
-    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= bricks) return;
-    const BrickCoord c = brick_coord(b, bx, by);
+                                                             BrickBox box) {
+    BrickCoord c;
+    uint64_t b;
+    if (!box_brick(box, bx, by, c, b)) return;
     const int32_t pos = AXIS == 0 ? c.bxi : (AXIS == 1 ? c.byi : c.bzi);
     const int32_t n = AXIS == 0 ? bx : (AXIS == 1 ? by : bz);
     const int64_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? (int64_t)bx : (int64_t)bx * by);
@@ -377,10 +390,10 @@ constexpr int kMaxOctantDistance = 15;
 __global__ void __launch_bounds__(256) brick_octant_x_kernel(const uint32_t* __restrict__ dir,
                                                              uint8_t* __restrict__ out,
                                                              int32_t bx, int32_t by,
-                                                             uint64_t bricks) {
-    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= bricks) return;
-    const BrickCoord c = brick_coord(b, bx, by);
+                                                             BrickBox box) {
+    BrickCoord c;
+    uint64_t b;
+    if (!box_brick(box, bx, by, c, b)) return;
     uint32_t packed = 0;
 #pragma unroll
     for (int neg = 0; neg < 2; ++neg) {
@@ -402,10 +415,10 @@ __global__ void __launch_bounds__(256) brick_octant_x_kernel(const uint32_t* __r
 __global__ void __launch_bounds__(256) brick_octant_y_kernel(const uint8_t* __restrict__ in,
                                                              uint16_t* __restrict__ out,
                                                              int32_t bx, int32_t by,
-                                                             uint64_t bricks) {
-    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= bricks) return;
-    const BrickCoord c = brick_coord(b, bx, by);
+                                                             BrickBox box) {
+    BrickCoord c;
+    uint64_t b;
+    if (!box_brick(box, bx, by, c, b)) return;
     uint32_t packed = 0;
 #pragma unroll
     for (int ny = 0; ny < 2; ++ny) {  // one walk per sy serves both sx
@@ -427,10 +440,10 @@ __global__ void __launch_bounds__(256) brick_octant_y_kernel(const uint8_t* __re
 __global__ void __launch_bounds__(256) brick_octant_z_kernel(const uint16_t* __restrict__ in,
                                                              uint32_t* __restrict__ out,
                                                              int32_t bx, int32_t by, int32_t bz,
-                                                             uint64_t bricks) {
-    const uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= bricks) return;
-    const BrickCoord c = brick_coord(b, bx, by);
+                                                             BrickBox box) {
+    BrickCoord c;
+    uint64_t b;
+    if (!box_brick(box, bx, by, c, b)) return;
     const int64_t plane = (int64_t)bx * by;
     uint32_t packed = 0;
 #pragma unroll
@@ -457,24 +470,49 @@ __global__ void __launch_bounds__(256) brick_octant_z_kernel(const uint16_t* __r
     out[b] = packed;
 }
 
+static unsigned box_blocks(const BrickBox& b) {
+    return (unsigned)(((uint64_t)b.nx * b.ny * b.nz + 255) / 256);
+}
+
+// The box grown by (gx, gy, gz) bricks on each side, clipped to the lattice.
+static BrickBox grow(const BrickBox& b, int32_t gx, int32_t gy, int32_t gz, int32_t bx, int32_t by,
+                     int32_t bz) {
+    BrickBox r;
+    r.x0 = max(b.x0 - gx, 0);
+    r.y0 = max(b.y0 - gy, 0);
+    r.z0 = max(b.z0 - gz, 0);
+    r.nx = min(b.x0 + b.nx + gx, bx) - r.x0;
+    r.ny = min(b.y0 + b.ny + gy, by) - r.y0;
+    r.nz = min(b.z0 + b.nz + gz, bz) - r.z0;
+    return r;
+}
+
 cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* tmp_y,
                                  uint32_t* oct, int32_t bx, int32_t by, int32_t bz,
-                                 cudaStream_t stream) {
-    const uint64_t bricks = (uint64_t)bx * by * bz;
-    const unsigned blocks = (unsigned)((bricks + 255) / 256);
-    brick_octant_x_kernel<<<blocks, 256, 0, stream>>>(dir, tmp_x, bx, by, bricks);
-    brick_octant_y_kernel<<<blocks, 256, 0, stream>>>(tmp_x, tmp_y, bx, by, bricks);
-    brick_octant_z_kernel<<<blocks, 256, 0, stream>>>(tmp_y, oct, bx, by, bz, bricks);
+                                 cudaStream_t stream, const BrickBox* changed) {
+    // pass z at the bricks within reach of a change reads pass y up to 14 bricks away in z, which
+    // reads pass x up to 14 away in y
+    const int32_t R = (int32_t)kMaxOctantDistance - 1;
+    const BrickBox all = {0, 0, 0, bx, by, bz};
+    const BrickBox w = changed ? grow(*changed, R, R, R, bx, by, bz) : all;
+    const BrickBox wy = grow(w, 0, 0, R, bx, by, bz), wx = grow(w, 0, R, R, bx, by, bz);
+    brick_octant_x_kernel<<<box_blocks(wx), 256, 0, stream>>>(dir, tmp_x, bx, by, wx);
+    brick_octant_y_kernel<<<box_blocks(wy), 256, 0, stream>>>(tmp_x, tmp_y, bx, by, wy);
+    brick_octant_z_kernel<<<box_blocks(w), 256, 0, stream>>>(tmp_y, oct, bx, by, bz, w);
     return cudaGetLastError();
 }
 
 cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,
-                                  int32_t bz, cudaStream_t stream) {
-    const uint64_t bricks = (uint64_t)bx * by * bz;
-    const unsigned blocks = (unsigned)((bricks + 255) / 256);
-    brick_distance_kernel<0><<<blocks, 256, 0, stream>>>(dir, nullptr, s.dist_a, bx, by, bz, bricks);
-    brick_distance_kernel<1><<<blocks, 256, 0, stream>>>(dir, s.dist_a, s.dist_b, bx, by, bz, bricks);
-    brick_distance_kernel<2><<<blocks, 256, 0, stream>>>(dir, s.dist_b, nullptr, bx, by, bz, bricks);
+                                  int32_t bz, cudaStream_t stream, const BrickBox* changed) {
+    // distances change only within kMaxBrickDistance of a change; each pass reads the previous
+    // one up to that far along its axis
+    const int32_t R = (int32_t)kMaxBrickDistance;
+    const BrickBox all = {0, 0, 0, bx, by, bz};
+    const BrickBox w = changed ? grow(*changed, R, R, R, bx, by, bz) : all;
+    const BrickBox w1 = grow(w, 0, 0, R, bx, by, bz), w0 = grow(w, 0, R, R, bx, by, bz);
+    brick_distance_kernel<0><<<box_blocks(w0), 256, 0, stream>>>(dir, nullptr, s.dist_a, bx, by, bz, w0);
+    brick_distance_kernel<1><<<box_blocks(w1), 256, 0, stream>>>(dir, s.dist_a, s.dist_b, bx, by, bz, w1);
+    brick_distance_kernel<2><<<box_blocks(w), 256, 0, stream>>>(dir, s.dist_b, nullptr, bx, by, bz, w);
     return cudaGetLastError();
 }
 

@@ -69,12 +69,19 @@ cudaError_t launch_brick_compact(const void* src, uint32_t format, int32_t nx, i
 
 // Phase 5: forward distances per ray octant (4 bits x 8 per brick) into `oct`; tmp_x holds one
 // byte and tmp_y two bytes per brick.
+// A box of bricks: origin and extent in brick coordinates.
+struct BrickBox {
+    int32_t x0, y0, z0, nx, ny, nz;
+};
+// Octant words of every brick, or (changed != nullptr) of the bricks a change of occupancy inside
+// `changed` can affect.
 cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* tmp_y,
                                  uint32_t* oct, int32_t bx, int32_t by, int32_t bz,
-                                 cudaStream_t stream);
+                                 cudaStream_t stream, const BrickBox* changed = nullptr);
 
 // Phase 4: Chebyshev distance of every empty brick to the nearest occupied one, into dir.
 cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,
-                                  int32_t bz, cudaStream_t stream);
+                                  int32_t bz, cudaStream_t stream,
+                                  const BrickBox* changed = nullptr);
 
 }  // namespace vt

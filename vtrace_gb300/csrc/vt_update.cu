@@ -13,8 +13,9 @@
 //      that became occupied;
 //   4. the new words and payloads are scattered into their slots and the directory entries
 //      rewritten;
-//   5. the Chebyshev distance field and the octant forward distances are recomputed over the
-//      whole directory (a few separable passes over 4 bytes per brick).
+//   5. the Chebyshev distance field and the octant forward distances are recomputed for the
+//      bricks within their caps (31 and 15 bricks) of the affected ones: a change cannot reach
+//      farther, and each separable pass reads the previous one only that far along its axis.
 //
 // The grid afterwards traverses exactly as a grid built from the updated dense array (same
 // occupancy, payload, distances and octant words; only slot numbers may differ).
@@ -266,11 +267,13 @@ extern "C" int32_t vt_grid_update(int32_t grid, const void* voxels, uint32_t ord
         BuildScratch bs;
         bs.dist_a = (uint8_t*)(scr + o_da);
         bs.dist_b = (uint8_t*)(scr + o_db);
+        const BrickBox changed = {u.bx0, u.by0, u.bz0, u.kx, u.ky, u.kz};
         if (e == cudaSuccess)
-            e = launch_brick_distance(bs, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st);
+            e = launch_brick_distance(bs, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st,
+                                      &changed);
         if (e == cudaSuccess)
             e = launch_brick_octants(g->dir, (uint8_t*)(scr + o_da), (uint16_t*)(scr + o_ty), g->oct,
-                                     (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st);
+                                     (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st, &changed);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) { rc = cuda_fail(e, "vt_grid_update: scatter"); break; }
         uint64_t nonempty = 0;
