@@ -56,6 +56,20 @@ def parse_args():
     return p.parse_args()
 
 
+def max_over_ranks(x, device):
+    """The largest of every rank's `x` (all ranks call it; one all-reduce)."""
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_rank, seconds, world):
+    """Whole-job rate of `world` replicas that each processed `units_per_rank` units, timed by
+    the slowest rank's `seconds` (weak scaling, no data-path exchange)."""
+    return world * units_per_rank / seconds
+
+
 def dist_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
             int(os.environ.get("WORLD_SIZE", "1")))
@@ -307,10 +321,8 @@ def run_ours(args):
     clocks = sampler.stop() if sampler else None
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
     if world > 1:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * rays_per_frame / (ms * 1e-3) / 1e6
+        ms = max_over_ranks(ms, "cuda")
+    value = replica_rate(rays_per_frame, ms * 1e-3, world) / 1e6
 
     # end to end through the C ABI with a pinned host output buffer
     host_out = torch.empty(npx * 16, dtype=torch.uint8, pin_memory=True)
@@ -325,10 +337,8 @@ def run_ours(args):
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = sum(e2e_times) / len(e2e_times)
     if world > 1:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * rays_per_frame / e2e_s / 1e6, "unit": "Mrays/s",
+        e2e_s = max_over_ranks(e2e_s, "cuda")
+    e2e = {"value": replica_rate(rays_per_frame, e2e_s, world) / 1e6, "unit": "Mrays/s",
            "h2d_bytes_per_step": 76, "d2h_bytes_per_step": npx * 16,
            "path": "vt_render_host (C ABI), pinned host output"}
 
