@@ -344,8 +344,10 @@ def run_ours(args):
 
     peak, peak_kind = measured_peak()
     achieved = algo_bytes / (ms * 1e-3) / 1e9
+    metric = METRIC if args.config == "shapes1024" else "Mrays/s (%dx%d, %d^3 grid)" % (
+        cam.width, cam.height, w["voxels"].shape[0])
     line = {
-        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world,
+        "metric": metric, "value": value, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generators, no dataset)",
@@ -370,7 +372,7 @@ def run_ours(args):
         line["parity"] = tie_divergence(w, grid)
     grid.destroy()
     del d_hits
-    if rank == 0 and args.serve_requests > 0 and world == 1:
+    if rank == 0 and args.serve_requests > 0 and world == 1 and args.config == "shapes1024":
         line["serve"] = serve_compare(args.serve_requests, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
