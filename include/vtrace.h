@@ -247,6 +247,11 @@ int32_t vt_grid_download_bricks(int32_t grid, uint32_t* directory, uint64_t* mas
  * o = (dx<0) | (dy<0)<<1 | (dz<0)<<2, nibble o holds the largest K <= 15 such that the K x K x K
  * bricks starting at the brick and extending along the octant's directions are all empty. */
 int32_t vt_grid_download_octants(int32_t grid, uint32_t* octants);
+/* Copy the grid's long-box words: 3 * bricks_total u32, axis-major (word a * bricks_total + brick
+ * for axis a = x, y, z); nibble o (octant o = (sx<0) | (sy<0)<<1 | (sz<0)<<2) holds the largest
+ * L <= 15 such that the box L bricks long along axis a and K x K across (K = the octant word's
+ * nibble o), from the brick toward octant o, holds no occupied brick. */
+int32_t vt_grid_download_long(int32_t grid, uint32_t* words);
 
 /* ---------------------------------------------------------------- tracing */
 

@@ -305,6 +305,34 @@ def expected_octants(directory, dims, cap=15):
     return out
 
 
+def expected_long(directory, octants, dims, cap=15):
+    """Long forward boxes by brute force: for axis a and octant o with forward cube K, the
+    largest L <= cap such that no occupied brick lies in the box L long along a and K x K across,
+    from the brick toward o (K = 0 gives 0, K = cap gives cap)."""
+    nx, ny, nz = dims
+    bx, by, bz = (nx + 7) // 8, (ny + 7) // 8, (nz + 7) // 8
+    occ = ((directory >> 31) == 0).reshape(bz, by, bx)
+    occ_c = np.argwhere(occ)[:, ::-1]
+    zz, yy, xx = np.meshgrid(np.arange(bz), np.arange(by), np.arange(bx), indexing="ij")
+    coords = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], 1)
+    out = np.zeros((3, len(coords)), np.uint32)
+    for o in range(8):
+        sgn = np.array([-1 if o & 1 else 1, -1 if o & 2 else 1, -1 if o & 4 else 1])
+        K = ((octants >> np.uint32(4 * o)) & np.uint32(15)).astype(np.int64)
+        rel = (occ_c[None, :, :] - coords[:, None, :]) * sgn if len(occ_c) else None
+        for a in range(3):
+            e1, e2 = (a + 1) % 3, (a + 2) % 3
+            if rel is not None:
+                inside = (rel >= 0).all(-1) & (rel[..., e1] < K[:, None]) & (rel[..., e2] < K[:, None])
+                L = np.where(inside, rel[..., a], cap).min(1)
+            else:
+                L = np.full(len(coords), cap)
+            L = np.minimum(np.maximum(L, K), cap)
+            L = np.where(K == 0, 0, np.where(K >= cap, cap, L))
+            out[a] |= L.astype(np.uint32) << np.uint32(4 * o)
+    return out
+
+
 def special_rays(rng, dims, n):
     """Axis-parallel, planar, exact-diagonal and grazing rays from inside and outside."""
     size = np.array(dims, np.float32)
@@ -343,7 +371,9 @@ def test_empty_space_skipping_is_exact(torch, dims, count):
         assert_hits_equal(hits_from_dev(d_hits), want, "counting kernel %r" % (dims,))
         wd, _, _ = expected_bricks(vox, pal)
         np.testing.assert_array_equal(d, wd)
-        np.testing.assert_array_equal(g.octants(), expected_octants(d, dims))
+        oc = g.octants()
+        np.testing.assert_array_equal(oc, expected_octants(d, dims))
+        np.testing.assert_array_equal(g.long_boxes(), expected_long(d, oc, dims))
     finally:
         g.destroy()
 

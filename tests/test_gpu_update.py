@@ -33,6 +33,7 @@ def same_as_fresh(g, fresh):
     np.testing.assert_array_equal(ma[da[full]], mb[db[full]])
     assert len(np.unique(da[full])) == len(full)  # no slot shared by two bricks
     np.testing.assert_array_equal(g.octants(), fresh.octants())
+    np.testing.assert_array_equal(g.long_boxes(), fresh.long_boxes())
 
 
 def random_box(rng, dims, max_edge):

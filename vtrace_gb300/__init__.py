@@ -186,6 +186,7 @@ SIGNATURES = [
     ("vt_grid_get_info", _i32, [_i32, ctypes.POINTER(GridInfo)]),
     ("vt_grid_download_bricks", _i32, [_i32, _vp, _vp]),
     ("vt_grid_download_octants", _i32, [_i32, _vp]),
+    ("vt_grid_download_long", _i32, [_i32, _vp]),
     ("vt_trace_rays", _i32, [_i32, _vp, _u64, _vp, _vp]),
     ("vt_trace_rays_host", _i32, [_i32, _vp, _u64, _vp]),
     ("vt_render", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp, _vp]),
@@ -478,6 +479,12 @@ class Grid:
         out = np.zeros(self.info()["bricks_total"], np.uint32)
         check(lib().vt_grid_download_octants(self.id, out.ctypes.data))
         return out
+
+    def long_boxes(self):
+        """Long-box words [3, bricks_total] (axis x, y, z)."""
+        out = np.zeros(3 * self.info()["bricks_total"], np.uint32)
+        check(lib().vt_grid_download_long(self.id, out.ctypes.data))
+        return out.reshape(3, -1)
 
     def destroy(self):
         if self.id is not None and self.id >= 0:

@@ -95,6 +95,8 @@ GridView Grid::view() const {
     GridView v;
     v.dir = dir;
     v.oct = oct;
+    v.lng = lng;
+    v.bricks = (uint32_t)bricks;
     v.masks = masks;
     v.payload8 = format == VT_PAYLOAD_U8 ? (const uint8_t*)payload : nullptr;
     v.payload32 = format == VT_PAYLOAD_RGBA8 ? (const uint32_t*)payload : nullptr;
@@ -113,6 +115,8 @@ GridView Grid::view() const {
 void Grid::release() {
     cudaFree(oct);
     oct = nullptr;
+    cudaFree(lng);
+    lng = nullptr;
     cudaFree(dir);
     cudaFree(masks);
     cudaFree(payload);
@@ -191,6 +195,7 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
         const size_t psize = format == VT_PAYLOAD_U8 ? 512 : 2048;
         if (cudaMalloc(&g->dir, g->bricks * 4) != cudaSuccess ||
             cudaMalloc(&g->oct, g->bricks * 4) != cudaSuccess ||
+            cudaMalloc(&g->lng, g->bricks * 12) != cudaSuccess ||
             cudaMalloc(&g->masks, slots * 64) != cudaSuccess ||
             cudaMalloc(&g->payload, slots * psize) != cudaSuccess) {
             cudaGetLastError();
@@ -206,9 +211,13 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
         e = launch_brick_octants(g->dir, (uint8_t*)s.words, (uint16_t*)((uint8_t*)s.words + ((g->bricks + 255) / 256) * 256),
                                  g->oct, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick octant kernels"); break; }
+        // and then the long-box runs and window minima (13 words per brick of the 16 there)
+        e = launch_brick_long(g->dir, g->oct, (uint32_t*)s.words, g->lng, (int32_t)g->bx,
+                              (int32_t)g->by, (int32_t)g->bz, stream);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "brick long-box kernels"); break; }
         e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick build"); break; }
-        g->bytes = g->bricks * 8 + slots * 64 + slots * psize + (g->palette ? 1024 : 0);
+        g->bytes = g->bricks * 20 + slots * 64 + slots * psize + (g->palette ? 1024 : 0);
         g->slot_capacity = slots;
         g->slots_used = g->nonempty;
     } while (0);
@@ -499,6 +508,17 @@ int32_t vt_grid_download_bricks(int32_t grid, uint32_t* directory, uint64_t* mas
         e = cudaMemcpyAsync(masks, g->masks, g->slots_used * 64, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_grid_download_bricks");
+    return VT_OK;
+}
+
+int32_t vt_grid_download_long(int32_t grid, uint32_t* words) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_grid_download_long: unknown grid");
+    if (!words) return fail(VT_EINVAL, "vt_grid_download_long: null output");
+    cudaStream_t st = state().stream;
+    cudaError_t e = cudaMemcpyAsync(words, g->lng, g->bricks * 12, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_grid_download_long");
     return VT_OK;
 }
 

@@ -28,6 +28,7 @@ struct Grid {
     uint32_t format = VT_PAYLOAD_U8;
     uint32_t* dir = nullptr;
     uint32_t* oct = nullptr;  // forward distances per ray octant
+    uint32_t* lng = nullptr;  // long forward boxes, 3 words per brick
     uint64_t* masks = nullptr;
     void* payload = nullptr;
     uint32_t* palette = nullptr;

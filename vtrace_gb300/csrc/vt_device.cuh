@@ -28,6 +28,8 @@ __device__ __forceinline__ bool brick_empty(uint32_t e) { return (e & kEmptyBit)
 struct GridView {
     const uint32_t* dir;
     const uint32_t* oct;  // forward distances per ray octant (4 bits x 8), or nullptr
+    const uint32_t* lng;  // long forward boxes: 3 words per brick, axis-major (lng[a * bricks +
+                          // brick], 4 bits x 8 octants), or nullptr
     const uint64_t* masks;
     const uint8_t* payload8;    // VT_PAYLOAD_U8
     const uint32_t* payload32;  // VT_PAYLOAD_RGBA8
@@ -36,6 +38,7 @@ struct GridView {
     int32_t bx, by, bz;
     uint32_t max_steps;  // nx + ny + nz (trace.frag:74)
     uint32_t format;
+    uint32_t bricks;     // bx * by * bz
 };
 
 struct LightView {
@@ -361,22 +364,42 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
 }
 
 // Voxel moves to the far face, along each stepping axis, of the empty box the ray crosses next
-// from the empty brick (bxi, byi, bzi).  Two boxes are known empty: the cube of bricks within
-// Chebyshev distance D - 1 (D from the directory entry `e`) and the box of K bricks from this
-// brick toward the ray's octant (K from the octant word `ow`).  Both reach R bricks forward
-// along every stepping direction (R = D for the cube, K for the forward box), and the ray only
-// moves forward, so the crossing uses R = max(D, K), clipped to the grid.  Axes with no step get
-// 1 (unused by cross_region).
+// from the empty brick (bxi, byi, bzi).  Three boxes are known empty: the cube of bricks within
+// Chebyshev distance D - 1 (D from the directory entry `e`), which reaches D bricks forward along
+// every stepping direction; the box of K bricks from this brick toward the ray's octant (K from
+// the octant word `ow`); and, when K >= D, the box that is K bricks across and L >= K bricks
+// long along the ray's dominant axis `dom` (L from the long-box word `lw`).  The ray only moves
+// forward, so the crossing uses the forward reach of the chosen box per axis, clipped to the
+// grid.  Axes with no step get 1 (unused by cross_region).
 __device__ __forceinline__ void empty_moves(const GridView& g, uint32_t e, uint32_t ow,
-                                            int32_t bxi, int32_t byi, int32_t bzi, int32_t vx,
-                                            int32_t vy, int32_t vz, int32_t stx, int32_t sty,
-                                            int32_t stz, uint32_t oct_shift, int32_t& nxe,
-                                            int32_t& nye, int32_t& nze) {
+                                            uint32_t lw, int32_t bxi, int32_t byi, int32_t bzi,
+                                            int32_t vx, int32_t vy, int32_t vz, int32_t stx,
+                                            int32_t sty, int32_t stz, uint32_t oct_shift,
+                                            int32_t dom, int32_t& nxe, int32_t& nye,
+                                            int32_t& nze) {
     const int32_t D = max((int32_t)(e & 0xFFu), 1);
-    const int32_t R = max(D, (int32_t)((ow >> oct_shift) & 15u));
-    nxe = stx > 0 ? min((bxi + R) << 3, g.nx) - vx : (stx < 0 ? vx - max((bxi - R + 1) << 3, 0) + 1 : 1);
-    nye = sty > 0 ? min((byi + R) << 3, g.ny) - vy : (sty < 0 ? vy - max((byi - R + 1) << 3, 0) + 1 : 1);
-    nze = stz > 0 ? min((bzi + R) << 3, g.nz) - vz : (stz < 0 ? vz - max((bzi - R + 1) << 3, 0) + 1 : 1);
+    const int32_t K = (int32_t)((ow >> oct_shift) & 15u);
+    int32_t rx = D, ry = D, rz = D;
+    if (K >= D) {
+        const int32_t L = max(K, (int32_t)((lw >> oct_shift) & 15u));
+        rx = dom == 0 ? L : K;
+        ry = dom == 1 ? L : K;
+        rz = dom == 2 ? L : K;
+    }
+    nxe = stx > 0 ? min((bxi + rx) << 3, g.nx) - vx : (stx < 0 ? vx - max((bxi - rx + 1) << 3, 0) + 1 : 1);
+    nye = sty > 0 ? min((byi + ry) << 3, g.ny) - vy : (sty < 0 ? vy - max((byi - ry + 1) << 3, 0) + 1 : 1);
+    nze = stz > 0 ? min((bzi + rz) << 3, g.nz) - vz : (stz < 0 ? vz - max((bzi - rz + 1) << 3, 0) + 1 : 1);
+}
+
+// Dominant axis of a direction (largest |component|; ties to the lower axis).
+__device__ __forceinline__ int32_t dominant_axis(float dx, float dy, float dz) {
+    const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+    return ax >= ay ? (ax >= az ? 0 : 2) : (ay >= az ? 1 : 2);
+}
+
+// The long-box words of the ray's dominant axis, or nullptr.
+__device__ __forceinline__ const uint32_t* long_words(const GridView& g, int32_t dom) {
+    return g.lng ? g.lng + (size_t)dom * g.bricks : nullptr;
 }
 
 // The octant word of brick `bidx`; 0 (no forward boxes) for a grid built without octant words.
@@ -410,6 +433,8 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
     }
     const uint32_t max_steps = g.max_steps;
     const uint32_t oshift = octant_shift(stx, sty, stz);
+    const int32_t dom = dominant_axis(dx, dy, dz);
+    const uint32_t* lp = long_words(g, dom);
     uint32_t steps = 0, slot = kEmptyBit;  // steps: only bounds the occupied-brick loop
     bool mx = false, my = false, mz = false, hit = false;
     // every pass of this loop advances at least one axis, monotonically, inside the grid
@@ -420,6 +445,7 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
         const uint32_t bidx = (uint32_t)bxi + (uint32_t)g.bx * ((uint32_t)byi + (uint32_t)g.by * (uint32_t)bzi);
         const uint32_t e = __ldg(g.dir + bidx);
         const uint32_t ow = octant_word(g, bidx);
+        const uint32_t lw = lp ? __ldg(lp + bidx) : 0u;
         if (!brick_empty(e)) {
             slot = e;
             const uint64_t* mk = g.masks + (size_t)slot * 8;
@@ -439,7 +465,8 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
             if (hit) break;
         } else {
             int32_t nxe, nye, nze;
-            empty_moves(g, e, ow, bxi, byi, bzi, vx, vy, vz, stx, sty, stz, oshift, nxe, nye, nze);
+            empty_moves(g, e, ow, lw, bxi, byi, bzi, vx, vy, vz, stx, sty, stz, oshift, dom, nxe,
+                        nye, nze);
             cross_region(sx, sy, sz, vx, vy, vz, dlx, dly, dlz, stx, sty, stz, nxe, nye, nze, mx,
                          my, mz);
         }

@@ -470,6 +470,177 @@ __global__ void __launch_bounds__(256) brick_octant_z_kernel(const uint16_t* __r
     out[b] = packed;
 }
 
+// Forward empty runs: for axis a and direction s = +1 / -1, the number of consecutive empty
+// bricks from this one (itself included) toward s along a, capped at kMaxOctantDistance; beyond the
+// grid counts as empty.  Nibble 2a + (s < 0).
+__global__ void __launch_bounds__(256) brick_run_kernel(const uint32_t* __restrict__ dir,
+                                                        uint32_t* __restrict__ run, int32_t bx,
+                                                        int32_t by, int32_t bz, BrickBox box) {
+    BrickCoord c;
+    uint64_t b;
+    if (!box_brick(box, bx, by, c, b)) return;
+    const int32_t pos[3] = {c.bxi, c.byi, c.bzi}, n[3] = {bx, by, bz};
+    const int64_t stride[3] = {1, (int64_t)bx, (int64_t)bx * by};
+    uint32_t packed = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int neg = 0; neg < 2; ++neg) {
+            const int32_t sg = neg ? -1 : 1;
+            int32_t best = kMaxOctantDistance;
+            for (int32_t k = 0; k < (int32_t)kMaxOctantDistance; ++k) {
+                const int32_t p = pos[a] + k * sg;
+                if (p < 0 || p >= n[a]) break;
+                if (!brick_empty(__ldg(dir + (int64_t)b + (int64_t)k * sg * stride[a]))) {
+                    best = k;
+                    break;
+                }
+            }
+            packed |= (uint32_t)best << (4 * (2 * a + neg));
+        }
+    }
+    run[b] = packed;
+}
+
+// Long forward boxes read directly off the runs (K x K cells per octant and axis): cheaper than
+// the pyramid below for the few bricks a paging update touches.  Same values.
+__global__ void __launch_bounds__(256) brick_long_direct_kernel(const uint32_t* __restrict__ oct,
+                                                                const uint32_t* __restrict__ run,
+                                                                uint32_t* __restrict__ lng,
+                                                                int32_t bx, int32_t by, int32_t bz,
+                                                                BrickBox box) {
+    BrickCoord c;
+    uint64_t b;
+    if (!box_brick(box, bx, by, c, b)) return;
+    const uint64_t bricks = (uint64_t)bx * by * bz;
+    const int32_t pos[3] = {c.bxi, c.byi, c.bzi}, n[3] = {bx, by, bz};
+    const int64_t stride[3] = {1, (int64_t)bx, (int64_t)bx * by};
+    const uint32_t ow = __ldg(oct + b);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int e1 = (a + 1) % 3, e2 = (a + 2) % 3;
+        uint32_t packed = 0;
+        for (int o = 0; o < 8; ++o) {
+            const int32_t K = (int32_t)((ow >> (4 * o)) & 15u);
+            int32_t L = K;
+            if (K > 0 && K < (int32_t)kMaxOctantDistance) {
+                const int32_t s1 = (o >> e1) & 1 ? -1 : 1, s2 = (o >> e2) & 1 ? -1 : 1;
+                const uint32_t nib = 4u * (2u * a + ((o >> a) & 1));
+                L = kMaxOctantDistance;
+                for (int32_t i = 0; i < K && L > K; ++i) {
+                    const int32_t p1 = pos[e1] + i * s1;
+                    if (p1 < 0 || p1 >= n[e1]) break;
+                    for (int32_t j = 0; j < K && L > K; ++j) {
+                        const int32_t p2 = pos[e2] + j * s2;
+                        if (p2 < 0 || p2 >= n[e2]) break;
+                        const int64_t cc = (int64_t)b + (int64_t)i * s1 * stride[e1] +
+                                           (int64_t)j * s2 * stride[e2];
+                        L = min(L, (int32_t)((__ldg(run + cc) >> nib) & 15u));
+                    }
+                }
+                L = max(L, K);
+            }
+            packed |= (uint32_t)L << (4 * o);
+        }
+        lng[(uint64_t)a * bricks + b] = packed;
+    }
+}
+
+// Window minima of the runs: level p of axis a holds, for octant o (nibble o), the smallest run
+// along a toward o over the 2^p x 2^p bricks across from the brick toward o (cells beyond the
+// grid count as the cap).  Level 0 repacks the runs per octant; level p + 1 is the minimum of four
+// level-p blocks.  Layout: pyr[(p * 3 + a) * bricks + brick].
+__global__ void __launch_bounds__(256) brick_pyramid_kernel(const uint32_t* __restrict__ run,
+                                                            uint32_t* __restrict__ pyr, int32_t p,
+                                                            int32_t bx, int32_t by, int32_t bz,
+                                                            BrickBox box) {
+    BrickCoord c;
+    uint64_t b;
+    if (!box_brick(box, bx, by, c, b)) return;
+    const uint64_t bricks = (uint64_t)bx * by * bz;
+    const int32_t pos[3] = {c.bxi, c.byi, c.bzi}, n[3] = {bx, by, bz};
+    const int64_t stride[3] = {1, (int64_t)bx, (int64_t)bx * by};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        uint32_t packed = 0;
+        if (p == 0) {
+            const uint32_t r = __ldg(run + b);
+#pragma unroll
+            for (int o = 0; o < 8; ++o) packed |= ((r >> (4 * (2 * a + ((o >> a) & 1)))) & 15u) << (4 * o);
+        } else {
+            const int e1 = (a + 1) % 3, e2 = (a + 2) % 3;
+            const int32_t h = 1 << (p - 1);
+            const uint32_t* prev = pyr + (uint64_t)((p - 1) * 3 + a) * bricks;
+            const uint32_t self = __ldg(prev + b);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {  // lateral signs (bit 0: e1 negative, bit 1: e2 negative)
+                const int32_t s1 = (q & 1) ? -1 : 1, s2 = (q & 2) ? -1 : 1;
+                const bool in1 = pos[e1] + h * s1 >= 0 && pos[e1] + h * s1 < n[e1];
+                const bool in2 = pos[e2] + h * s2 >= 0 && pos[e2] + h * s2 < n[e2];
+                const int64_t d1 = (int64_t)h * s1 * stride[e1], d2 = (int64_t)h * s2 * stride[e2];
+                const uint32_t w1 = in1 ? __ldg(prev + b + d1) : 0xFFFFFFFFu;
+                const uint32_t w2 = in2 ? __ldg(prev + b + d2) : 0xFFFFFFFFu;
+                const uint32_t w3 = in1 && in2 ? __ldg(prev + b + d1 + d2) : 0xFFFFFFFFu;
+#pragma unroll
+                for (int o = 0; o < 8; ++o) {
+                    if (((o >> e1) & 1) != (q & 1) || ((o >> e2) & 1) != ((q >> 1) & 1)) continue;
+                    const uint32_t sh = 4 * o;
+                    const uint32_t m = min(min((self >> sh) & 15u, (w1 >> sh) & 15u),
+                                           min((w2 >> sh) & 15u, (w3 >> sh) & 15u));
+                    packed |= m << sh;
+                }
+            }
+        }
+        pyr[(uint64_t)(p * 3 + a) * bricks + b] = packed;
+    }
+}
+
+// Long forward boxes: for axis a and octant o with forward cube K (octant word), the largest
+// L <= kMaxOctantDistance such that the box L bricks long along a and K x K across, all toward o,
+// is empty: the smallest run along a over the box's K x K cross-section, read as the minimum of
+// four overlapping 2^p blocks of the pyramid (2^p <= K < 2^(p+1)).  L >= K since the cube is
+// empty; K = 0 (occupied brick) gives 0 and K at the cap gives the cap.
+__global__ void __launch_bounds__(256) brick_long_kernel(const uint32_t* __restrict__ oct,
+                                                         const uint32_t* __restrict__ pyr,
+                                                         uint32_t* __restrict__ lng, int32_t bx,
+                                                         int32_t by, int32_t bz, BrickBox box) {
+    BrickCoord c;
+    uint64_t b;
+    if (!box_brick(box, bx, by, c, b)) return;
+    const uint64_t bricks = (uint64_t)bx * by * bz;
+    const int32_t pos[3] = {c.bxi, c.byi, c.bzi}, n[3] = {bx, by, bz};
+    const int64_t stride[3] = {1, (int64_t)bx, (int64_t)bx * by};
+    const uint32_t ow = __ldg(oct + b);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int e1 = (a + 1) % 3, e2 = (a + 2) % 3;
+        uint32_t packed = 0;
+        for (int o = 0; o < 8; ++o) {
+            const int32_t K = (int32_t)((ow >> (4 * o)) & 15u);
+            int32_t L = K;
+            if (K > 0 && K < (int32_t)kMaxOctantDistance) {
+                const int32_t p = 31 - __clz(K);  // 2^p <= K < 2^(p+1), p <= 3
+                const int32_t off = K - (1 << p);
+                const int32_t s1 = (o >> e1) & 1 ? -1 : 1, s2 = (o >> e2) & 1 ? -1 : 1;
+                const uint32_t* lev = pyr + (uint64_t)(p * 3 + a) * bricks;
+                L = kMaxOctantDistance;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int32_t o1 = (k & 1) ? off : 0, o2 = (k & 2) ? off : 0;
+                    const int32_t p1 = pos[e1] + o1 * s1, p2 = pos[e2] + o2 * s2;
+                    if (p1 < 0 || p1 >= n[e1] || p2 < 0 || p2 >= n[e2]) continue;
+                    const int64_t cc = (int64_t)b + (int64_t)o1 * s1 * stride[e1] +
+                                       (int64_t)o2 * s2 * stride[e2];
+                    L = min(L, (int32_t)((__ldg(lev + cc) >> (4 * o)) & 15u));
+                }
+                L = max(L, K);
+            }
+            packed |= (uint32_t)L << (4 * o);
+        }
+        lng[(uint64_t)a * bricks + b] = packed;
+    }
+}
+
 static unsigned box_blocks(const BrickBox& b) {
     return (unsigned)(((uint64_t)b.nx * b.ny * b.nz + 255) / 256);
 }
@@ -499,6 +670,31 @@ cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* 
     brick_octant_x_kernel<<<box_blocks(wx), 256, 0, stream>>>(dir, tmp_x, bx, by, wx);
     brick_octant_y_kernel<<<box_blocks(wy), 256, 0, stream>>>(tmp_x, tmp_y, bx, by, wy);
     brick_octant_z_kernel<<<box_blocks(w), 256, 0, stream>>>(tmp_y, oct, bx, by, bz, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_brick_long(const uint32_t* dir, const uint32_t* oct, uint32_t* tmp,
+                              uint32_t* lng, int32_t bx, int32_t by, int32_t bz,
+                              cudaStream_t stream, const BrickBox* changed) {
+    // tmp: runs (1 word per brick), then the pyramid (12 words per brick).  With a change, long
+    // boxes are recomputed within 15 bricks of it, directly from the runs, which they read up to
+    // 13 bricks across (and the runs are recomputed there).
+    const int32_t R = (int32_t)kMaxOctantDistance;
+    const uint64_t bricks = (uint64_t)bx * by * bz;
+    uint32_t* run = tmp;
+    uint32_t* pyr = tmp + bricks;
+    if (changed) {
+        const BrickBox w = grow(*changed, R, R, R, bx, by, bz);
+        const BrickBox wr = grow(w, R - 2, R - 2, R - 2, bx, by, bz);
+        brick_run_kernel<<<box_blocks(wr), 256, 0, stream>>>(dir, run, bx, by, bz, wr);
+        brick_long_direct_kernel<<<box_blocks(w), 256, 0, stream>>>(oct, run, lng, bx, by, bz, w);
+        return cudaGetLastError();
+    }
+    const BrickBox w = {0, 0, 0, bx, by, bz};
+    brick_run_kernel<<<box_blocks(w), 256, 0, stream>>>(dir, run, bx, by, bz, w);
+    for (int32_t p = 0; p < 4; ++p)
+        brick_pyramid_kernel<<<box_blocks(w), 256, 0, stream>>>(run, pyr, p, bx, by, bz, w);
+    brick_long_kernel<<<box_blocks(w), 256, 0, stream>>>(oct, pyr, lng, bx, by, bz, w);
     return cudaGetLastError();
 }
 

@@ -80,6 +80,11 @@ cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* 
                                  cudaStream_t stream, const BrickBox* changed = nullptr);
 
 // Phase 4: Chebyshev distance of every empty brick to the nearest occupied one, into dir.
+// Long forward boxes (3 words per brick, axis-major) from the directory and the octant words;
+// tmp holds 13 words per brick.
+cudaError_t launch_brick_long(const uint32_t* dir, const uint32_t* oct, uint32_t* tmp,
+                              uint32_t* lng, int32_t bx, int32_t by, int32_t bz,
+                              cudaStream_t stream, const BrickBox* changed = nullptr);
 cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,
                                   int32_t bz, cudaStream_t stream,
                                   const BrickBox* changed = nullptr);

@@ -24,6 +24,7 @@ struct LaneRay {
     bool mx, my, mz;     // axes stepped on the final iteration
     uint32_t flags;      // VT_HIT_FLAG_INVALID for rejected input
     uint32_t oshift;     // nibble of the ray's octant in the octant words
+    int32_t dom;         // dominant axis of the direction
 };
 
 // Validity, slab entry and DDA set-up (trace.frag:68-71).  Returns kRayRunning, or the final
@@ -69,6 +70,7 @@ __device__ __forceinline__ int ray_begin(const GridView& g, const float o[3], co
     }
     R.guard = g.nx + g.ny + g.nz + 2;
     R.oshift = octant_shift(R.stx, R.sty, R.stz);
+    R.dom = dominant_axis(d[0], d[1], d[2]);
     return grid_inside(g, R.vx, R.vy, R.vz) ? kRayRunning : kRayMiss;
 }
 
@@ -85,6 +87,8 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
     const uint32_t bidx = (uint32_t)bxi + (uint32_t)g.bx * ((uint32_t)byi + (uint32_t)g.by * (uint32_t)bzi);
     const uint32_t e = __ldg(g.dir + bidx);
     const uint32_t ow = octant_word(g, bidx);
+    const uint32_t* lp = long_words(g, R.dom);
+    const uint32_t lw = lp ? __ldg(lp + bidx) : 0u;
     if (!brick_empty(e)) {
         const uint64_t* mk = g.masks + (size_t)e * 8;
         const int32_t ex = stx > 0 ? min((bxi << 3) + 8, g.nx) : (stx < 0 ? (bxi << 3) - 1 : INT_MIN);
@@ -103,7 +107,8 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
         }
     } else {
         int32_t nxe, nye, nze;
-        empty_moves(g, e, ow, bxi, byi, bzi, vx, vy, vz, stx, sty, stz, R.oshift, nxe, nye, nze);
+        empty_moves(g, e, ow, lw, bxi, byi, bzi, vx, vy, vz, stx, sty, stz, R.oshift, R.dom, nxe,
+                    nye, nze);
         cross_region(sx, sy, sz, vx, vy, vz, dlx, dly, dlz, stx, sty, stz, nxe, nye, nze, mx, my,
                      mz);
     }

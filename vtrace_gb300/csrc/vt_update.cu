@@ -13,9 +13,9 @@
 //      that became occupied;
 //   4. the new words and payloads are scattered into their slots and the directory entries
 //      rewritten;
-//   5. the Chebyshev distance field and the octant forward distances are recomputed for the
-//      bricks within their caps (31 and 15 bricks) of the affected ones: a change cannot reach
-//      farther, and each separable pass reads the previous one only that far along its axis.
+//   5. the Chebyshev distance field, the octant forward distances and the long forward boxes are
+//      recomputed for the bricks within their caps (31, 15 and 15 bricks) of the affected ones:
+//      a change cannot reach farther, and each pass reads the previous one only that far.
 //
 // The grid afterwards traverses exactly as a grid built from the updated dense array (same
 // occupancy, payload, distances and octant words; only slot numbers may differ).
@@ -194,7 +194,8 @@ extern "C" int32_t vt_grid_update(int32_t grid, const void* voxels, uint32_t ord
     const size_t o_pay = o_words + al(K * 64), o_flags = o_pay + al(K * 512 * elem);
     const size_t o_old = o_flags + al(K * 4), o_slots = o_old + al(K * 4), o_delta = o_slots + al(K * 4);
     const size_t o_da = o_delta + 256, o_db = o_da + al(g->bricks), o_ty = o_db + al(g->bricks);
-    const size_t total = o_ty + al(g->bricks * 2);
+    const size_t o_run = o_ty + al(g->bricks * 2);
+    const size_t total = o_run + al(g->bricks * 4);
     char* scr = nullptr;
     cudaError_t e = cudaMallocAsync((void**)&scr, total, st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_grid_update: scratch");
@@ -274,6 +275,9 @@ extern "C" int32_t vt_grid_update(int32_t grid, const void* voxels, uint32_t ord
         if (e == cudaSuccess)
             e = launch_brick_octants(g->dir, (uint8_t*)(scr + o_da), (uint16_t*)(scr + o_ty), g->oct,
                                      (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st, &changed);
+        if (e == cudaSuccess)
+            e = launch_brick_long(g->dir, g->oct, (uint32_t*)(scr + o_run), g->lng, (int32_t)g->bx,
+                                  (int32_t)g->by, (int32_t)g->bz, st, &changed);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) { rc = cuda_fail(e, "vt_grid_update: scatter"); break; }
         uint64_t nonempty = 0;
