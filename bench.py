@@ -290,8 +290,12 @@ def run_ours(args):
     stream = torch.cuda.Stream()  # the render and its events share this stream
     torch.cuda.set_stream(stream)
 
-    # counters of one frame (counting kernel, not timed): rays traced and algorithmic bytes
+    # counters of one frame (counting kernel, not timed): rays traced and algorithmic bytes, and
+    # the frame's distinct footprint
     stats = vt.render_stats(grid, cam, light, d_hits)
+    fp = vt.render_footprint(grid, cam, light, d_hits)
+    unique_bytes = (4 * fp["bricks"] + 64 * fp["nonempty_bricks"] + 512 * fp["hit_bricks"] +
+                    16 * npx)
     rays_per_frame = stats["rays"]
     algo_bytes = (4 * stats["bricks_entered"] + 64 * stats["nonempty_bricks_entered"] +
                   5 * stats["hits"] + 16 * npx)
@@ -362,7 +366,14 @@ def run_ours(args):
                      "traffic": profiled_traffic("shapes1024_1080p") if args.config == "shapes1024" else None,
                      "traffic_source": "profiles/render_shapes1024_1080p.md (ncu, one launch)",
                      "algorithmic_bytes_per_launch": algo_bytes,
-                     "kernel": "vt::render_kernel<false>"},
+                     "kernel": "vt::render_kernel<false>",
+                     "unique_footprint": {
+                         "bytes_per_launch": unique_bytes,
+                         "achieved": unique_bytes / (ms * 1e-3) / 1e9,
+                         "frac": unique_bytes / (ms * 1e-3) / 1e9 / peak,
+                         "bricks": fp, "note": "distinct directory entries x 4 B + masks x 64 B "
+                         "+ hit bricks' payload x 512 B + 16 B records, along the reference's "
+                         "iteration path"}},
         "clocks": clocks,
         "grid_info": grid.info(),
     }

@@ -273,6 +273,17 @@ int32_t vt_render_host(int32_t grid, const vt_camera* camera, const vt_light* li
  * kernel build; for roofline accounting, not for timing).  rays == NULL selects the render form. */
 int32_t vt_render_stats(int32_t grid, const vt_camera* camera, const vt_light* light,
                         vt_hit* d_hits, vt_trace_stats* stats);
+/* Distinct bricks a frame touches along the reference's iteration path (the counting kernel, not
+ * timed): the conservative "unique footprint" of a launch, beside the per-ray byte counts of
+ * vt_trace_stats. */
+typedef struct vt_footprint {
+    uint64_t bricks;          /* distinct bricks entered (directory entries read) */
+    uint64_t nonempty_bricks; /* distinct occupied bricks entered (masks read) */
+    uint64_t hit_bricks;      /* distinct bricks holding a hit voxel (payload read) */
+    uint64_t reserved;
+} vt_footprint;
+int32_t vt_render_footprint(int32_t grid, const vt_camera* camera, const vt_light* light,
+                            vt_hit* d_hits, vt_footprint* out);
 int32_t vt_trace_rays_stats(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_hit* d_hits,
                             vt_trace_stats* stats);
 

@@ -455,3 +455,23 @@ def test_host_forms_split_into_pieces_agree(torch):
         assert_hits_equal(vt.trace_rays_host(g, rays), hits, "trace_rays_host chunks")
     finally:
         g.destroy()
+
+
+def test_render_footprint_bounds(torch):
+    """The distinct footprint of a frame: hit bricks are exactly the bricks of the hit voxels (no
+    shadow rays), within the occupied bricks entered, within the bricks entered."""
+    w = workloads.terrain256(n=96, width=160, height=120)
+    g = vt.Grid.from_u8(w["voxels"], w["palette"])
+    try:
+        img, d_hits = device_render(torch, g, w["camera"], None)
+        fp = vt.render_footprint(g, w["camera"], None, d_hits)
+        st = vt.render_stats(g, w["camera"], None, d_hits)
+        hit = (img["face"] & vt.FLAG_HIT) != 0
+        bx, by = 12, 12
+        bricks = np.unique((img["x"][hit] // 8).astype(np.int64) + bx * ((img["y"][hit] // 8).astype(np.int64) +
+                                                                        by * (img["z"][hit] // 8).astype(np.int64)))
+        assert fp["hit_bricks"] == len(bricks) > 0
+        assert fp["hit_bricks"] <= fp["nonempty_bricks"] <= min(st["nonempty_bricks_entered"], g.info()["bricks_nonempty"])
+        assert fp["nonempty_bricks"] <= fp["bricks"] <= min(st["bricks_entered"], g.info()["bricks_total"])
+    finally:
+        g.destroy()

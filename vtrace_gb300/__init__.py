@@ -143,6 +143,11 @@ def make_path_params(spp=4, max_bounces=3, seed=0, out_format=PATH_OUT_F32X4,
     return p
 
 
+class Footprint(ctypes.Structure):
+    _fields_ = [("bricks", ctypes.c_uint64), ("nonempty_bricks", ctypes.c_uint64),
+                ("hit_bricks", ctypes.c_uint64), ("reserved", ctypes.c_uint64)]
+
+
 class VoxInfo(ctypes.Structure):
     _fields_ = [("version", ctypes.c_uint32), ("models", ctypes.c_uint32),
                 ("has_palette", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
@@ -193,6 +198,8 @@ SIGNATURES = [
     ("vt_render_host", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp]),
     ("vt_render_stats", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp,
                                ctypes.POINTER(TraceStats)]),
+    ("vt_render_footprint", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp,
+                                   ctypes.POINTER(Footprint)]),
     ("vt_trace_rays_stats", _i32, [_i32, _vp, _u64, _vp, ctypes.POINTER(TraceStats)]),
     ("vt_path_trace", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(PathParams), _vp, _vp,
                              _vp]),
@@ -544,6 +551,15 @@ def path_trace_host(grid, camera, params):
     check(lib().vt_path_trace_host(grid.id, ctypes.byref(camera), ctypes.byref(params),
                                    out.ctypes.data, ctypes.byref(rays)))
     return out, rays.value
+
+
+def render_footprint(grid, camera, light, d_hits):
+    """Distinct bricks one frame touches: {"bricks", "nonempty_bricks", "hit_bricks"}."""
+    fp = Footprint()
+    check(lib().vt_render_footprint(grid.id, ctypes.byref(camera),
+                                    ctypes.byref(light) if light is not None else None,
+                                    _ptr(d_hits), ctypes.byref(fp)))
+    return {"bricks": fp.bricks, "nonempty_bricks": fp.nonempty_bricks, "hit_bricks": fp.hit_bricks}
 
 
 def render_stats(grid, camera, light, d_hits):

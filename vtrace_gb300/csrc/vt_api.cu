@@ -656,6 +656,44 @@ int32_t vt_render_stats(int32_t grid, const vt_camera* camera, const vt_light* l
     return VT_OK;
 }
 
+int32_t vt_render_footprint(int32_t grid, const vt_camera* camera, const vt_light* light,
+                            vt_hit* d_hits, vt_footprint* out) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_render_footprint: unknown grid");
+    int32_t rc = check_camera(camera);
+    if (rc) return rc;
+    if (!out || !d_hits || ((uintptr_t)d_hits & 15u)) return fail(VT_EINVAL, "vt_render_footprint: bad buffer");
+    const size_t words = (g->bricks + 31) / 32;
+    const size_t bytes = 256 + 3 * words * 4;
+    char* buf = nullptr;
+    cudaStream_t st = state().stream;
+    if (cudaMalloc(&buf, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(VT_ENOMEM, "cudaMalloc(footprint)");
+    }
+    Counters hc;
+    memset(&hc, 0, sizeof(hc));
+    hc.touched = (unsigned int*)(buf + 256);
+    std::vector<uint32_t> maps(3 * words);
+    cudaError_t e = cudaMemsetAsync(buf, 0, bytes, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf, &hc, sizeof(hc), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = launch_render(g->view(), *camera, light_view(light), (uint4*)d_hits, (Counters*)buf, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(maps.data(), buf + 256, 3 * words * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_render_footprint");
+    uint64_t n[3] = {0, 0, 0};
+    for (int m = 0; m < 3; ++m)
+        for (size_t i = 0; i < words; ++i) n[m] += (uint64_t)__builtin_popcount(maps[m * words + i]);
+    out->bricks = n[0];
+    out->nonempty_bricks = n[1];
+    out->hit_bricks = n[2];
+    out->reserved = 0;
+    return VT_OK;
+}
+
 int32_t vt_render_host(int32_t grid, const vt_camera* camera, const vt_light* light,
                        vt_hit* hits) {
     Grid* g = lookup_grid(grid);

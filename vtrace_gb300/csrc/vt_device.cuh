@@ -49,8 +49,13 @@ struct LightView {
 };
 
 // Traversal counters of the counting kernels (vt_trace_stats).
+struct GridView;
+
 struct Counters {
     unsigned long long rays, shadow_rays, hits, steps, bricks, nonempty, tested, ties;
+    // nullptr, or three bitmaps of ceil(bricks / 32) words: bricks entered, occupied bricks
+    // entered, bricks holding a hit voxel (the launch's distinct footprint)
+    unsigned int* touched;
 };
 
 template <bool STATS>
@@ -64,6 +69,8 @@ struct Tally {
     __device__ __forceinline__ void tested() {}
     __device__ __forceinline__ void tie() {}
     __device__ __forceinline__ void flush(Counters*) {}
+    __device__ __forceinline__ void bind(const Counters*, uint32_t) {}
+    __device__ __forceinline__ void mark(uint32_t, int) {}
 };
 
 template <>
@@ -77,6 +84,22 @@ struct Tally<true> {
     __device__ __forceinline__ void nonempty() { c.nonempty++; }
     __device__ __forceinline__ void tested() { c.tested++; }
     __device__ __forceinline__ void tie() { c.ties++; }
+    unsigned int* fp = nullptr;
+    uint32_t fp_words = 0;
+    // footprint bitmaps of the launch, if the counters carry them (`bricks` of the grid)
+    __device__ __forceinline__ void bind(const Counters* g, uint32_t bricks) {
+        if (g && g->touched) {
+            fp = g->touched;
+            fp_words = (bricks + 31u) / 32u;
+        }
+    }
+    // set bit `b` of footprint map `m` (read first: most bricks are already marked)
+    __device__ __forceinline__ void mark(uint32_t b, int m) {
+        if (!fp) return;
+        unsigned int* w = fp + (size_t)m * fp_words + (b >> 5);
+        const unsigned int bit = 1u << (b & 31u);
+        if (!(*(volatile unsigned int*)w & bit)) atomicOr(w, bit);
+    }
     __device__ __forceinline__ void flush(Counters* g) {
         atomicAdd(&g->rays, c.rays);
         atomicAdd(&g->shadow_rays, c.shadow_rays);
@@ -141,7 +164,11 @@ __device__ __forceinline__ void dda_literal(const GridView& g, int32_t vx, int32
         slot = __ldg(g.dir + brick);
         if (brick != prev) {
             tl.brick();
-            if (!brick_empty(slot)) tl.nonempty();
+            tl.mark((uint32_t)brick, 0);
+            if (!brick_empty(slot)) {
+                tl.nonempty();
+                tl.mark((uint32_t)brick, 1);
+            }
         }
         prev = brick;
         if (!brick_empty(slot)) {
@@ -222,7 +249,10 @@ __device__ __forceinline__ void dda(const GridView& g, float px, float py, float
     if (grid_inside(g, vx, vy, vz)) {
         for (;;) {
             const int32_t bxi = vx >> 3, byi = vy >> 3, bzi = vz >> 3;
-            slot = __ldg(g.dir + ((size_t)bxi + (size_t)g.bx * ((size_t)byi + (size_t)g.by * bzi)));
+            const uint32_t bidx = (uint32_t)bxi + (uint32_t)g.bx * ((uint32_t)byi + (uint32_t)g.by * (uint32_t)bzi);
+            slot = __ldg(g.dir + bidx);
+            tl.mark(bidx, 0);
+            if (!brick_empty(slot)) tl.mark(bidx, 1);
             // first coordinate outside this brick (or the grid) along each stepping direction
             const int32_t ex = stx > 0 ? min((bxi << 3) + 8, g.nx) : (stx < 0 ? (bxi << 3) - 1 : INT_MIN);
             const int32_t ey = sty > 0 ? min((byi << 3) + 8, g.ny) : (sty < 0 ? (byi << 3) - 1 : INT_MIN);
@@ -612,6 +642,7 @@ __device__ __forceinline__ HitRec trace_ray(const GridView& g, const float o[3],
         dda_skip(g, pos[0], pos[1], pos[2], d[0], d[1], d[2], r);
     if (r.tie) tl.tie();
     if (!r.hit) return miss_rec(0u, 0u);
+    tl.mark((uint32_t)(r.vx >> 3) + (uint32_t)g.bx * ((uint32_t)(r.vy >> 3) + (uint32_t)g.by * (uint32_t)(r.vz >> 3)), 2);
     return hit_record(g, o, d, r.vx, r.vy, r.vz, r.last, r.slot, kind == 1 ? entry_axis : -1,
                       t_entry);
 }

@@ -23,6 +23,7 @@ __global__ void __launch_bounds__(256) render_kernel(GridView g, vt_camera cam, 
     const uint32_t py = row0 + blockIdx.y * kTileH + (warp >> 1) * 4u + (lane >> 3);
     if (px >= cam.width || py >= row1) return;
     Tally<STATS> tl;
+    tl.bind(counters, g.bricks);
     float o[3], d[3];
     raygen(cam, px, py, 0.5f, 0.5f, o, d);
     const HitRec h = shade_ray<STATS>(g, light, o, d, tl);
@@ -38,6 +39,7 @@ __global__ void __launch_bounds__(256) trace_rays_kernel(GridView g,
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Tally<STATS> tl;
+    tl.bind(counters, g.bricks);
     // 24-byte rays: three 8-byte loads
     const float2 a = __ldg(rays + 3 * i), b = __ldg(rays + 3 * i + 1), c = __ldg(rays + 3 * i + 2);
     const float o[3] = {a.x, a.y, b.x}, d[3] = {b.y, c.x, c.y};
