@@ -225,13 +225,14 @@ def test_shapes1024_trace_rays_sample_with_t_accuracy(torch, shapes):
 
 
 def test_cave512_trace_rays_parity(torch):
-    w = workloads.cave512(rays=1 << 20)
+    """All 16,777,216 rays of the incoherent-batch workload, bit-exact against the oracle."""
+    w = workloads.cave512()
     g = vt.Grid.from_u8(w["voxels"], w["palette"])
     try:
         hits, d_rays, d_hits = device_trace(torch, g, w["rays"])
         og = po.Grid(w["voxels"], w["palette"])
         want, ostats = po.trace_rays(og, w["rays"], stats=True)
-        assert_hits_equal(hits, want, "cave512 1M rays")
+        assert_hits_equal(hits, want, "cave512 16M rays")
         gstats = vt.trace_rays_stats(g, d_rays, w["rays"].shape[0], d_hits)
         assert gstats == ostats
         assert_hits_equal(vt.trace_rays_host(g, w["rays"][:4096]), want[:4096], "host form")
@@ -475,3 +476,38 @@ def test_render_footprint_bounds(torch):
         assert fp["nonempty_bricks"] <= fp["bricks"] <= min(st["bricks_entered"], g.info()["bricks_total"])
     finally:
         g.destroy()
+
+
+def test_full_multiview_batch_sample_matches_oracle(torch):
+    """The batched multi-view workload at full size (8 scenes, 64 views), replayed from its graph;
+    the smallest views are checked record by record against the oracle (about a million samples)."""
+    scenes, views = workloads.multiview()
+    grids = [vt.Grid.from_u8(s["voxels"], s["palette"]) for s in scenes]
+    try:
+        outs, specs = [], []
+        for v in views:
+            c = v["camera"]
+            buf = torch.zeros(c.width * c.height * v["spp"] * 16, dtype=torch.uint8, device="cuda")
+            outs.append(buf)
+            specs.append(vt.make_view(grids[v["scene"]], c, buf, v["spp"], v["seed"],
+                                      v["view_id"], v["light"]))
+        b = vt.Batch(specs)
+        b.run(graph=True)
+        torch.cuda.synchronize()
+        order = sorted(range(len(views)), key=lambda i: views[i]["camera"].width * views[i]["camera"].height * views[i]["spp"])
+        checked, ogrids = 0, {}
+        for i in order:
+            v = views[i]
+            if checked > (1 << 20):
+                break
+            if v["scene"] not in ogrids:
+                ogrids[v["scene"]] = po.Grid(scenes[v["scene"]]["voxels"], scenes[v["scene"]]["palette"])
+            want = po.render_view(ogrids[v["scene"]], oracle_camera(v["camera"]), oracle_light(v["light"]),
+                                  v["spp"], v["seed"], v["view_id"])
+            assert_hits_equal(hits_from_dev(outs[i]), want, "multiview view %d" % v["view_id"])
+            checked += want.size
+        assert checked > (1 << 20)
+        b.destroy()
+    finally:
+        for gr in grids:
+            gr.destroy()
