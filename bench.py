@@ -53,6 +53,8 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=2.0,
                    help="wall-clock budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--views", type=int, default=64,
+                   help="views of the multiview configuration (fewer for small profiling runs)")
     return p.parse_args()
 
 
@@ -497,7 +499,7 @@ def run_config(args):
                     tuning=vt.get_tuning(vt.KERNEL_TRACE_RAYS), gpu_launches=args.steps)
         g.destroy()
     elif args.config == "multiview":
-        scenes, views = workloads.multiview()
+        scenes, views = workloads.multiview(n_views=args.views)
         grids = [vt.Grid.from_u8(sc["voxels"], sc["palette"]) for sc in scenes]
         bufs, specs = [], []
         for v in views:
@@ -514,7 +516,7 @@ def run_config(args):
         singles = [vt.Batch([sp]) for sp in specs]
         ms_single = autotune.time_ms(lambda: [x.run(stream) for x in singles], stream,
                                      repeats=max(1, args.steps // 2), warmup=1, flush=flush)
-        line.update(metric="Mrays/s (64 views over 8 scenes, 1-4 spp, one graph replay)",
+        line.update(metric="Mrays/s (%d views over 8 scenes, 1-4 spp, one graph replay)" % len(views),
                     value=rays / ms / 1e3, unit="Mrays/s", ms_per_step=ms,
                     config={"workload": "multiview", "views": len(views),
                             "primary_rays": batch.primary_rays, "shadow_rays": shadow},
