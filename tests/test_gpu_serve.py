@@ -44,7 +44,7 @@ def pinned(torch, cam):
 
 def test_results_same_alone_and_in_the_mix(torch):
     scenes, views = small_world()
-    svc = vt.Service()
+    svc = vt.Service(max_inflight=1)
     try:
         sids = [svc.add_scene(s["voxels"], s["palette"]) for s in scenes]
         alone = []
@@ -53,13 +53,18 @@ def test_results_same_alone_and_in_the_mix(torch):
             svc.wait(svc.submit(sids[v["scene"]], v["camera"], buf, v["spp"], v["seed"],
                                 v["view_id"], v["light"]))
             alone.append(buf.numpy().copy())
-        launches_alone = svc.stats()["launches"]
+        # a large request occupies the only slot while the others queue up behind it, so they
+        # are packed into shared launches whatever the timing
+        big = vt.camera_look_at((-40.0, 80.0, -40.0), (32.0, 16.0, 32.0), (0, 1, 0), 60.0, 1920, 1080)
+        blocker = svc.submit(sids[0], big, pinned(torch, big), 8)
         bufs = [pinned(torch, v["camera"]) for v in views]
         rids = [svc.submit(sids[v["scene"]], v["camera"], b, v["spp"], v["seed"], v["view_id"],
                            v["light"]) for v, b in zip(views, bufs)]
+        svc.wait(blocker)
+        launches_blocked = svc.stats()["launches"]
         timings = [svc.wait(r) for r in rids]
         st = svc.stats()
-        assert st["launches"] - launches_alone < len(views)  # requests shared launches
+        assert st["launches"] - launches_blocked < len(views)  # requests shared launches
         for a, b, v in zip(alone, bufs, views):
             np.testing.assert_array_equal(a, b.numpy(), err_msg="view %d" % v["view_id"])
         for i in (0, 4, 7, 11):

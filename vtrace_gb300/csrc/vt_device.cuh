@@ -517,6 +517,17 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
 __device__ __forceinline__ int slab_entry(const GridView& g, const float o[3], const float d[3],
                                           float pos[3], float& t_entry, int& axis) {
     const float size[3] = {__int2float_rn(g.nx), __int2float_rn(g.ny), __int2float_rn(g.nz)};
+    // an origin strictly inside the box has tn < 0 < tf on every axis: the slab test below would
+    // return "inside" with the origin as the entry point, so skip its six divisions
+    if (o[0] > 0.0f && o[0] < size[0] && o[1] > 0.0f && o[1] < size[1] && o[2] > 0.0f &&
+        o[2] < size[2]) {
+        pos[0] = o[0];
+        pos[1] = o[1];
+        pos[2] = o[2];
+        t_entry = 0.0f;
+        axis = -1;
+        return 2;
+    }
     float tn = -INFINITY, tf = INFINITY;
     int ax = -1;
 #pragma unroll
