@@ -553,7 +553,8 @@ def run_config(args):
                     e2e={"value": rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 96,
                          "d2h_bytes_per_step": cam.width * cam.height * 4,
                          "path": "vt_path_trace_host (C ABI), RGBA8 out"},
-                    gpu_launches=args.steps)
+                    # persistent path kernel + in-order sample resolve per frame
+                    gpu_launches=2 * args.steps)
         if not args.no_cpu_baseline:
             from oracle import pyoracle as po
             og = po.Grid(w["voxels"], w["palette"])
@@ -598,7 +599,9 @@ def run_config(args):
                     e2e={"value": 1e3 / ms, "unit": "chunks/s", "h2d_bytes_per_step": 4096,
                          "d2h_bytes_per_step": 8 * 2 * 8 + 8,
                          "path": "vt_grid_update (C ABI), synchronous, host wall clock"},
-                    frame_after_updates_ms=frame_ms, gpu_launches=9 * args.steps)
+                    frame_after_updates_ms=frame_ms,
+                    # merge, scatter, 3 distance, 3 octant, run and long-box kernels per chunk
+                    gpu_launches=10 * args.steps)
         g.destroy()
     elif args.config == "pager_world":
         # the reference-compatible frame (render_tick) over vtrace's own world shape
