@@ -147,3 +147,36 @@ def test_failures_are_reported_per_request(torch):
     th.join(timeout=60)
     assert not th.is_alive()
     assert got.get("code") == -7  # VT_ECANCELED
+
+
+def test_protocol_errors(torch):
+    """Requests are consumed by the poll that reports them; a poll with no wait on a running
+    request says "not ready"; bad arguments and unknown ids fail without disturbing the service."""
+    scenes, views = small_world(2)
+    svc = vt.Service(max_inflight=1)
+    service_id = svc.id
+    try:
+        sid = svc.add_scene(scenes[0]["voxels"], scenes[0]["palette"])
+        v = views[0]
+        with pytest.raises(vt.VtError) as e:
+            svc.submit(sid, v["camera"], None)  # no output buffer
+        assert e.value.code == -1
+        with pytest.raises(vt.VtError) as e:
+            svc.submit(sid, v["camera"], pinned(torch, v["camera"]), spp=0)
+        assert e.value.code == -1
+        with pytest.raises(vt.VtError) as e:
+            svc.poll(123456789)
+        assert e.value.code == -4  # VT_ENOTFOUND
+        big = vt.camera_look_at((-40.0, 80.0, -40.0), (32.0, 16.0, 32.0), (0, 1, 0), 60.0, 1920, 1080)
+        rid = svc.submit(sid, big, pinned(torch, big), 8)
+        quick = svc.submit(sid, v["camera"], pinned(torch, v["camera"]), 1)
+        assert svc.poll(quick, 0) is None  # queued behind the large request
+        assert svc.wait(rid)["samples"] == 1920 * 1080 * 8
+        assert svc.wait(quick)["samples"] == v["camera"].width * v["camera"].height
+        with pytest.raises(vt.VtError) as e:
+            svc.poll(rid)  # already reported
+        assert e.value.code == -4
+        assert svc.stats()["completed"] >= 2
+    finally:
+        svc.stop()
+    assert vt.lib().vt_serve_poll(service_id, 1, 0, None) == -4  # the stopped service is gone
