@@ -121,14 +121,15 @@ struct InstanceCursor {
     }
 };
 
-__global__ void __launch_bounds__(256) compat_kernel(const GridView* __restrict__ views,
+// Blocks of 128 threads cover 16 x 8 pixels, two per 16 x 16 binning tile.
+__global__ void __launch_bounds__(128) compat_kernel(const GridView* __restrict__ views,
                                                      const CompatInstance* __restrict__ inst,
                                                      int32_t ninst, const uint32_t* __restrict__ bins,
                                                      int32_t words, CompatFrame f,
                                                      uchar4* __restrict__ fb) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const int32_t px = (int32_t)(blockIdx.x * 16 + (warp & 1u) * 8u + (lane & 7u));
-    const int32_t py = (int32_t)(blockIdx.y * 16 + (warp >> 1) * 4u + (lane >> 3));
+    const int32_t py = (int32_t)(blockIdx.y * 8 + (warp >> 1) * 4u + (lane >> 3));
     if (px >= f.width || py >= f.height) return;
     const float inv_w = __fdiv_rn(2.0f, __int2float_rn(f.width));
     const float xn = __fsub_rn(__fmul_rn(__fadd_rn(__int2float_rn(px), 0.5f), inv_w), 1.0f);
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(256) compat_kernel(const GridView* __restrict_
     uint32_t cr = VT_SKY_RGBA & 0xFFu, cg = (VT_SKY_RGBA >> 8) & 0xFFu,
              cb = (VT_SKY_RGBA >> 16) & 0xFFu, ca = VT_SKY_RGBA >> 24;
     float depth = INFINITY;
-    InstanceCursor cur(bins, ninst, words, (int32_t)(blockIdx.y * gridDim.x + blockIdx.x));
+    InstanceCursor cur(bins, ninst, words, (int32_t)((blockIdx.y >> 1) * gridDim.x + blockIdx.x));
     for (int32_t i = cur.next(); i >= 0; i = cur.next()) {
         const CompatInstance& I = inst[i];
         const GridView g = views[I.texture];
@@ -620,7 +621,8 @@ int32_t render_tick(int32_t* window_width, int32_t* window_height, const render_
         compat_bin_kernel<<<bgrid, 256, 0, st>>>(c.d_inst, ninst, words, (int32_t)grid.x, ntiles,
                                                  bins);
     }
-    compat_kernel<<<grid, 256, 0, st>>>(c.d_views, c.d_inst, ninst, bins, words, f, c.fb);
+    const dim3 pgrid(grid.x, (c.height + 7) / 8);
+    compat_kernel<<<pgrid, 128, 0, st>>>(c.d_views, c.d_inst, ninst, bins, words, f, c.fb);
     if (cudaGetLastError() != cudaSuccess) return -1;
     // the host vectors above are staged by the copies: wait before they go out of scope
     if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
