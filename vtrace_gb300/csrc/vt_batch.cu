@@ -25,37 +25,44 @@
 
 namespace vt {
 
+// Lane state: kind 0 idle, 1 camera sample, 2 shadow ray of `prim`; pend 1 or 2 when that ray is
+// queued but not started (ray_begin, batch_finish and ray_unit each have one call site, so lanes
+// starting rays do so together).
 struct BatchLane {
     LaneRay R;
-    int kind;
-    uint32_t pix;
+    int kind, pend;
+    uint32_t pix;     // sample record index in the view's output
+    uint32_t px, py, sample;
     HitRec prim;
     float ndl;
+    float so[3];      // origin of the queued shadow ray
     uint32_t view;
 };
 
-__device__ __forceinline__ int batch_finish(const BatchView& V, BatchLane& s, int st) {
+constexpr int kRayQueued = 3;
+
+// A ray of the lane ended with `st`: write the sample record, or queue the shadow ray.
+__device__ __forceinline__ void batch_finish(const BatchView& V, BatchLane& s, int st) {
     if (s.kind == 1) {
         HitRec h = ray_record(V.g, s.R, st, VT_SKY_RGBA);
         float nd;
         if (st != kRayHit || !V.light.enabled || !face_lit(h, V.light, nd)) {
             V.out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
             s.kind = 0;
-            return kRayMiss;
+            return;
         }
         if (nd > 0.0f && V.light.shadows) {
-            float so[3];
-            shadow_origin(h, s.R.o, s.R.d, so);
+            shadow_origin(h, s.R.o, s.R.d, s.so);
             s.prim = h;
             s.ndl = nd;
             s.kind = 2;
-            const float ld[3] = {V.light.dx, V.light.dy, V.light.dz};
-            return ray_begin(V.g, so, ld, s.R);
+            s.pend = 2;
+            return;
         }
         h.w3 = shade_rgba(h.w3, nd, 1.0f, V.light.ambient);
         V.out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
         s.kind = 0;
-        return kRayMiss;
+        return;
     }
     const bool shadowed = st == kRayHit;
     HitRec h = s.prim;
@@ -63,10 +70,9 @@ __device__ __forceinline__ int batch_finish(const BatchView& V, BatchLane& s, in
     h.w1 |= (VT_HIT_FLAG_SHADOW_RAY | (shadowed ? VT_HIT_FLAG_SHADOWED : 0u)) << 24;
     V.out[s.pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
     s.kind = 0;
-    return kRayMiss;
 }
 
-__global__ void __launch_bounds__(256) batch_kernel(const BatchView* __restrict__ table,
+__global__ void __launch_bounds__(256, 4) batch_kernel(const BatchView* __restrict__ table,
                                                     uint32_t nviews, uint64_t total,
                                                     unsigned long long* __restrict__ counter,
                                                     uint32_t refill_min) {
@@ -82,9 +88,11 @@ __global__ void __launch_bounds__(256) batch_kernel(const BatchView* __restrict_
     const uint32_t lane = threadIdx.x & 31u;
     BatchLane s;
     s.kind = 0;
+    s.pend = 0;
     s.pix = 0;
     s.ndl = 0.0f;
     s.view = 0;
+    int st = kRayMiss;
     bool more = true;
     for (;;) {
         uint32_t idle = __ballot_sync(0xFFFFFFFFu, s.kind == 0);
@@ -111,24 +119,42 @@ __global__ void __launch_bounds__(256) batch_kernel(const BatchView* __restrict_
                 const uint32_t px = (uint32_t)(tile % V.tiles_x) * 8u + (l & 7u);
                 const uint32_t py = (uint32_t)(tile / V.tiles_x) * 4u + (l >> 3);
                 if (px < V.cam.width && py < V.cam.height) {
-                    float jx, jy, o[3], d[3];
-                    jitter(V.seed, V.view_id, px, py, sample, jx, jy);
-                    raygen(V.cam, px, py, jx, jy, o, d);
                     s.view = lo;
+                    s.px = px;
+                    s.py = py;
+                    s.sample = sample;
                     s.pix = ((py * V.cam.width) + px) * V.spp + sample;
                     s.kind = 1;
-                    int st = ray_begin(V.g, o, d, s.R);
-                    while (s.kind != 0 && st != kRayRunning) st = batch_finish(V, s, st);
+                    s.pend = 1;
+                    st = kRayQueued;
                 }
             }
             idle = __ballot_sync(0xFFFFFFFFu, s.kind == 0);
         }
         if (!more && idle == 0xFFFFFFFFu) break;
-        if (s.kind != 0) {
+        while (s.kind != 0 && st != kRayRunning) {
             const BatchView& V = views[s.view];
-            int st = ray_unit(V.g, s.R);
-            while (s.kind != 0 && st != kRayRunning) st = batch_finish(V, s, st);
+            if (s.pend != 0) {
+                float o[3], d[3];
+                if (s.pend == 1) {
+                    float jx, jy;
+                    jitter(V.seed, V.view_id, s.px, s.py, s.sample, jx, jy);
+                    raygen(V.cam, s.px, s.py, jx, jy, o, d);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) o[k] = s.so[k];
+                    d[0] = V.light.dx;
+                    d[1] = V.light.dy;
+                    d[2] = V.light.dz;
+                }
+                s.pend = 0;
+                st = ray_begin(V.g, o, d, s.R);
+            } else {
+                batch_finish(V, s, st);
+                st = kRayQueued;
+            }
         }
+        if (s.kind != 0) st = ray_unit(views[s.view].g, s.R);
     }
 }
 
