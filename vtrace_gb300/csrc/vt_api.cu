@@ -710,7 +710,8 @@ int32_t vt_render_host(int32_t grid, const vt_camera* camera, const vt_light* li
     const GridView v = g->view();
     const LightView L = light_view(light);
     cudaError_t e;
-    if (s.tune_render.persistent || s.tune_render.wavefront || H < 64) {
+    // bands only pay when the copy of one is long enough to hide behind the next one's traversal
+    if (s.tune_render.persistent || s.tune_render.wavefront || (uint64_t)W * H < (1u << 20)) {
         cudaStream_t st = s.stream;
         e = launch_frame(v, *camera, L, (uint4*)buf, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(hits, buf, hb, cudaMemcpyDeviceToHost, st);
