@@ -23,12 +23,14 @@ def oracle_params(p):
                                list(p.sun))
 
 
-@pytest.fixture(params=[(1, 32), (1, 4), (0, 32)], ids=["persistent", "refill4", "per_pixel"])
+@pytest.fixture(params=[(1, 32, 0), (1, 4, 0), (0, 32, 0), (1, 8, 1)],
+                ids=["persistent", "refill4", "per_pixel", "wavefront"])
 def form(request, torch):
     saved = vt.get_tuning(vt.KERNEL_PATH)
-    vt.set_tuning(vt.KERNEL_PATH, request.param[1], 0, bool(request.param[0]))
+    vt.set_tuning(vt.KERNEL_PATH, request.param[1], 0, bool(request.param[0]), bool(request.param[2]))
     yield request.param
-    vt.set_tuning(vt.KERNEL_PATH, saved["refill_min"], saved["blocks_per_sm"], saved["persistent"])
+    vt.set_tuning(vt.KERNEL_PATH, saved["refill_min"], saved["blocks_per_sm"], saved["persistent"],
+                  saved["wavefront"])
 
 
 @pytest.mark.parametrize("case", ["terrain", "shapes", "nosun", "deep"])

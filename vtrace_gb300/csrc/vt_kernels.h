@@ -31,7 +31,8 @@ cudaError_t launch_render_persistent(const GridView& g, const vt_camera& cam,
 cudaError_t launch_trace_rays_persistent(const GridView& g, const vt_ray* rays, uint64_t n,
                                          uint4* out, unsigned long long* counter,
                                          const TraceTuning& tune, int sm_count,
-                                         cudaStream_t stream);
+                                         cudaStream_t stream,
+                                         const unsigned int* n_dev = nullptr);
 
 cudaError_t launch_render(const GridView& g, const vt_camera& cam, const LightView& light,
                           uint4* out, Counters* counters, cudaStream_t stream, uint32_t row0 = 0,

@@ -450,6 +450,337 @@ static cudaError_t launch_path_persistent(const GridView& g, const vt_camera& ca
     return e != cudaSuccess ? e : f;
 }
 
+
+// ---------------------------------------------------------------------------------------------
+// Wavefront form: the paths of a chunk of samples advance one vertex at a time through ray
+// queues traced by the persistent ray-buffer kernel.  Per vertex: trace the path rays, shade
+// (sky on a miss; throughput, sun ray and bounce ray otherwise), trace the sun rays, add their
+// light, and bucket the bounce rays by direction octant and origin cell (8^3 cells of the grid)
+// so that the next pass hands each warp rays that start near one another and head the same way.
+// Every path's radiance sees the same operations in the same order as path_pixel; queue order
+// only changes speed.  Queue lengths stay on the device.
+// ---------------------------------------------------------------------------------------------
+
+struct WaveState {
+    float T[3], L[3], so[3];
+    uint32_t face;
+    uint32_t pad[2];
+};
+
+constexpr int32_t kWaveCells = 8;
+constexpr uint32_t kWaveBuckets = 8u * kWaveCells * kWaveCells * kWaveCells;  // 4096
+constexpr uint64_t kWaveChunkPaths = 16u << 20;
+
+// Appends the lanes with `want` to a queue: one atomic per warp; every lane of the warp calls it.
+__device__ __forceinline__ uint32_t wave_append(unsigned int* count, bool want) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, want);
+    if (!ballot) return 0;
+    const int leader = __ffs(ballot) - 1;
+    unsigned int base = 0;
+    if ((int)lane == leader) base = atomicAdd(count, (unsigned int)__popc(ballot));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return base + __popc(ballot & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void wave_path_pixel(uint32_t p, uint32_t sn, uint32_t s0, uint32_t w,
+                                                uint32_t& px, uint32_t& py, uint32_t& s) {
+    const uint32_t i = p / sn;
+    s = s0 + (p - i * sn);
+    px = i % w;
+    py = i / w;
+}
+
+__global__ void __launch_bounds__(256) wave_camera_kernel(vt_camera cam, PathParams P, uint32_t s0,
+                                                          uint32_t sn, uint32_t tiles_x,
+                                                          uint64_t total, vt_ray* __restrict__ q,
+                                                          uint32_t* __restrict__ qid,
+                                                          unsigned int* __restrict__ qn,
+                                                          WaveState* __restrict__ st) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool valid = false;
+    uint32_t px = 0, py = 0, smp = 0;
+    if (t < total) {  // t = (tile * sn + sample) * 32 + pixel of the 8 x 4 tile
+        const uint32_t l = (uint32_t)(t & 31u);
+        const uint64_t ts = t >> 5;
+        smp = (uint32_t)(ts % sn);
+        const uint64_t tile = ts / sn;
+        px = (uint32_t)(tile % tiles_x) * 8u + (l & 7u);
+        py = (uint32_t)(tile / tiles_x) * 4u + (l >> 3);
+        valid = px < cam.width && py < cam.height;
+    }
+    const uint32_t slot = wave_append(qn, valid);
+    if (!valid) return;
+    const uint32_t p = (py * cam.width + px) * sn + smp;
+    float jx, jy, o[3], d[3];
+    jitter(P.seed, 0u, px, py, s0 + smp, jx, jy);
+    raygen(cam, px, py, jx, jy, o, d);
+    q[slot] = vt_ray{{o[0], o[1], o[2]}, {d[0], d[1], d[2]}};
+    qid[slot] = p;
+    WaveState& S = st[p];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        S.T[c] = 1.0f;
+        S.L[c] = 0.0f;
+    }
+}
+
+// Vertex b of every queued path: its ray ended with record h.
+__global__ void __launch_bounds__(256) wave_shade_kernel(
+    GridView g, PathParams P, uint32_t b, uint32_t s0, uint32_t sn, uint32_t w,
+    const vt_ray* __restrict__ q, const uint32_t* __restrict__ qid,
+    const unsigned int* __restrict__ qn, const uint4* __restrict__ hits,
+    WaveState* __restrict__ st, float4* __restrict__ samples, vt_ray* __restrict__ sq,
+    uint32_t* __restrict__ sid, unsigned int* __restrict__ sqn, vt_ray* __restrict__ nq,
+    uint32_t* __restrict__ nqid, unsigned int* __restrict__ nqn,
+    unsigned long long* __restrict__ rays_out) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = *qn;
+    if (rays_out && j == 0) atomicAdd(rays_out, (unsigned long long)n);
+    bool sun = false, bounce = false;
+    uint32_t p = 0;
+    float so[3] = {0.0f, 0.0f, 0.0f}, nd[3] = {0.0f, 0.0f, 0.0f};
+    if (j < n) {
+        p = qid[j];
+        const uint4 hv = hits[j];
+        HitRec h;
+        h.w0 = hv.x;
+        h.w1 = hv.y;
+        h.w2 = hv.z;
+        h.w3 = hv.w;
+        WaveState& S = st[p];
+        const uint32_t flags = h.w1 >> 24;
+        const uint32_t face = flags & VT_FACE_MASK;
+        if (!(flags & VT_HIT_FLAG_HIT) || face == 0) {
+            if (!(flags & VT_HIT_FLAG_HIT)) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) S.L[c] = __fadd_rn(S.L[c], __fmul_rn(S.T[c], P.sky[c]));
+            }
+            samples[p] = make_float4(S.L[0], S.L[1], S.L[2], 0.0f);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                S.T[c] = __fmul_rn(S.T[c], __fdiv_rn(__uint2float_rn((h.w3 >> (8 * c)) & 0xFFu), 255.0f));
+            const vt_ray r = q[j];
+            shadow_origin(h, r.origin, r.dir, so);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) S.so[c] = so[c];
+            S.face = face;
+            const int a = (int)(face - 1) / 2;
+            const bool npos = (face & 1u) != 0u;
+            if (P.sun_on) {
+                const float la = a == 0 ? P.sun_dir[0] : (a == 1 ? P.sun_dir[1] : P.sun_dir[2]);
+                sun = (npos ? la : -la) > 0.0f;
+            }
+            if (b < P.max_bounces) {
+                bounce = true;
+                uint32_t px, py, s;
+                wave_path_pixel(p, sn, s0, w, px, py, s);
+                float n3[3] = {0.0f, 0.0f, 0.0f}, u[3];
+                n3[a] = npos ? 1.0f : -1.0f;
+                if (sphere_sample(P.seed, px, py, s, b, u)) {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) nd[k] = __fadd_rn(n3[k], u[k]);
+                    const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nd[0], nd[0]),
+                                                                   __fmul_rn(nd[1], nd[1])),
+                                                         __fmul_rn(nd[2], nd[2])));
+                    if (l > 1e-6f) {
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) nd[k] = __fdiv_rn(nd[k], l);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) nd[k] = n3[k];
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) nd[k] = n3[k];
+                }
+            } else if (!sun) {
+                samples[p] = make_float4(S.L[0], S.L[1], S.L[2], 0.0f);  // the path ends here
+            }
+        }
+    }
+    const uint32_t ks = wave_append(sqn, sun);
+    if (sun) {
+        sq[ks] = vt_ray{{so[0], so[1], so[2]}, {P.sun_dir[0], P.sun_dir[1], P.sun_dir[2]}};
+        sid[ks] = p;
+    }
+    const uint32_t kb = wave_append(nqn, bounce);
+    if (bounce) {
+        nq[kb] = vt_ray{{so[0], so[1], so[2]}, {nd[0], nd[1], nd[2]}};
+        nqid[kb] = p;
+    }
+}
+
+// The sun rays of vertex b: light of the unblocked ones; paths ending at this vertex are done.
+__global__ void __launch_bounds__(256) wave_sun_kernel(PathParams P, bool last,
+                                                       const uint32_t* __restrict__ sid,
+                                                       const unsigned int* __restrict__ sqn,
+                                                       const uint4* __restrict__ hits,
+                                                       WaveState* __restrict__ st,
+                                                       float4* __restrict__ samples,
+                                                       unsigned long long* __restrict__ rays_out) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = *sqn;
+    if (rays_out && j == 0) atomicAdd(rays_out, (unsigned long long)n);
+    if (j >= n) return;
+    const uint32_t p = sid[j];
+    WaveState& S = st[p];
+    if (!((hits[j].y >> 24) & VT_HIT_FLAG_HIT)) {
+        const int a = (int)(S.face - 1) / 2;
+        const bool npos = (S.face & 1u) != 0u;
+        const float la = a == 0 ? P.sun_dir[0] : (a == 1 ? P.sun_dir[1] : P.sun_dir[2]);
+        const float ndl = npos ? la : -la;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) S.L[c] = __fadd_rn(S.L[c], __fmul_rn(__fmul_rn(S.T[c], P.sun[c]), ndl));
+    }
+    if (last) samples[p] = make_float4(S.L[0], S.L[1], S.L[2], 0.0f);
+}
+
+__device__ __forceinline__ uint32_t wave_key(const GridView& g, const vt_ray& r) {
+    const uint32_t o = (r.dir[0] < 0.0f ? 1u : 0u) | (r.dir[1] < 0.0f ? 2u : 0u) | (r.dir[2] < 0.0f ? 4u : 0u);
+    int32_t c[3];
+    const int32_t n[3] = {g.nx, g.ny, g.nz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float x = r.origin[a] * ((float)kWaveCells / (float)n[a]);  // approximate bin: order only
+        c[a] = x < 0.0f ? 0 : (x >= (float)kWaveCells ? kWaveCells - 1 : (int32_t)x);
+    }
+    return (o * kWaveCells + (uint32_t)c[2]) * kWaveCells * kWaveCells + (uint32_t)c[1] * kWaveCells + (uint32_t)c[0];
+}
+
+__global__ void __launch_bounds__(256) wave_hist_kernel(GridView g, const vt_ray* __restrict__ nq,
+                                                        const unsigned int* __restrict__ nqn,
+                                                        unsigned int* __restrict__ hist) {
+    __shared__ unsigned int h[kWaveBuckets];
+    for (uint32_t i = threadIdx.x; i < kWaveBuckets; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const uint32_t n = *nqn;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        atomicAdd(&h[wave_key(g, nq[j])], 1u);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kWaveBuckets; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+// Exclusive scan of the 4096 bucket counts (one block of 1024 threads, 4 buckets each) into the
+// scatter cursors; the next queue's length is the previous bounce queue's.
+__global__ void __launch_bounds__(1024) wave_scan_kernel(const unsigned int* __restrict__ hist,
+                                                         unsigned int* __restrict__ cursor,
+                                                         const unsigned int* __restrict__ nqn,
+                                                         unsigned int* __restrict__ qn) {
+    __shared__ unsigned int part[1024];
+    const uint32_t t = threadIdx.x;
+    unsigned int v[4], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        v[k] = hist[4 * t + k];
+        sum += v[k];
+    }
+    part[t] = sum;
+    __syncthreads();
+    for (uint32_t off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
+        const unsigned int x = t >= off ? part[t - off] : 0u;
+        __syncthreads();
+        part[t] += x;
+        __syncthreads();
+    }
+    unsigned int run = part[t] - sum;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        cursor[4 * t + k] = run;
+        run += v[k];
+    }
+    if (t == 0) *qn = *nqn;
+}
+
+__global__ void __launch_bounds__(256) wave_scatter_kernel(GridView g, const vt_ray* __restrict__ nq,
+                                                           const uint32_t* __restrict__ nqid,
+                                                           const unsigned int* __restrict__ nqn,
+                                                           unsigned int* __restrict__ cursor,
+                                                           vt_ray* __restrict__ q,
+                                                           uint32_t* __restrict__ qid) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *nqn) return;
+    const vt_ray r = nq[j];
+    const uint32_t k = atomicAdd(&cursor[wave_key(g, r)], 1u);
+    q[k] = r;
+    qid[k] = nqid[j];
+}
+
+static cudaError_t launch_path_wave(const GridView& g, const vt_camera& cam, const PathParams& P,
+                                    void* out, unsigned long long* rays, int sm_count,
+                                    cudaStream_t st) {
+    const State& S = state();
+    const uint32_t npx = cam.width * cam.height;
+    const uint32_t tiles_x = (cam.width + 7) / 8, tiles_y = (cam.height + 3) / 4;
+    const uint32_t sn = (uint32_t)std::max<uint64_t>(
+        1, std::min<uint64_t>(std::min(P.spp, kPathChunkSpp), kWaveChunkPaths / npx));
+    const uint64_t cap = (uint64_t)npx * sn;
+    auto al = [](uint64_t v) { return (v + 255) / 256 * 256; };
+    // q, nq, sq (rays); qid, nqid, sid; hits; state; samples; sums; counts; hist; cursor
+    const uint64_t o_q = 0, o_nq = al(cap * 24), o_sq = o_nq + al(cap * 24), o_qid = o_sq + al(cap * 24);
+    const uint64_t o_nqid = o_qid + al(cap * 4), o_sid = o_nqid + al(cap * 4), o_hit = o_sid + al(cap * 4);
+    const uint64_t o_st = o_hit + al(cap * 16), o_smp = o_st + al(cap * sizeof(WaveState));
+    const uint64_t o_sum = o_smp + al(cap * 16), o_cnt = o_sum + al((uint64_t)npx * 16);
+    const uint64_t o_hist = o_cnt + 256, o_cur = o_hist + al(kWaveBuckets * 4);
+    const uint64_t total_bytes = o_cur + al(kWaveBuckets * 4);
+    char* buf = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&buf, total_bytes, st);
+    if (e != cudaSuccess) return e;
+    vt_ray* q = (vt_ray*)(buf + o_q);
+    vt_ray* nq = (vt_ray*)(buf + o_nq);
+    vt_ray* sq = (vt_ray*)(buf + o_sq);
+    uint32_t* qid = (uint32_t*)(buf + o_qid);
+    uint32_t* nqid = (uint32_t*)(buf + o_nqid);
+    uint32_t* sid = (uint32_t*)(buf + o_sid);
+    uint4* hits = (uint4*)(buf + o_hit);
+    WaveState* wst = (WaveState*)(buf + o_st);
+    float4* samples = (float4*)(buf + o_smp);
+    float4* sums = (float4*)(buf + o_sum);
+    unsigned int* cnt = (unsigned int*)(buf + o_cnt);  // qn, sqn, nqn
+    unsigned int* hist = (unsigned int*)(buf + o_hist);
+    unsigned int* cursor = (unsigned int*)(buf + o_cur);
+    const unsigned blocks = (unsigned)((cap + 255) / 256);
+    for (uint32_t s0 = 0; s0 < P.spp && e == cudaSuccess; s0 += sn) {
+        const uint32_t n = std::min(sn, P.spp - s0);
+        const uint64_t items = (uint64_t)tiles_x * tiles_y * n * 32;
+        e = cudaMemsetAsync(cnt, 0, 16, st);
+        if (e != cudaSuccess) break;
+        wave_camera_kernel<<<(unsigned)((items + 255) / 256), 256, 0, st>>>(cam, P, s0, n, tiles_x,
+                                                                           items, q, qid, cnt, wst);
+        for (uint32_t b = 0; b <= P.max_bounces && e == cudaSuccess; ++b) {
+            e = launch_trace_rays_persistent(g, q, cap, hits, next_counter(), S.tune_rays, sm_count,
+                                             st, cnt);
+            if (e == cudaSuccess) e = cudaMemsetAsync(cnt + 1, 0, 8, st);
+            if (e != cudaSuccess) break;
+            wave_shade_kernel<<<blocks, 256, 0, st>>>(g, P, b, s0, n, cam.width, q, qid, cnt, hits,
+                                                      wst, samples, sq, sid, cnt + 1, nq, nqid,
+                                                      cnt + 2, rays);
+            e = launch_trace_rays_persistent(g, sq, cap, hits, next_counter(), S.tune_rays,
+                                             sm_count, st, cnt + 1);
+            if (e != cudaSuccess) break;
+            wave_sun_kernel<<<blocks, 256, 0, st>>>(P, b >= P.max_bounces, sid, cnt + 1, hits, wst,
+                                                    samples, rays);
+            if (b < P.max_bounces) {
+                e = cudaMemsetAsync(hist, 0, kWaveBuckets * 4, st);
+                if (e != cudaSuccess) break;
+                wave_hist_kernel<<<(unsigned)(sm_count * 4), 256, 0, st>>>(g, nq, cnt + 2, hist);
+                wave_scan_kernel<<<1, 1024, 0, st>>>(hist, cursor, cnt + 2, cnt);
+                wave_scatter_kernel<<<blocks, 256, 0, st>>>(g, nq, nqid, cnt + 2, cursor, q, qid);
+            }
+            e = cudaGetLastError();
+        }
+        if (e != cudaSuccess) break;
+        path_resolve_kernel<<<(npx + 255) / 256, 256, 0, st>>>(samples, sums, npx, n, s0 == 0,
+                                                               s0 + n >= P.spp, P.spp,
+                                                               P.out_format, out);
+        e = cudaGetLastError();
+    }
+    const cudaError_t f = cudaFreeAsync(buf, st);
+    return e != cudaSuccess ? e : f;
+}
+
 static int32_t path_params(const vt_path_params* in, PathParams& P) {
     if (!in) return fail(VT_EINVAL, "vt_path_trace: null params");
     if (in->spp < 1 || in->spp > 65536) return fail(VT_EINVAL, "vt_path_trace: spp must be 1..65536");
@@ -475,6 +806,7 @@ static int32_t path_params(const vt_path_params* in, PathParams& P) {
 static cudaError_t launch_path(const GridView& g, const vt_camera& cam, const PathParams& P,
                                void* out, unsigned long long* rays, cudaStream_t st) {
     State& S = state();
+    if (S.tune_path.wavefront) return launch_path_wave(g, cam, P, out, rays, S.sm_count, st);
     if (S.tune_path.persistent)
         return launch_path_persistent(g, cam, P, out, rays, S.tune_path, S.sm_count, st);
     const dim3 grid((cam.width + 15) / 16, (cam.height + 15) / 16);

@@ -200,9 +200,13 @@ __global__ void __launch_bounds__(256) render_persistent_kernel(
     }
 }
 
+// n_dev: nullptr, or the device-side ray count (at most n), read at the start (ray queues whose
+// length the host does not know).
 __global__ void __launch_bounds__(256) trace_rays_persistent_kernel(
     GridView g, const float2* __restrict__ rays, uint64_t n, uint4* __restrict__ out,
-    unsigned long long* __restrict__ counter, uint32_t refill_min) {
+    unsigned long long* __restrict__ counter, uint32_t refill_min,
+    const unsigned int* __restrict__ n_dev) {
+    if (n_dev) n = min((uint64_t)*n_dev, n);
     const uint32_t lane = threadIdx.x & 31u;
     LaneRay R;
     bool busy = false;
@@ -270,7 +274,7 @@ cudaError_t launch_render_persistent(const GridView& g, const vt_camera& cam,
 cudaError_t launch_trace_rays_persistent(const GridView& g, const vt_ray* rays, uint64_t n,
                                          uint4* out, unsigned long long* counter,
                                          const TraceTuning& tune, int sm_count,
-                                         cudaStream_t stream) {
+                                         cudaStream_t stream, const unsigned int* n_dev) {
     if (n == 0) return cudaSuccess;
     static int per_sm = resident_blocks((const void*)trace_rays_persistent_kernel);
     const int bps = tune.blocks_per_sm > 0 ? min(tune.blocks_per_sm, per_sm) : per_sm;
@@ -279,7 +283,7 @@ cudaError_t launch_trace_rays_persistent(const GridView& g, const vt_ray* rays, 
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     trace_rays_persistent_kernel<<<blocks, 256, 0, stream>>>(
-        g, reinterpret_cast<const float2*>(rays), n, out, counter, tune.refill_min);
+        g, reinterpret_cast<const float2*>(rays), n, out, counter, tune.refill_min, n_dev);
     return cudaGetLastError();
 }
 
