@@ -58,6 +58,22 @@ def parse_args():
     return p.parse_args()
 
 
+def path_launches(tuning, spp, bounces, pixels):
+    """Kernels one vt_path_trace launches under `tuning`, per frame.
+
+    Wavefront form, per chunk of samples (up to 16 spp, 16M paths): the vertex-0 kernel, then
+    per later vertex the path-ray trace, the shading, the sun-ray trace and the sun light, then
+    the resolve.  Persistent form: the path kernel and the resolve
+    per chunk (up to 16 spp, 64M samples).  Per-pixel form: one kernel."""
+    if tuning["wavefront"]:
+        sn = max(1, min(spp, 16, (16 << 20) // pixels))
+        return -(-spp // sn) * (2 + 4 * bounces)
+    if tuning["persistent"]:
+        sn = max(1, min(spp, 16, (64 << 20) // pixels))
+        return -(-spp // sn) * 2
+    return 1
+
+
 def max_over_ranks(x, device):
     """The largest of every rank's `x` (all ranks call it; one all-reduce)."""
     import torch
@@ -553,8 +569,8 @@ def run_config(args):
                     e2e={"value": rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 96,
                          "d2h_bytes_per_step": cam.width * cam.height * 4,
                          "path": "vt_path_trace_host (C ABI), RGBA8 out"},
-                    # persistent path kernel + in-order sample resolve per frame
-                    gpu_launches=2 * args.steps)
+                    gpu_launches=path_launches(vt.get_tuning(vt.KERNEL_PATH), 2, 3,
+                                               cam.width * cam.height) * args.steps)
         if not args.no_cpu_baseline:
             from oracle import pyoracle as po
             og = po.Grid(w["voxels"], w["palette"])

@@ -165,13 +165,16 @@ typedef struct vt_tuning {
     int32_t blocks_per_sm;
     uint32_t persistent;
     uint32_t wavefront; /* VT_KERNEL_RENDER tile launches: trace shadow rays in a second pass over
-                           a compacted queue instead of in the primary ray's thread */
+                           a compacted queue instead of in the primary ray's thread.
+                           VT_KERNEL_PATH: advance all paths one vertex at a time through ray
+                           queues (the default; faster than either per-path form) */
 } vt_tuning;
 
 #define VT_KERNEL_RENDER 1
 #define VT_KERNEL_TRACE_RAYS 2
 #define VT_KERNEL_BATCH 3
-#define VT_KERNEL_PATH 4 /* vt_path_trace: persistent = paths refilled per lane, else a thread per pixel */
+#define VT_KERNEL_PATH 4 /* vt_path_trace: wavefront = ray queues per path vertex; else
+                            persistent = paths refilled per lane, else a thread per pixel */
 
 int32_t vt_get_tuning(int32_t kernel, vt_tuning* out);
 int32_t vt_set_tuning(int32_t kernel, const vt_tuning* in);

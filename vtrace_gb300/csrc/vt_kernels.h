@@ -37,8 +37,10 @@ cudaError_t launch_trace_rays_persistent(const GridView& g, const vt_ray* rays, 
 cudaError_t launch_render(const GridView& g, const vt_camera& cam, const LightView& light,
                           uint4* out, Counters* counters, cudaStream_t stream, uint32_t row0 = 0,
                           uint32_t row1 = 0);
+// n_dev as for launch_trace_rays_persistent: the device-side ray count (at most n), or nullptr.
 cudaError_t launch_trace_rays(const GridView& g, const vt_ray* rays, uint64_t n, uint4* out,
-                              Counters* counters, cudaStream_t stream);
+                              Counters* counters, cudaStream_t stream,
+                              const unsigned int* n_dev = nullptr);
 
 // Scratch of one brick build, sized for `bricks` bricks.
 struct BuildScratch {

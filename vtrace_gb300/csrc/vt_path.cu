@@ -453,12 +453,14 @@ static cudaError_t launch_path_persistent(const GridView& g, const vt_camera& ca
 
 // ---------------------------------------------------------------------------------------------
 // Wavefront form: the paths of a chunk of samples advance one vertex at a time through ray
-// queues traced by the persistent ray-buffer kernel.  Per vertex: trace the path rays, shade
-// (sky on a miss; throughput, sun ray and bounce ray otherwise), trace the sun rays, add their
-// light, and bucket the bounce rays by direction octant and origin cell (8^3 cells of the grid)
-// so that the next pass hands each warp rays that start near one another and head the same way.
-// Every path's radiance sees the same operations in the same order as path_pixel; queue order
-// only changes speed.  Queue lengths stay on the device.
+// queues.  Vertex 0 (camera ray, shading, sun ray) runs a thread per path in 8 x 4 pixel tiles;
+// per vertex after that: trace the path rays, shade (sky on a miss; throughput, sun ray and
+// bounce ray otherwise), trace the sun rays and add their light, the two ray queues traced by the
+// persistent ray-buffer kernel.  Queues keep append order, which follows the pixel tiles:
+// neighbouring entries start at neighbouring surface points (bucketing the bounce rays by
+// direction octant and origin cell measured 9% slower in all).  Every path's radiance sees the
+// same operations in the same order as path_pixel; queue order only changes speed.  Queue
+// lengths stay on the device.
 // ---------------------------------------------------------------------------------------------
 
 struct WaveState {
@@ -467,9 +469,8 @@ struct WaveState {
     uint32_t pad[2];
 };
 
-constexpr int32_t kWaveCells = 8;
-constexpr uint32_t kWaveBuckets = 8u * kWaveCells * kWaveCells * kWaveCells;  // 4096
 constexpr uint64_t kWaveChunkPaths = 16u << 20;
+constexpr uint32_t kWaveCounters = 256;  // 2 x 128 queue lengths: max_bounces <= 64
 
 // Appends the lanes with `want` to a queue: one atomic per warp; every lane of the warp calls it.
 __device__ __forceinline__ uint32_t wave_append(unsigned int* count, bool want) {
@@ -491,12 +492,42 @@ __device__ __forceinline__ void wave_path_pixel(uint32_t p, uint32_t sn, uint32_
     py = i / w;
 }
 
-__global__ void __launch_bounds__(256) wave_camera_kernel(vt_camera cam, PathParams P, uint32_t s0,
-                                                          uint32_t sn, uint32_t tiles_x,
-                                                          uint64_t total, vt_ray* __restrict__ q,
-                                                          uint32_t* __restrict__ qid,
-                                                          unsigned int* __restrict__ qn,
-                                                          WaveState* __restrict__ st) {
+// Direction of the bounce at vertex b of sample s of pixel (px, py), off the face with axis `a`
+// and sign `npos`: the normalised sum of the normal and a unit vector uniform on the sphere (the
+// normal itself when the sphere sample is rejected or the sum degenerates).  Same operations as
+// path_pixel.
+__device__ __forceinline__ void bounce_dir(const PathParams& P, uint32_t px, uint32_t py,
+                                           uint32_t s, uint32_t b, int a, bool npos, float nd[3]) {
+    float n3[3] = {0.0f, 0.0f, 0.0f}, u[3];
+    n3[a] = npos ? 1.0f : -1.0f;
+    if (sphere_sample(P.seed, px, py, s, b, u)) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) nd[k] = __fadd_rn(n3[k], u[k]);
+        const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nd[0], nd[0]),
+                                                       __fmul_rn(nd[1], nd[1])),
+                                             __fmul_rn(nd[2], nd[2])));
+        if (l > 1e-6f) {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) nd[k] = __fdiv_rn(nd[k], l);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) nd[k] = n3[k];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) nd[k] = n3[k];
+    }
+}
+
+// Vertex 0 of the chunk's paths, one thread per path in 8 x 4 pixel tiles (the render kernel's
+// launch shape: the rays of a warp start together and stay coherent): camera ray, traversal,
+// shading, the sun ray traced in the same thread (as the render kernel traces its shadow rays),
+// and the bounce ray appended to the queue of vertex 1.
+__global__ void __launch_bounds__(128) wave_primary_kernel(
+    GridView g, vt_camera cam, PathParams P, uint32_t s0, uint32_t sn, uint32_t tiles_x,
+    uint64_t total, vt_ray* __restrict__ nq, uint32_t* __restrict__ nqid,
+    unsigned int* __restrict__ nqn, WaveState* __restrict__ st, float4* __restrict__ samples,
+    unsigned long long* __restrict__ rays_out) {
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool valid = false;
     uint32_t px = 0, py = 0, smp = 0;
@@ -509,19 +540,67 @@ __global__ void __launch_bounds__(256) wave_camera_kernel(vt_camera cam, PathPar
         py = (uint32_t)(tile / tiles_x) * 4u + (l >> 3);
         valid = px < cam.width && py < cam.height;
     }
-    const uint32_t slot = wave_append(qn, valid);
-    if (!valid) return;
-    const uint32_t p = (py * cam.width + px) * sn + smp;
-    float jx, jy, o[3], d[3];
-    jitter(P.seed, 0u, px, py, s0 + smp, jx, jy);
-    raygen(cam, px, py, jx, jy, o, d);
-    q[slot] = vt_ray{{o[0], o[1], o[2]}, {d[0], d[1], d[2]}};
-    qid[slot] = p;
-    WaveState& S = st[p];
+    bool bounce = false;
+    uint32_t p = 0, nrays = 0;
+    float so[3] = {0.0f, 0.0f, 0.0f}, nd[3] = {0.0f, 0.0f, 0.0f};
+    if (valid) {
+        p = (py * cam.width + px) * sn + smp;
+        float jx, jy, o[3], d[3];
+        jitter(P.seed, 0u, px, py, s0 + smp, jx, jy);
+        raygen(cam, px, py, jx, jy, o, d);
+        Tally<false> tl;
+        const HitRec h = trace_ray<false>(g, o, d, tl);
+        nrays = 1;
+        float T[3] = {1.0f, 1.0f, 1.0f}, L[3] = {0.0f, 0.0f, 0.0f};
+        const uint32_t flags = h.w1 >> 24;
+        const uint32_t face = flags & VT_FACE_MASK;
+        if (!(flags & VT_HIT_FLAG_HIT)) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        S.T[c] = 1.0f;
-        S.L[c] = 0.0f;
+            for (int c = 0; c < 3; ++c) L[c] = __fadd_rn(L[c], __fmul_rn(T[c], P.sky[c]));
+        } else if (face != 0) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                T[c] = __fmul_rn(T[c], __fdiv_rn(__uint2float_rn((h.w3 >> (8 * c)) & 0xFFu), 255.0f));
+            shadow_origin(h, o, d, so);
+            const int a = (int)(face - 1) / 2;
+            const bool npos = (face & 1u) != 0u;
+            if (P.sun_on) {
+                const float la = a == 0 ? P.sun_dir[0] : (a == 1 ? P.sun_dir[1] : P.sun_dir[2]);
+                const float ndl = npos ? la : -la;
+                if (ndl > 0.0f) {
+                    const HitRec sh = trace_ray<false>(g, so, P.sun_dir, tl);
+                    ++nrays;
+                    if (!((sh.w1 >> 24) & VT_HIT_FLAG_HIT)) {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c)
+                            L[c] = __fadd_rn(L[c], __fmul_rn(__fmul_rn(T[c], P.sun[c]), ndl));
+                    }
+                }
+            }
+            if (P.max_bounces > 0) {
+                bounce = true;
+                bounce_dir(P, px, py, s0 + smp, 0u, a, npos, nd);
+            }
+        }
+        if (bounce) {
+            WaveState& S = st[p];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                S.T[c] = T[c];
+                S.L[c] = L[c];
+            }
+        } else {
+            samples[p] = make_float4(L[0], L[1], L[2], 0.0f);
+        }
+    }
+    const uint32_t kb = wave_append(nqn, bounce);
+    if (bounce) {
+        nq[kb] = vt_ray{{so[0], so[1], so[2]}, {nd[0], nd[1], nd[2]}};
+        nqid[kb] = p;
+    }
+    if (rays_out) {
+        const uint32_t wr = __reduce_add_sync(0xFFFFFFFFu, nrays);
+        if ((threadIdx.x & 31u) == 0 && wr) atomicAdd(rays_out, (unsigned long long)wr);
     }
 }
 
@@ -576,25 +655,7 @@ __global__ void __launch_bounds__(256) wave_shade_kernel(
                 bounce = true;
                 uint32_t px, py, s;
                 wave_path_pixel(p, sn, s0, w, px, py, s);
-                float n3[3] = {0.0f, 0.0f, 0.0f}, u[3];
-                n3[a] = npos ? 1.0f : -1.0f;
-                if (sphere_sample(P.seed, px, py, s, b, u)) {
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) nd[k] = __fadd_rn(n3[k], u[k]);
-                    const float l = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nd[0], nd[0]),
-                                                                   __fmul_rn(nd[1], nd[1])),
-                                                         __fmul_rn(nd[2], nd[2])));
-                    if (l > 1e-6f) {
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) nd[k] = __fdiv_rn(nd[k], l);
-                    } else {
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) nd[k] = n3[k];
-                    }
-                } else {
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) nd[k] = n3[k];
-                }
+                bounce_dir(P, px, py, s, b, a, npos, nd);
             } else if (!sun) {
                 samples[p] = make_float4(S.L[0], S.L[1], S.L[2], 0.0f);  // the path ends here
             }
@@ -637,77 +698,6 @@ __global__ void __launch_bounds__(256) wave_sun_kernel(PathParams P, bool last,
     if (last) samples[p] = make_float4(S.L[0], S.L[1], S.L[2], 0.0f);
 }
 
-__device__ __forceinline__ uint32_t wave_key(const GridView& g, const vt_ray& r) {
-    const uint32_t o = (r.dir[0] < 0.0f ? 1u : 0u) | (r.dir[1] < 0.0f ? 2u : 0u) | (r.dir[2] < 0.0f ? 4u : 0u);
-    int32_t c[3];
-    const int32_t n[3] = {g.nx, g.ny, g.nz};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float x = r.origin[a] * ((float)kWaveCells / (float)n[a]);  // approximate bin: order only
-        c[a] = x < 0.0f ? 0 : (x >= (float)kWaveCells ? kWaveCells - 1 : (int32_t)x);
-    }
-    return (o * kWaveCells + (uint32_t)c[2]) * kWaveCells * kWaveCells + (uint32_t)c[1] * kWaveCells + (uint32_t)c[0];
-}
-
-__global__ void __launch_bounds__(256) wave_hist_kernel(GridView g, const vt_ray* __restrict__ nq,
-                                                        const unsigned int* __restrict__ nqn,
-                                                        unsigned int* __restrict__ hist) {
-    __shared__ unsigned int h[kWaveBuckets];
-    for (uint32_t i = threadIdx.x; i < kWaveBuckets; i += blockDim.x) h[i] = 0;
-    __syncthreads();
-    const uint32_t n = *nqn;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        atomicAdd(&h[wave_key(g, nq[j])], 1u);
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < kWaveBuckets; i += blockDim.x)
-        if (h[i]) atomicAdd(&hist[i], h[i]);
-}
-
-// Exclusive scan of the 4096 bucket counts (one block of 1024 threads, 4 buckets each) into the
-// scatter cursors; the next queue's length is the previous bounce queue's.
-__global__ void __launch_bounds__(1024) wave_scan_kernel(const unsigned int* __restrict__ hist,
-                                                         unsigned int* __restrict__ cursor,
-                                                         const unsigned int* __restrict__ nqn,
-                                                         unsigned int* __restrict__ qn) {
-    __shared__ unsigned int part[1024];
-    const uint32_t t = threadIdx.x;
-    unsigned int v[4], sum = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        v[k] = hist[4 * t + k];
-        sum += v[k];
-    }
-    part[t] = sum;
-    __syncthreads();
-    for (uint32_t off = 1; off < 1024; off <<= 1) {  // inclusive Hillis-Steele scan
-        const unsigned int x = t >= off ? part[t - off] : 0u;
-        __syncthreads();
-        part[t] += x;
-        __syncthreads();
-    }
-    unsigned int run = part[t] - sum;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        cursor[4 * t + k] = run;
-        run += v[k];
-    }
-    if (t == 0) *qn = *nqn;
-}
-
-__global__ void __launch_bounds__(256) wave_scatter_kernel(GridView g, const vt_ray* __restrict__ nq,
-                                                           const uint32_t* __restrict__ nqid,
-                                                           const unsigned int* __restrict__ nqn,
-                                                           unsigned int* __restrict__ cursor,
-                                                           vt_ray* __restrict__ q,
-                                                           uint32_t* __restrict__ qid) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= *nqn) return;
-    const vt_ray r = nq[j];
-    const uint32_t k = atomicAdd(&cursor[wave_key(g, r)], 1u);
-    q[k] = r;
-    qid[k] = nqid[j];
-}
-
 static cudaError_t launch_path_wave(const GridView& g, const vt_camera& cam, const PathParams& P,
                                     void* out, unsigned long long* rays, int sm_count,
                                     cudaStream_t st) {
@@ -718,13 +708,12 @@ static cudaError_t launch_path_wave(const GridView& g, const vt_camera& cam, con
         1, std::min<uint64_t>(std::min(P.spp, kPathChunkSpp), kWaveChunkPaths / npx));
     const uint64_t cap = (uint64_t)npx * sn;
     auto al = [](uint64_t v) { return (v + 255) / 256 * 256; };
-    // q, nq, sq (rays); qid, nqid, sid; hits; state; samples; sums; counts; hist; cursor
+    // q, nq, sq (rays); qid, nqid, sid; hits; state; samples; sums; counts
     const uint64_t o_q = 0, o_nq = al(cap * 24), o_sq = o_nq + al(cap * 24), o_qid = o_sq + al(cap * 24);
     const uint64_t o_nqid = o_qid + al(cap * 4), o_sid = o_nqid + al(cap * 4), o_hit = o_sid + al(cap * 4);
     const uint64_t o_st = o_hit + al(cap * 16), o_smp = o_st + al(cap * sizeof(WaveState));
     const uint64_t o_sum = o_smp + al(cap * 16), o_cnt = o_sum + al((uint64_t)npx * 16);
-    const uint64_t o_hist = o_cnt + 256, o_cur = o_hist + al(kWaveBuckets * 4);
-    const uint64_t total_bytes = o_cur + al(kWaveBuckets * 4);
+    const uint64_t total_bytes = o_cnt + kWaveCounters * 4;
     char* buf = nullptr;
     cudaError_t e = cudaMallocAsync((void**)&buf, total_bytes, st);
     if (e != cudaSuccess) return e;
@@ -738,37 +727,38 @@ static cudaError_t launch_path_wave(const GridView& g, const vt_camera& cam, con
     WaveState* wst = (WaveState*)(buf + o_st);
     float4* samples = (float4*)(buf + o_smp);
     float4* sums = (float4*)(buf + o_sum);
-    unsigned int* cnt = (unsigned int*)(buf + o_cnt);  // qn, sqn, nqn
-    unsigned int* hist = (unsigned int*)(buf + o_hist);
-    unsigned int* cursor = (unsigned int*)(buf + o_cur);
+    // lengths of the path queue of each vertex (one counter per vertex, so that the bounce queue
+    // built at vertex b is the path queue of vertex b + 1 without a copy) and of the sun queues
+    unsigned int* qn = (unsigned int*)(buf + o_cnt);
+    unsigned int* sqn = qn + kWaveCounters / 2;
     const unsigned blocks = (unsigned)((cap + 255) / 256);
     for (uint32_t s0 = 0; s0 < P.spp && e == cudaSuccess; s0 += sn) {
         const uint32_t n = std::min(sn, P.spp - s0);
         const uint64_t items = (uint64_t)tiles_x * tiles_y * n * 32;
-        e = cudaMemsetAsync(cnt, 0, 16, st);
+        e = cudaMemsetAsync(qn, 0, kWaveCounters * 4, st);
         if (e != cudaSuccess) break;
-        wave_camera_kernel<<<(unsigned)((items + 255) / 256), 256, 0, st>>>(cam, P, s0, n, tiles_x,
-                                                                           items, q, qid, cnt, wst);
-        for (uint32_t b = 0; b <= P.max_bounces && e == cudaSuccess; ++b) {
-            e = launch_trace_rays_persistent(g, q, cap, hits, next_counter(), S.tune_rays, sm_count,
-                                             st, cnt);
-            if (e == cudaSuccess) e = cudaMemsetAsync(cnt + 1, 0, 8, st);
+        wave_primary_kernel<<<(unsigned)((items + 127) / 128), 128, 0, st>>>(
+            g, cam, P, s0, n, tiles_x, items, q, qid, qn + 1, wst, samples, rays);
+        e = cudaGetLastError();
+        for (uint32_t b = 1; b <= P.max_bounces && e == cudaSuccess; ++b) {
+            // queue lengths: qn[b] paths at vertex b, qn[b + 1] bounce rays, sqn[b] sun rays
+            unsigned int* cq = qn + b;
+            unsigned int* cs = sqn + b;
+            e = launch_trace_rays_persistent(g, q, cap, hits, next_counter(), S.tune_rays,
+                                             sm_count, st, cq);
             if (e != cudaSuccess) break;
-            wave_shade_kernel<<<blocks, 256, 0, st>>>(g, P, b, s0, n, cam.width, q, qid, cnt, hits,
-                                                      wst, samples, sq, sid, cnt + 1, nq, nqid,
-                                                      cnt + 2, rays);
+            wave_shade_kernel<<<blocks, 256, 0, st>>>(g, P, b, s0, n, cam.width, q, qid, cq, hits,
+                                                      wst, samples, sq, sid, cs, nq, nqid, cq + 1,
+                                                      rays);
             e = launch_trace_rays_persistent(g, sq, cap, hits, next_counter(), S.tune_rays,
-                                             sm_count, st, cnt + 1);
+                                             sm_count, st, cs);
             if (e != cudaSuccess) break;
-            wave_sun_kernel<<<blocks, 256, 0, st>>>(P, b >= P.max_bounces, sid, cnt + 1, hits, wst,
+            wave_sun_kernel<<<blocks, 256, 0, st>>>(P, b >= P.max_bounces, sid, cs, hits, wst,
                                                     samples, rays);
-            if (b < P.max_bounces) {
-                e = cudaMemsetAsync(hist, 0, kWaveBuckets * 4, st);
-                if (e != cudaSuccess) break;
-                wave_hist_kernel<<<(unsigned)(sm_count * 4), 256, 0, st>>>(g, nq, cnt + 2, hist);
-                wave_scan_kernel<<<1, 1024, 0, st>>>(hist, cursor, cnt + 2, cnt);
-                wave_scatter_kernel<<<blocks, 256, 0, st>>>(g, nq, nqid, cnt + 2, cursor, q, qid);
-            }
+            // the bounce rays stay in the order the shading appended them, which follows the
+            // path queue: neighbouring entries leave neighbouring surface points
+            std::swap(q, nq);
+            std::swap(qid, nqid);
             e = cudaGetLastError();
         }
         if (e != cudaSuccess) break;

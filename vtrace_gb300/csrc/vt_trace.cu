@@ -36,8 +36,10 @@ template <bool STATS>
 __global__ void __launch_bounds__(256) trace_rays_kernel(GridView g,
                                                          const float2* __restrict__ rays,
                                                          uint64_t n, uint4* __restrict__ out,
-                                                         Counters* __restrict__ counters) {
+                                                         Counters* __restrict__ counters,
+                                                         const unsigned int* __restrict__ n_dev) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n_dev) n = min((uint64_t)*n_dev, n);
     if (i >= n) return;
     Tally<STATS> tl;
     tl.bind(counters, g.bricks);
@@ -63,14 +65,14 @@ cudaError_t launch_render(const GridView& g, const vt_camera& cam, const LightVi
 }
 
 cudaError_t launch_trace_rays(const GridView& g, const vt_ray* rays, uint64_t n, uint4* out,
-                              Counters* counters, cudaStream_t stream) {
+                              Counters* counters, cudaStream_t stream, const unsigned int* n_dev) {
     if (n == 0) return cudaSuccess;
     const uint64_t blocks = (n + 255) / 256;
     const float2* r2 = reinterpret_cast<const float2*>(rays);
     if (counters)
-        trace_rays_kernel<true><<<(unsigned)blocks, 256, 0, stream>>>(g, r2, n, out, counters);
+        trace_rays_kernel<true><<<(unsigned)blocks, 256, 0, stream>>>(g, r2, n, out, counters, n_dev);
     else
-        trace_rays_kernel<false><<<(unsigned)blocks, 256, 0, stream>>>(g, r2, n, out, nullptr);
+        trace_rays_kernel<false><<<(unsigned)blocks, 256, 0, stream>>>(g, r2, n, out, nullptr, n_dev);
     return cudaGetLastError();
 }
 
