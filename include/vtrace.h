@@ -159,7 +159,9 @@ void* vt_get_stream(void);
  * 8 x 4 pixel tiles per warp.  persistent = 1: resident warps keep one ray per lane and refill
  * lanes whose rays have ended with new work once at least `refill_min` lanes are idle (1..32;
  * 32 = only when the whole warp is idle), with at most `blocks_per_sm` 256-thread blocks per SM
- * (0 = as many as fit).  vtrace_gb300.autotune picks them per workload. */
+ * (0 = as many as fit).  VT_KERNEL_BATCH is always persistent; its refill_min 32 (the default)
+ * hands warps whole 8 x 4 tile units traced to the end in each lane.  vtrace_gb300.autotune picks
+ * them per workload. */
 typedef struct vt_tuning {
     uint32_t refill_min;
     int32_t blocks_per_sm;

@@ -406,12 +406,15 @@ def test_launch_shapes_agree(torch, persistent, refill_min, wavefront):
         g.destroy()
 
 
-def test_batched_multiview_matches_oracle(torch):
+@pytest.mark.parametrize("refill", [32, 8], ids=["tile_units", "lane_refill"])
+def test_batched_multiview_matches_oracle(torch, refill):
     """A small batch of uneven views over several grids, replayed from its CUDA graph twice and
-    launched directly once, against the oracle's jittered per-view render."""
+    launched directly once, against the oracle's jittered per-view render; both batch forms."""
     scenes, views = workloads.multiview(n_scenes=3, n_views=7, sizes=(64, 96, 48),
                                         min_px=40 * 30, max_px=200 * 150)
     grids = [vt.Grid.from_u8(s["voxels"], s["palette"]) for s in scenes]
+    saved = vt.get_tuning(vt.KERNEL_BATCH)
+    vt.set_tuning(vt.KERNEL_BATCH, refill, 0, True, False)
     try:
         outs, specs = [], []
         for v in views:
@@ -436,6 +439,8 @@ def test_batched_multiview_matches_oracle(torch):
         assert b.primary_rays == sum(v["camera"].width * v["camera"].height * v["spp"] for v in views)
         b.destroy()
     finally:
+        vt.set_tuning(vt.KERNEL_BATCH, saved["refill_min"], saved["blocks_per_sm"], saved["persistent"],
+                      saved["wavefront"])
         for g in grids:
             if g.id is not None:
                 g.destroy()

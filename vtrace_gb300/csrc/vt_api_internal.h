@@ -60,7 +60,7 @@ struct State {
     std::atomic<uint32_t> counter_next{0};
     // defaults from sweeps on GB300: coherent camera rays keep their 8 x 4 tiles (refills would
     // mix tiles), incoherent ray buffers and path tracing refill a warp once 8 lanes are idle
-    TraceTuning tune_render{16, 0, 0, 0}, tune_rays{8, 0, 1, 0}, tune_batch{16, 0, 0, 0},
+    TraceTuning tune_render{16, 0, 0, 0}, tune_rays{8, 0, 1, 0}, tune_batch{32, 0, 1, 0},
         tune_path{8, 0, 1, 1};
 };
 
