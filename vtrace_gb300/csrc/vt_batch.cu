@@ -164,7 +164,9 @@ __global__ void __launch_bounds__(256, 4) batch_kernel(const BatchView* __restri
 // and shadow ray to the end in the lane (the render kernel's traversal), so that a warp's rays
 // start together and no lane state is kept between units.  Same item order and records as the
 // lane form with whole-warp refills, 23% faster on the 64-view workload.
-__global__ void __launch_bounds__(256) batch_tile_kernel(const BatchView* __restrict__ table,
+constexpr int kBatchTileThreads = 128;
+
+__global__ void __launch_bounds__(kBatchTileThreads) batch_tile_kernel(const BatchView* __restrict__ table,
                                                          uint32_t nviews, uint64_t units,
                                                          unsigned long long* __restrict__ counter) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -270,14 +272,15 @@ unsigned batch_blocks(uint32_t n, uint64_t total, const TraceTuning& tune) {
     const size_t smem = (size_t)n * sizeof(BatchView);
     int per_sm = 0;
     const void* kernel = batch_tile_form(tune) ? (const void*)batch_tile_kernel : (const void*)batch_kernel;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, smem) !=
+    const int threads = batch_tile_form(tune) ? kBatchTileThreads : 256;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) !=
             cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
     }
     if (tune.blocks_per_sm > 0) per_sm = std::min(per_sm, tune.blocks_per_sm);
-    const uint64_t need = (total + 255) / 256;
+    const uint64_t need = (total + threads - 1) / threads;
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)state().sm_count * per_sm, need));
 }
 
@@ -287,7 +290,7 @@ cudaError_t launch_batch(const BatchView* d_table, uint32_t n, uint64_t total,
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     if (batch_tile_form(tune))
-        batch_tile_kernel<<<blocks, 256, (size_t)n * sizeof(BatchView), stream>>>(d_table, n,
+        batch_tile_kernel<<<blocks, kBatchTileThreads, (size_t)n * sizeof(BatchView), stream>>>(d_table, n,
                                                                                   total / 32, counter);
     else
         batch_kernel<<<blocks, 256, (size_t)n * sizeof(BatchView), stream>>>(d_table, n, total,
