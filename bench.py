@@ -557,10 +557,11 @@ def run_config(args):
                               repeats=args.steps, warmup=args.warmup, flush=flush)
         p8 = vt.make_path_params(spp=2, max_bounces=3, seed=1, sun_dir=tuple(w["light"].dir),
                                  out_format=vt.PATH_OUT_RGBA8)
-        vt.path_trace_host(g, cam, p8)
+        host_img = torch.empty(cam.width * cam.height * 4, dtype=torch.uint8, pin_memory=True)
+        vt.path_trace_host(g, cam, p8, out=host_img)
         t0 = time.perf_counter()
         for _ in range(max(1, args.steps // 4)):
-            vt.path_trace_host(g, cam, p8)
+            vt.path_trace_host(g, cam, p8, out=host_img)
         e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 4)
         line.update(metric="Mrays/s (path tracing, 1080p, 1024^3 grid, 2 spp, 3 bounces + sun)",
                     value=rays / ms / 1e3, unit="Mrays/s", ms_per_step=ms,
@@ -568,7 +569,7 @@ def run_config(args):
                             "samples_per_frame": cam.width * cam.height * 2},
                     e2e={"value": rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 96,
                          "d2h_bytes_per_step": cam.width * cam.height * 4,
-                         "path": "vt_path_trace_host (C ABI), RGBA8 out"},
+                         "path": "vt_path_trace_host (C ABI), RGBA8 out to pinned host memory"},
                     gpu_launches=path_launches(vt.get_tuning(vt.KERNEL_PATH), 2, 3,
                                                cam.width * cam.height) * args.steps)
         if not args.no_cpu_baseline:

@@ -272,7 +272,9 @@ int32_t vt_trace_rays_host(int32_t grid, const vt_ray* rays, uint64_t n, vt_hit*
  * row (device).  Asynchronous on `stream`. */
 int32_t vt_render(int32_t grid, const vt_camera* camera, const vt_light* light,
                   vt_hit* d_hits, void* stream);
-/* Same through a host output buffer; returns when the records are in `hits`. */
+/* Same through a host output buffer; returns when the records are in `hits`.  Page-locked
+ * memory (cudaHostAlloc / cudaHostRegister, 16-byte aligned) is written by the render kernel
+ * directly; other memory through a device staging buffer and copies. */
 int32_t vt_render_host(int32_t grid, const vt_camera* camera, const vt_light* light, vt_hit* hits);
 /* Counting variant of vt_render / vt_trace_rays: same records, plus traversal counters (a slower
  * kernel build; for roofline accounting, not for timing).  rays == NULL selects the render form. */
@@ -321,7 +323,8 @@ typedef struct vt_path_params {
  * NULL or a device u64 the launch adds the number of rays it traced to. */
 int32_t vt_path_trace(int32_t grid, const vt_camera* camera, const vt_path_params* params,
                       void* d_out, uint64_t* d_rays_traced, void* stream);
-/* Synchronous, host output; rays_traced may be NULL. */
+/* Synchronous, host output (written by the kernel directly when page-locked and 16-byte
+ * aligned); rays_traced may be NULL. */
 int32_t vt_path_trace_host(int32_t grid, const vt_camera* camera, const vt_path_params* params,
                            void* out, uint64_t* rays_traced);
 

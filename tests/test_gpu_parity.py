@@ -463,6 +463,41 @@ def test_host_forms_split_into_pieces_agree(torch):
         g.destroy()
 
 
+def test_host_forms_write_pinned_outputs_directly(torch):
+    """Page-locked host outputs of vt_render_host and vt_path_trace_host are written by the
+    kernels themselves (no staging copy); vt_trace_rays_host copies into them.  Records and
+    images equal the device forms: a frame above the band size, a ray buffer of several chunks,
+    a path-traced image."""
+    w = workloads.terrain256(n=128, width=1440, height=801)
+    g = vt.Grid.from_u8(w["voxels"], w["palette"])
+    try:
+        cam = w["camera"]
+        light = workloads.seeded_light(1, shadows=True)
+        img, _ = device_render(torch, g, cam, light)
+        out = torch.zeros(cam.width * cam.height * 16, dtype=torch.uint8, pin_memory=True)
+        vt.render_host(g, cam, light, out=out)
+        assert_hits_equal(out.numpy().view(vt.HIT_DTYPE), img, "render_host pinned")
+        with pytest.raises(ValueError):
+            vt.render_host(g, cam, light, out=torch.zeros(16, dtype=torch.uint8, pin_memory=True))
+        n = (1 << 22) + 12345
+        rays = vt.gen_rays_uniform(128, 4, n)
+        hits, _, _ = device_trace(torch, g, rays)
+        h_rays = torch.from_numpy(np.ascontiguousarray(rays, np.float32)).pin_memory()
+        h_hits = torch.zeros(n * 16, dtype=torch.uint8, pin_memory=True)
+        vt.check(vt.lib().vt_trace_rays_host(g.id, h_rays.data_ptr(), n, h_hits.data_ptr()))
+        assert_hits_equal(h_hits.numpy().view(vt.HIT_DTYPE), hits, "trace_rays_host pinned")
+        small = workloads.terrain256(n=128, width=200, height=120)["camera"]
+        p = vt.make_path_params(spp=2, max_bounces=2, seed=3, sun_dir=tuple(light.dir),
+                                out_format=vt.PATH_OUT_RGBA8)
+        want, r_want = vt.path_trace_host(g, small, p)
+        got = torch.zeros(small.width * small.height * 4, dtype=torch.uint8, pin_memory=True)
+        _, r_got = vt.path_trace_host(g, small, p, out=got)
+        assert r_got == r_want > 0
+        assert np.array_equal(got.numpy(), want.reshape(-1))
+    finally:
+        g.destroy()
+
+
 def test_render_footprint_bounds(torch):
     """The distinct footprint of a frame: hit bricks are exactly the bricks of the hit voxels (no
     shadow rays), within the occupied bricks entered, within the bricks entered."""

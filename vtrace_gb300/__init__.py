@@ -526,7 +526,13 @@ def render(grid, camera, light, d_hits, stream=None):
                           _stream(stream)))
 
 
+def _nbytes(x):
+    return x.nbytes if isinstance(x, np.ndarray) else x.numel() * x.element_size()
+
+
 def render_host(grid, camera, light=None, out=None):
+    if out is not None and _nbytes(out) < camera.height * camera.width * 16:
+        raise ValueError("render_host: out holds fewer than width*height 16-byte records")
     hits = out if out is not None else np.zeros(camera.height * camera.width, HIT_DTYPE)
     check(lib().vt_render_host(grid.id, ctypes.byref(camera),
                                ctypes.byref(light) if light is not None else None,
@@ -541,15 +547,18 @@ def path_trace(grid, camera, params, d_out, d_rays=None, stream=None):
                               _ptr(d_rays), _stream(stream)))
 
 
-def path_trace_host(grid, camera, params):
-    """-> (image [height, width, 4] float32 or uint8, rays traced)."""
-    if params.out_format == PATH_OUT_F32X4:
-        out = np.zeros((camera.height, camera.width, 4), np.float32)
-    else:
-        out = np.zeros((camera.height, camera.width, 4), np.uint8)
+def path_trace_host(grid, camera, params, out=None):
+    """-> (image [height, width, 4] float32 or uint8, rays traced).  `out`: optional host buffer
+    of the image's size (a page-locked one is written by the kernel directly)."""
+    px = 16 if params.out_format == PATH_OUT_F32X4 else 4
+    if out is None:
+        dt = np.float32 if params.out_format == PATH_OUT_F32X4 else np.uint8
+        out = np.zeros((camera.height, camera.width, 4), dt)
+    elif _nbytes(out) < camera.height * camera.width * px:
+        raise ValueError("path_trace_host: out is smaller than the image")
     rays = ctypes.c_uint64(0)
     check(lib().vt_path_trace_host(grid.id, ctypes.byref(camera), ctypes.byref(params),
-                                   out.ctypes.data, ctypes.byref(rays)))
+                                   _ptr(out), ctypes.byref(rays)))
     return out, rays.value
 
 

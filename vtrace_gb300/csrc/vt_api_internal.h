@@ -82,6 +82,9 @@ Grid* lookup_grid(int32_t id);
 int32_t register_grid(std::unique_ptr<Grid> g);
 int32_t check_dims(uint32_t nx, uint32_t ny, uint32_t nz);
 int32_t check_camera(const vt_camera* cam);
+// Device address of page-locked, 16-byte aligned host memory (kernels write outputs there
+// directly), or nullptr for any other pointer.
+void* host_mapped(void* p);
 LightView light_view(const vt_light* light);
 int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_host,
                    uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,

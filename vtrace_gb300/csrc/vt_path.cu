@@ -842,14 +842,16 @@ int32_t vt_path_trace_host(int32_t grid, const vt_camera* camera, const vt_path_
     const size_t bytes = out_bytes(*camera, P.out_format);
     State& s = state();
     cudaStream_t st = s.stream;
+    void* mapped = host_mapped(out);  // page-locked output: the resolve kernel writes it directly
+    const size_t dbytes = mapped ? 0 : bytes;
     void* d = nullptr;
-    cudaError_t e = cudaMallocAsync(&d, bytes + 256, st);
+    cudaError_t e = cudaMallocAsync(&d, dbytes + 256, st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_path_trace_host: cudaMallocAsync");
-    unsigned long long* dr = (unsigned long long*)((char*)d + ((bytes + 15) / 16) * 16);
+    unsigned long long* dr = (unsigned long long*)((char*)d + ((dbytes + 15) / 16) * 16);
     unsigned long long hr = 0;
     e = cudaMemsetAsync(dr, 0, 8, st);
-    if (e == cudaSuccess) e = launch_path(g->view(), *camera, P, d, dr, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = launch_path(g->view(), *camera, P, mapped ? mapped : d, dr, st);
+    if (e == cudaSuccess && !mapped) e = cudaMemcpyAsync(out, d, bytes, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&hr, dr, 8, cudaMemcpyDeviceToHost, st);
     cudaFreeAsync(d, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
