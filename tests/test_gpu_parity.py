@@ -447,8 +447,8 @@ def test_batched_multiview_matches_oracle(torch, refill):
 
 
 def test_host_forms_split_into_pieces_agree(torch):
-    """vt_render_host renders in row bands and vt_trace_rays_host in chunks of 4 Mi rays on
-    helper streams; both equal the device forms."""
+    """Into pageable memory vt_render_host renders in row bands, and vt_trace_rays_host works in
+    chunks of 2 Mi rays, on helper streams; both equal the device forms."""
     w = workloads.terrain256(n=128, width=1440, height=801)  # above 1 Mpixel: row bands
     g = vt.Grid.from_u8(w["voxels"], w["palette"])
     try:
