@@ -317,6 +317,10 @@ def run_ours(args):
     rays_per_frame = stats["rays"]
     algo_bytes = (4 * stats["bricks_entered"] + 64 * stats["nonempty_bricks_entered"] +
                   5 * stats["hits"] + 16 * npx)
+    # the per-ray figure as first written for this path: a 64-byte mask for every brick entered,
+    # empty or not, 1 B per voxel tested in occupied bricks, 4 B palette entry per hit, 16 B record
+    spec_bytes = (64 * stats["bricks_entered"] + stats["voxels_tested"] + 4 * stats["hits"] +
+                  16 * npx)
 
     for _ in range(args.warmup):
         vt.render(grid, cam, light, d_hits, stream)
@@ -385,6 +389,13 @@ def run_ours(args):
                      "traffic_source": "profiles/render_shapes1024_1080p.md (ncu, one launch)",
                      "algorithmic_bytes_per_launch": algo_bytes,
                      "kernel": "vt::render_kernel<false>",
+                     "as_first_specified": {
+                         "bytes_per_launch": spec_bytes,
+                         "achieved": spec_bytes / (ms * 1e-3) / 1e9,
+                         "frac": spec_bytes / (ms * 1e-3) / 1e9 / peak,
+                         "note": "64 B per brick entered including empty ones (the brick layout "
+                         "reads a 4 B directory entry there) + 1 B per voxel tested + 4 B per hit "
+                         "+ 16 B record"},
                      "unique_footprint": {
                          "bytes_per_launch": unique_bytes,
                          "achieved": unique_bytes / (ms * 1e-3) / 1e9,

@@ -94,7 +94,8 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
         const int32_t ex = stx > 0 ? min((bxi << 3) + 8, g.nx) : (stx < 0 ? (bxi << 3) - 1 : INT_MIN);
         const int32_t ey = sty > 0 ? min((byi << 3) + 8, g.ny) : (sty < 0 ? (byi << 3) - 1 : INT_MIN);
         const int32_t ez = stz > 0 ? min((bzi << 3) + 8, g.nz) : (stz < 0 ? (bzi << 3) - 1 : INT_MIN);
-        uint32_t steps = 0;  // a brick is left within 22 iterations; 24 bounds the loop
+        // a brick is left within 22 iterations (dda_skip's walk, same argument)
+        uint32_t steps = 0;  // counted by VT_DDA_STEP, not used here
         for (;;) {
             const uint64_t w = __ldg(mk + (vz & 7));
             if ((w >> (((vy & 7) << 3) | (vx & 7))) & 1ull) {
@@ -103,7 +104,7 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
                 break;
             }
             VT_DDA_STEP
-            if (vx == ex || vy == ey || vz == ez || steps >= 24u) break;
+            if (vx == ex || vy == ey || vz == ez) break;
         }
     } else {
         int32_t nxe, nye, nze;
