@@ -446,6 +446,44 @@ def test_batched_multiview_matches_oracle(torch, refill):
                 g.destroy()
 
 
+@pytest.mark.parametrize("refill", [32, 8], ids=["tile_units", "lane_refill"])
+def test_batch_of_the_most_views(torch, refill):
+    """A batch of 256 views (the limit: a 53 KB view table in shared memory, above the default
+    48 KiB a launch gets) over two grids, every view against the oracle."""
+    scenes = [workloads.terrain256(n=48), workloads.terrain256(n=40)]
+    grids = [vt.Grid.from_u8(sc["voxels"], sc["palette"]) for sc in scenes]
+    saved = vt.get_tuning(vt.KERNEL_BATCH)
+    vt.set_tuning(vt.KERNEL_BATCH, refill, 0, True, False)
+    try:
+        rng = np.random.default_rng(11)
+        outs, specs, views = [], [], []
+        for i in range(256):
+            sc = i % 2
+            n = scenes[sc]["voxels"].shape[0]
+            eye, target = workloads.seeded_pose((n, n, n), 100 + i, 1.2 * n)
+            cam = vt.camera_look_at(eye, target, (0.0, 1.0, 0.0), 60.0, int(rng.integers(8, 40)),
+                                    int(rng.integers(4, 24)))
+            spp = int(rng.integers(1, 3))
+            light = workloads.seeded_light(i, shadows=bool(i % 3))
+            buf = torch.zeros(cam.width * cam.height * spp * 16, dtype=torch.uint8, device="cuda")
+            outs.append(buf)
+            views.append((sc, cam, light, spp, i))
+            specs.append(vt.make_view(grids[sc], cam, buf, spp, 5, i, light))
+        b = vt.Batch(specs)
+        b.run(graph=True)
+        torch.cuda.synchronize()
+        ogrids = [po.Grid(sc["voxels"], sc["palette"]) for sc in scenes]
+        for (sc, cam, light, spp, i), o in zip(views, outs):
+            want = po.render_view(ogrids[sc], oracle_camera(cam), oracle_light(light), spp, 5, i)
+            assert_hits_equal(hits_from_dev(o), want, "view %d" % i)
+        b.destroy()
+    finally:
+        vt.set_tuning(vt.KERNEL_BATCH, saved["refill_min"], saved["blocks_per_sm"], saved["persistent"],
+                      saved["wavefront"])
+        for g in grids:
+            g.destroy()
+
+
 def test_host_forms_split_into_pieces_agree(torch):
     """Into pageable memory vt_render_host renders in row bands, and vt_trace_rays_host works in
     chunks of 2 Mi rays, on helper streams; both equal the device forms."""

@@ -270,6 +270,14 @@ BatchView make_batch_view(const Grid& g, const vt_camera& cam, const vt_light* l
 
 unsigned batch_blocks(uint32_t n, uint64_t total, const TraceTuning& tune) {
     const size_t smem = (size_t)n * sizeof(BatchView);
+    // a full table (256 views x 208 B) is above the 48 KiB of dynamic shared memory a launch
+    // gets without opting in; set on every call (cheap), so that a re-created context has it too
+    const int table_max = (int)(kMaxBatchViews * sizeof(BatchView));
+    if (cudaFuncSetAttribute((const void*)batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             table_max) != cudaSuccess ||
+        cudaFuncSetAttribute((const void*)batch_tile_kernel,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, table_max) != cudaSuccess)
+        cudaGetLastError();
     int per_sm = 0;
     const void* kernel = batch_tile_form(tune) ? (const void*)batch_tile_kernel : (const void*)batch_kernel;
     const int threads = batch_tile_form(tune) ? kBatchTileThreads : 256;
