@@ -333,8 +333,8 @@ int32_t vt_path_trace_host(int32_t grid, const vt_camera* camera, const vt_path_
 /* One view of a batch: a camera over a grid with `spp` jittered samples per pixel.  Sample s of
  * pixel (px, py) uses the sub-pixel offset Philox4x32-10(counter = {px, py, s, view_id},
  * key = {seed, 0x56544752}) words 0 and 1, each >> 8 and scaled by 2^-24, and is written to
- * d_out[(py * width + px) * spp + s] (device memory, 16-byte aligned).  The light is used when
- * flags & VT_VIEW_LIGHT. */
+ * d_out[(py * width + px) * spp + s] (device memory, 16-byte aligned; width * height * spp below
+ * 2^32, else VT_ELIMIT).  The light is used when flags & VT_VIEW_LIGHT. */
 typedef struct vt_view {
     int32_t grid;
     uint32_t spp;
@@ -412,6 +412,7 @@ int32_t vt_serve_start(const vt_serve_config* cfg, int32_t* service_out);
  * the life of the service: the cache rebuilds evicted scenes from it). */
 int32_t vt_serve_add_scene(int32_t service, const uint8_t* voxels, const uint32_t* palette,
                            uint32_t nx, uint32_t ny, uint32_t nz, int32_t* scene_out);
+/* Queue a request (width * height * spp below 2^32, else VT_ELIMIT). */
 int32_t vt_serve_submit(int32_t service, const vt_serve_request* req, uint64_t* request_id);
 /* Wait up to timeout_us for a request: VT_OK (image written; the request is released),
  * VT_ENOTREADY, or the request's error (VT_ENOMEM when its scene exceeds the budget,

@@ -1,6 +1,7 @@
 """The continuous-batching service: every request's image is the same whether it ran alone or
 packed with others into shared launches, and equals the oracle's averaged jittered samples; the
 grid cache respects its HBM budget; failures are reported per request."""
+import ctypes
 import numpy as np
 import pytest
 
@@ -164,6 +165,17 @@ def test_protocol_errors(torch):
         with pytest.raises(vt.VtError) as e:
             svc.submit(sid, v["camera"], pinned(torch, v["camera"]), spp=0)
         assert e.value.code == -1
+        with pytest.raises(ValueError):
+            svc.submit(sid, v["camera"], torch.zeros(16, dtype=torch.uint8, pin_memory=True))
+        # 2^32 samples: refused before the (here far too small) output is touched
+        r = vt.ServeRequest()
+        r.scene, r.spp = sid, 1
+        r.camera = vt.camera_look_at((-40.0, 80.0, -40.0), (32.0, 16.0, 32.0), (0, 1, 0), 60.0,
+                                     65536, 65536)
+        tiny = torch.zeros(16, dtype=torch.uint8, pin_memory=True)
+        r.host_rgba = tiny.data_ptr()
+        rid0 = ctypes.c_uint64(0)
+        assert vt.lib().vt_serve_submit(svc.id, ctypes.byref(r), ctypes.byref(rid0)) == -9  # VT_ELIMIT
         with pytest.raises(vt.VtError) as e:
             svc.poll(123456789)
         assert e.value.code == -4  # VT_ENOTFOUND

@@ -653,6 +653,9 @@ class Service:
         return out.value
 
     def submit(self, scene, camera, out_rgba, spp=1, seed=0, view_id=0, light=None):
+        if out_rgba is not None and not isinstance(out_rgba, int) and \
+                _nbytes(out_rgba) < camera.width * camera.height * 4:
+            raise ValueError("submit: out_rgba is smaller than the width x height RGBA8 image")
         r = ServeRequest()
         r.scene, r.spp, r.seed, r.view_id = scene, spp, seed, view_id
         r.flags = VIEW_LIGHT if light is not None else 0

@@ -348,6 +348,11 @@ int32_t vt_batch_create(const vt_view* views, uint32_t n, int32_t* batch_out) {
             return fail(VT_EINVAL, "vt_batch_create: view " + std::to_string(i) +
                                        " needs spp in 1..64 and a 16-byte aligned output");
         }
+        if ((uint64_t)v.camera.width * v.camera.height * v.spp >= (1ull << 32)) {
+            batch_free(*b);  // sample records are indexed with 32 bits
+            return fail(VT_ELIMIT, "vt_batch_create: view " + std::to_string(i) +
+                                       " has 2^32 or more samples");
+        }
         g->refs.fetch_add(1);
         b->grids.push_back(v.grid);
         table[i] = make_batch_view(*g, v.camera, (v.flags & VT_VIEW_LIGHT) ? &v.light : nullptr,

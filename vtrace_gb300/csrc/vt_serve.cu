@@ -417,6 +417,8 @@ int32_t vt_serve_submit(int32_t service, const vt_serve_request* req, uint64_t* 
     int32_t rc = check_camera(&req->camera);
     if (rc) return rc;
     if (req->spp == 0 || req->spp > 64) return fail(VT_EINVAL, "vt_serve_submit: spp must be 1..64");
+    if ((uint64_t)req->camera.width * req->camera.height * req->spp >= (1ull << 32))
+        return fail(VT_ELIMIT, "vt_serve_submit: 2^32 or more samples in one request");
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) return fail(VT_ECANCELED, "vt_serve_submit: service stopping");
     if (req->scene < 0 || (size_t)req->scene >= s->scenes.size())
