@@ -319,8 +319,9 @@ typedef struct vt_path_params {
     float sun_dir[3];     /* unit direction toward the sun */
     float sun[3];         /* sun irradiance; all zero: no next-event rays */
 } vt_path_params;
-/* d_out: width*height pixels of the chosen format (device, 16-byte aligned).  d_rays_traced:
- * NULL or a device u64 the launch adds the number of rays it traced to. */
+/* d_out: width*height pixels of the chosen format (device, 16-byte aligned; width*height below
+ * 2^32, else VT_ELIMIT).  d_rays_traced: NULL or a device u64 the launch adds the number of rays
+ * it traced to. */
 int32_t vt_path_trace(int32_t grid, const vt_camera* camera, const vt_path_params* params,
                       void* d_out, uint64_t* d_rays_traced, void* stream);
 /* Synchronous, host output (written by the kernel directly when page-locked and 16-byte

@@ -1,5 +1,7 @@
 """Path tracing on the device against the oracle's restatement of the estimator: bit-identical
 float radiance and RGBA8, the same ray count, on u8 and RGBA8 grids."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -101,5 +103,11 @@ def test_path_trace_rgba8_grid_and_determinism(torch, form):
         with pytest.raises(vt.VtError):
             p.spp = 0
             vt.path_trace_host(g, cam, p)
+        # 2^32 pixels: refused before any buffer is touched (here an output far too small)
+        p.spp = 1
+        huge = vt.camera_look_at((-20.0, 45.0, -25.0), (20.0, 10.0, 20.0), (0, 1, 0), 60.0, 65536, 65536)
+        tiny = torch.zeros(256, dtype=torch.uint8, device="cuda")
+        assert vt.lib().vt_path_trace(g.id, ctypes.byref(huge), ctypes.byref(p), tiny.data_ptr(),
+                                      None, None) == -9  # VT_ELIMIT
     finally:
         g.destroy()

@@ -804,6 +804,15 @@ static cudaError_t launch_path(const GridView& g, const vt_camera& cam, const Pa
     return cudaGetLastError();
 }
 
+// Pixel counts are 32-bit in the path kernels: a 65536 x 65536 image is refused.
+static int32_t check_path_camera(const vt_camera* cam) {
+    int32_t rc = check_camera(cam);
+    if (rc) return rc;
+    if ((uint64_t)cam->width * cam->height >= (1ull << 32))
+        return fail(VT_ELIMIT, "vt_path_trace: 2^32 or more pixels");
+    return VT_OK;
+}
+
 static size_t out_bytes(const vt_camera& cam, uint32_t fmt) {
     return (size_t)cam.width * cam.height * (fmt == VT_PATH_OUT_F32X4 ? 16 : 4);
 }
@@ -818,7 +827,7 @@ int32_t vt_path_trace(int32_t grid, const vt_camera* camera, const vt_path_param
                       void* d_out, uint64_t* d_rays_traced, void* stream) {
     Grid* g = lookup_grid(grid);
     if (!g) return fail(VT_ENOTFOUND, "vt_path_trace: unknown grid");
-    int32_t rc = check_camera(camera);
+    int32_t rc = check_path_camera(camera);
     if (rc) return rc;
     PathParams P;
     if ((rc = path_params(params, P))) return rc;
@@ -834,7 +843,7 @@ int32_t vt_path_trace_host(int32_t grid, const vt_camera* camera, const vt_path_
                            void* out, uint64_t* rays_traced) {
     Grid* g = lookup_grid(grid);
     if (!g) return fail(VT_ENOTFOUND, "vt_path_trace_host: unknown grid");
-    int32_t rc = check_camera(camera);
+    int32_t rc = check_path_camera(camera);
     if (rc) return rc;
     PathParams P;
     if ((rc = path_params(params, P))) return rc;
