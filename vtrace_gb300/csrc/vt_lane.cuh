@@ -126,6 +126,12 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
     return status;
 }
 
+// Whether the lane's next unit is an occupied-brick walk (else an empty-region crossing).
+__device__ __forceinline__ bool ray_next_walk(const GridView& g, const LaneRay& R) {
+    const uint32_t bidx = (uint32_t)(R.vx >> 3) + (uint32_t)g.bx * ((uint32_t)(R.vy >> 3) + (uint32_t)g.by * (uint32_t)(R.vz >> 3));
+    return !brick_empty(__ldg(g.dir + bidx));
+}
+
 // Record of a finished ray (unshaded colour; misses carry `miss_rgba`).
 __device__ __forceinline__ HitRec ray_record(const GridView& g, const LaneRay& R, int status,
                                              uint32_t miss_rgba) {

@@ -202,6 +202,8 @@ __global__ void __launch_bounds__(256) render_persistent_kernel(
     }
 }
 
+constexpr int kUnitWait = 4;
+
 // n_dev: nullptr, or the device-side ray count (at most n), read at the start (ray queues whose
 // length the host does not know).
 __global__ void __launch_bounds__(256) trace_rays_persistent_kernel(
@@ -214,6 +216,7 @@ __global__ void __launch_bounds__(256) trace_rays_persistent_kernel(
     bool busy = false;
     uint64_t idx = 0;
     bool more = true;
+    int wait_w = 0, wait_c = 0;  // warp-uniform: iterations a unit kind was passed over
     for (;;) {
         uint32_t idle = __ballot_sync(0xFFFFFFFFu, !busy);
         while (more && __popc(idle) >= (int)refill_min) {
@@ -236,7 +239,23 @@ __global__ void __launch_bounds__(256) trace_rays_persistent_kernel(
             idle = __ballot_sync(0xFFFFFFFFu, !busy);
         }
         if (!more && idle == 0xFFFFFFFFu) break;
-        if (busy) {
+        // One kind of unit per pass: the lanes whose next unit is the more common kind (walk or
+        // crossing) run it, the others wait, unless their kind has already waited kUnitWait
+        // passes.  A warp then issues one kind's instructions per pass instead of both; every
+        // pass with busy lanes runs at least one unit.  2% faster on the 16M incoherent rays.
+        const bool walk = busy && ray_next_walk(g, R);
+        const uint32_t wb = __ballot_sync(0xFFFFFFFFu, walk);
+        const uint32_t cb = __ballot_sync(0xFFFFFFFFu, busy && !walk);
+        bool run_walk = __popc(wb) >= __popc(cb);
+        if (run_walk ? (cb && wait_c >= kUnitWait) : (wb && wait_w >= kUnitWait)) run_walk = !run_walk;
+        if (run_walk) {
+            wait_w = 0;
+            wait_c = cb ? wait_c + 1 : 0;
+        } else {
+            wait_c = 0;
+            wait_w = wb ? wait_w + 1 : 0;
+        }
+        if (busy && walk == run_walk) {
             const int st = ray_unit(g, R);
             if (st != kRayRunning) {
                 const HitRec h = ray_record(g, R, st, 0u);
