@@ -52,6 +52,17 @@ int32_t ensure_init_locked(int32_t device) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
     e = cudaMalloc(&s.counters, kCounterRing * sizeof(unsigned long long));
     if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(work counters)");
+    // stream-ordered temporaries (build scratch, uploads, path-tracing queues) come from the
+    // device's default pool; keep up to 4 GiB of freed pool memory for the next call instead
+    // of returning it at every synchronisation (a process-local setting of this context)
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = 4ull << 30;
+        if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess)
+            cudaGetLastError();
+    } else {
+        cudaGetLastError();
+    }
     s.device = device;
     s.inited = true;
     return VT_OK;
@@ -112,18 +123,25 @@ GridView Grid::view() const {
     return v;
 }
 
-void Grid::release() {
-    cudaFree(oct);
-    oct = nullptr;
-    cudaFree(lng);
-    lng = nullptr;
-    cudaFree(dir);
-    cudaFree(masks);
-    cudaFree(payload);
-    cudaFree(palette);
-    dir = nullptr;
+bool Grid::in_block(const void* p) const {
+    return block && p >= block && (const char*)p < (const char*)block + block_bytes;
+}
+
+void Grid::free_slot_arrays() {
+    if (!in_block(masks)) cudaFree(masks);
+    if (!in_block(payload)) cudaFree(payload);
     masks = nullptr;
     payload = nullptr;
+}
+
+void Grid::release() {
+    free_slot_arrays();
+    cudaFree(block);  // directory, octant and long-box words, palette (and the first slot arrays)
+    block = nullptr;
+    block_bytes = 0;
+    dir = nullptr;
+    oct = nullptr;
+    lng = nullptr;
     palette = nullptr;
 }
 
@@ -138,6 +156,10 @@ int32_t check_dims(uint32_t nx, uint32_t ny, uint32_t nz) {
 }
 
 // Builds the brick layout of a dense device grid on `stream` and waits for it.
+// Grids of up to this many bricks (64^3 voxels) get slot arrays for every brick at once, so that
+// their build needs no mid-way count readback (at most 1 MiB over-allocated).
+constexpr uint64_t kSmallGridBricks = 512;
+
 int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_host,
                    uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,
                    std::unique_ptr<Grid>& out) {
@@ -150,57 +172,73 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
     g->bz = (nz + 7) / 8;
     g->bricks = (uint64_t)g->bx * g->by * g->bz;
     g->format = format;
-    cudaError_t e;
-    if (format == VT_PAYLOAD_U8) {
-        e = cudaMalloc(&g->palette, 256 * sizeof(uint32_t));
-        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(palette)");
-        e = cudaMemcpyAsync(g->palette, palette_host, 256 * sizeof(uint32_t),
-                            cudaMemcpyHostToDevice, stream);
-        if (e != cudaSuccess) {
-            g->release();
-            return cuda_fail(e, "cudaMemcpy(palette)");
+    const bool small = g->bricks <= kSmallGridBricks;
+    const size_t psize = format == VT_PAYLOAD_U8 ? 512 : 2048;
+    // one allocation: directory, octant words, long-box words, palette, masks, payloads
+    auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+    auto allocate = [&](uint64_t slots) -> int32_t {
+        const size_t o_oct = al(g->bricks * 4), o_lng = o_oct + al(g->bricks * 4);
+        const size_t o_pal = o_lng + al(g->bricks * 12), o_msk = o_pal + 1024;
+        const size_t o_pay = o_msk + al(slots * 64), total = o_pay + al(slots * psize);
+        if (cudaMalloc(&g->block, total) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(VT_ENOMEM, "cudaMalloc(brick grid) failed");
         }
+        char* b = (char*)g->block;
+        g->block_bytes = total;
+        g->dir = (uint32_t*)b;
+        g->oct = (uint32_t*)(b + o_oct);
+        g->lng = (uint32_t*)(b + o_lng);
+        g->palette = format == VT_PAYLOAD_U8 ? (uint32_t*)(b + o_pal) : nullptr;
+        g->masks = (uint64_t*)(b + o_msk);
+        g->payload = b + o_pay;
+        g->slot_capacity = slots;
+        if (g->palette &&
+            cudaMemcpyAsync(g->palette, palette_host, 1024, cudaMemcpyHostToDevice, stream) !=
+                cudaSuccess)
+            return cuda_fail(cudaGetLastError(), "cudaMemcpy(palette)");
+        return VT_OK;
+    };
+    int32_t rc = VT_OK;
+    if (small && (rc = allocate(g->bricks))) {
+        g->release();
+        return rc;
     }
+    // the words kernel reads the palette from device memory: a large grid uploads it first
+    uint32_t* d_palette = g->palette;
     void* scratch = nullptr;
-    const size_t sbytes = build_scratch_bytes(g->bricks);
-    e = cudaMalloc(&scratch, sbytes);
+    const size_t sbytes = build_scratch_bytes(g->bricks) + (small ? 0 : 1024);
+    cudaError_t e = cudaMallocAsync(&scratch, sbytes, stream);
     if (e != cudaSuccess) {
         g->release();
         cudaGetLastError();
-        return fail(VT_ENOMEM, "cudaMalloc(brick build scratch) failed");
+        return fail(VT_ENOMEM, "cudaMallocAsync(brick build scratch) failed");
     }
     BuildScratch s = carve_build_scratch(scratch, g->bricks);
-    int32_t rc = VT_OK;
-    uint32_t last_off = 0, last_flag = 0;
+    uint32_t counts[2] = {0, 0};
     unsigned long long occ = 0;
     do {
+        if (!small && format == VT_PAYLOAD_U8) {
+            d_palette = (uint32_t*)((char*)scratch + build_scratch_bytes(g->bricks));
+            e = cudaMemcpyAsync(d_palette, palette_host, 1024, cudaMemcpyHostToDevice, stream);
+            if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpy(palette)"); break; }
+        }
         // u8 palettes whose only transparent entry is index 0: occupancy is "index != 0"
         bool nonzero = format == VT_PAYLOAD_U8 && (palette_host[0] >> 24) == 0u;
         for (int i = 1; nonzero && i < 256; ++i) nonzero = (palette_host[i] >> 24) != 0u;
-        e = launch_brick_words(d_src, format, g->palette, (int32_t)nx, (int32_t)ny, (int32_t)nz, s,
+        e = launch_brick_words(d_src, format, d_palette, (int32_t)nx, (int32_t)ny, (int32_t)nz, s,
                                stream, nonzero);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick words kernel"); break; }
         e = launch_brick_scan(s, g->bricks, stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick scan kernel"); break; }
-        e = cudaMemcpyAsync(&last_off, s.offsets + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(&last_flag, s.flags + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(&occ, s.occupied, 8, cudaMemcpyDeviceToHost, stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-        if (e != cudaSuccess) { rc = cuda_fail(e, "brick count readback"); break; }
-        g->nonempty = (uint64_t)last_off + last_flag;
-        g->occupied = occ;
-        const uint64_t slots = g->nonempty ? g->nonempty : 1;
-        const size_t psize = format == VT_PAYLOAD_U8 ? 512 : 2048;
-        if (cudaMalloc(&g->dir, g->bricks * 4) != cudaSuccess ||
-            cudaMalloc(&g->oct, g->bricks * 4) != cudaSuccess ||
-            cudaMalloc(&g->lng, g->bricks * 12) != cudaSuccess ||
-            cudaMalloc(&g->masks, slots * 64) != cudaSuccess ||
-            cudaMalloc(&g->payload, slots * psize) != cudaSuccess) {
-            cudaGetLastError();
-            rc = fail(VT_ENOMEM, "cudaMalloc(brick grid) failed");
-            break;
+        if (!small) {  // slot arrays sized by the count of occupied bricks
+            e = cudaMemcpyAsync(&counts[0], s.offsets + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(&counts[1], s.flags + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            if (e != cudaSuccess) { rc = cuda_fail(e, "brick count readback"); break; }
+            const uint64_t nonempty = (uint64_t)counts[0] + counts[1];
+            if ((rc = allocate(nonempty ? nonempty : 1))) break;
         }
         e = launch_brick_compact(d_src, format, (int32_t)nx, (int32_t)ny, (int32_t)nz, s, g->dir,
                                  g->masks, g->payload, stream);
@@ -215,14 +253,21 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
         e = launch_brick_long(g->dir, g->oct, (uint32_t*)s.words, g->lng, (int32_t)g->bx,
                               (int32_t)g->by, (int32_t)g->bz, stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick long-box kernels"); break; }
-        e = cudaStreamSynchronize(stream);
+        e = cudaMemcpyAsync(&counts[0], s.offsets + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&counts[1], s.flags + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&occ, s.occupied, 8, cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick build"); break; }
-        g->bytes = g->bricks * 20 + slots * 64 + slots * psize + (g->palette ? 1024 : 0);
-        g->slot_capacity = slots;
+        g->nonempty = (uint64_t)counts[0] + counts[1];
+        g->occupied = occ;
+        g->bytes = g->block_bytes;
         g->slots_used = g->nonempty;
     } while (0);
-    cudaFree(scratch);
+    const cudaError_t f = cudaFreeAsync(scratch, stream);
+    if (rc == VT_OK && f != cudaSuccess) rc = cuda_fail(f, "cudaFreeAsync(brick build scratch)");
     if (rc != VT_OK) {
+        cudaStreamSynchronize(stream);
         g->release();
         return rc;
     }
@@ -434,12 +479,12 @@ static int32_t create_from_host(const void* data, size_t elem, uint32_t format, 
     if ((rc = ensure_init())) return rc;
     const size_t bytes = (size_t)nx * ny * nz * elem;
     const int nbuf = order == VT_ORDER_Z_FASTEST ? 2 : 1;
-    void* d = nullptr;
-    if (cudaMalloc(&d, bytes * nbuf) != cudaSuccess) {
-        cudaGetLastError();
-        return fail(VT_ENOMEM, "cudaMalloc(dense grid upload) failed");
-    }
     cudaStream_t st = state().stream;
+    void* d = nullptr;
+    if (cudaMallocAsync(&d, bytes * nbuf, st) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(VT_ENOMEM, "cudaMallocAsync(dense grid upload) failed");
+    }
     // z-fastest input lands in the second half and is transposed into the first
     void* up = (char*)d + bytes * (nbuf - 1);
     cudaError_t e = cudaMemcpyAsync(up, data, bytes, cudaMemcpyHostToDevice, st);
@@ -450,8 +495,8 @@ static int32_t create_from_host(const void* data, size_t elem, uint32_t format, 
         rc = cuda_fail(e, "dense grid upload");
     else
         rc = build_grid(d, format, palette, nx, ny, nz, st, g);
-    cudaStreamSynchronize(st);
-    cudaFree(d);
+    cudaFreeAsync(d, st);
+    cudaStreamSynchronize(st);  // the caller's buffer is read by then
     if (rc) return rc;
     return register_grid(std::move(g));
 }

@@ -32,12 +32,18 @@ struct Grid {
     uint64_t* masks = nullptr;
     void* payload = nullptr;
     uint32_t* palette = nullptr;
+    // one allocation holding dir, oct, lng and palette, and masks and payload until an update
+    // grows the slots into separate allocations
+    void* block = nullptr;
+    size_t block_bytes = 0;
     size_t bytes = 0;
     // slots of masks/payload: allocated, handed out (high-water mark), and freed by updates
     uint64_t slot_capacity = 0, slots_used = 0;
     std::vector<uint32_t> free_slots;
     std::atomic<int32_t> refs{0};  // in-flight batches / serving requests using the grid
     GridView view() const;
+    bool in_block(const void* p) const;
+    void free_slot_arrays();  // masks and payload (when not inside `block`)
     void release();
 };
 

@@ -144,11 +144,11 @@ static int32_t grow_slots(Grid& g, uint64_t need, cudaStream_t st) {
         cudaFree(p);
         return cuda_fail(e, "vt_grid_update: slot copy");
     }
-    cudaFree(g.masks);
-    cudaFree(g.payload);
+    // slot arrays of the build's single allocation stay allocated with it: only later ones go
+    g.bytes += (g.in_block(g.masks) ? cap : cap - g.slot_capacity) * (64 + psize);
+    g.free_slot_arrays();
     g.masks = m;
     g.payload = p;
-    g.bytes += (cap - g.slot_capacity) * (64 + psize);
     g.slot_capacity = cap;
     return VT_OK;
 }
