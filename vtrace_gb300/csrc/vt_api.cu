@@ -156,9 +156,207 @@ int32_t check_dims(uint32_t nx, uint32_t ny, uint32_t nz) {
 }
 
 // Builds the brick layout of a dense device grid on `stream` and waits for it.
-// Grids of up to this many bricks (64^3 voxels) get slot arrays for every brick at once, so that
-// their build needs no mid-way count readback (at most 1 MiB over-allocated).
-constexpr uint64_t kSmallGridBricks = 512;
+// One device allocation per grid: directory, octant words, long-box words, palette, masks and
+// payloads of `slots` slots, each part 256-byte aligned.
+struct BlockLayout {
+    size_t oct, lng, pal, msk, pay, total;
+};
+
+static BlockLayout block_layout(uint64_t bricks, uint64_t slots, uint32_t format) {
+    auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+    const size_t psize = format == VT_PAYLOAD_U8 ? 512 : 2048;
+    BlockLayout L;
+    L.oct = al(bricks * 4);
+    L.lng = L.oct + al(bricks * 4);
+    L.pal = L.lng + al(bricks * 12);
+    L.msk = L.pal + 1024;
+    L.pay = L.msk + al(slots * 64);
+    L.total = L.pay + al(slots * psize);
+    return L;
+}
+
+static void point_into_block(Grid& g, void* block, const BlockLayout& L, uint64_t slots) {
+    char* b = (char*)block;
+    g.block = block;
+    g.block_bytes = L.total;
+    g.dir = (uint32_t*)b;
+    g.oct = (uint32_t*)(b + L.oct);
+    g.lng = (uint32_t*)(b + L.lng);
+    g.palette = g.format == VT_PAYLOAD_U8 ? (uint32_t*)(b + L.pal) : nullptr;
+    g.masks = (uint64_t*)(b + L.msk);
+    g.payload = b + L.pay;
+    g.slot_capacity = slots;
+}
+
+// The brick build's launches on `stream` (captured or not): occupancy words, slot scan, compaction
+// into dir / masks / payload, distance field, octant words, long-box words.
+static cudaError_t build_launches(const void* d_src, uint32_t format, const uint32_t* d_palette,
+                                  bool nonzero, const Grid& g, const BuildScratch& s,
+                                  cudaStream_t stream) {
+    const int32_t nx = (int32_t)g.nx, ny = (int32_t)g.ny, nz = (int32_t)g.nz;
+    cudaError_t e = launch_brick_words(d_src, format, d_palette, nx, ny, nz, s, stream, nonzero);
+    if (e == cudaSuccess) e = launch_brick_scan(s, g.bricks, stream);
+    if (e == cudaSuccess)
+        e = launch_brick_compact(d_src, format, nx, ny, nz, s, g.dir, g.masks, g.payload, stream);
+    if (e == cudaSuccess)
+        e = launch_brick_distance(s, g.dir, (int32_t)g.bx, (int32_t)g.by, (int32_t)g.bz, stream);
+    // the occupancy words are no longer needed: their scratch holds the octant passes, and then
+    // the long-box runs and window minima (13 words per brick of the 16 there)
+    if (e == cudaSuccess)
+        e = launch_brick_octants(g.dir, (uint8_t*)s.words,
+                                 (uint16_t*)((uint8_t*)s.words + ((g.bricks + 255) / 256) * 256),
+                                 g.oct, (int32_t)g.bx, (int32_t)g.by, (int32_t)g.bz, stream);
+    if (e == cudaSuccess)
+        e = launch_brick_long(g.dir, g.oct, (uint32_t*)s.words, g.lng, (int32_t)g.bx,
+                              (int32_t)g.by, (int32_t)g.bz, stream);
+    return e;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Small grids (vtrace's 16^3 chunk textures, .vox models): the build's twenty-odd launches cost
+// more than their work, so they are captured once per grid shape into a CUDA graph that reads a
+// fixed input buffer and builds into a fixed template of the grid's allocation (every brick has a
+// slot).  A build copies its voxels in, replays the graph, and copies the template into the new
+// grid's allocation.  Builds of small grids are serialised by g_small_mu.
+// ---------------------------------------------------------------------------------------------
+constexpr uint64_t kSmallGridBricks = 512;  // 64^3 voxels: at most 1 MiB of unused slots
+constexpr size_t kSmallGraphs = 64;
+
+struct SmallBuild {
+    uint32_t nx = 0, ny = 0, nz = 0, format = 0;
+    bool nonzero = false;
+    void* in = nullptr;          // the shape's dense voxels
+    void* tmpl = nullptr;        // block layout with a slot per brick
+    void* scratch = nullptr;
+    uint32_t* counts = nullptr;  // last slot offset, last flag, occupied voxels (u64)
+    cudaGraphExec_t exec = nullptr;
+    uint64_t last_use = 0;
+};
+
+static std::mutex g_small_mu;
+static std::vector<SmallBuild> g_small;
+static uint64_t g_small_clock = 0;
+
+static void small_free(SmallBuild& b) {
+    if (b.exec) cudaGraphExecDestroy(b.exec);
+    cudaFree(b.in);
+    cudaFree(b.tmpl);
+    cudaFree(b.scratch);
+    cudaFree(b.counts);
+    b = SmallBuild();
+}
+
+void release_small_builds() {
+    std::lock_guard<std::mutex> lk(g_small_mu);
+    for (SmallBuild& b : g_small) small_free(b);
+    g_small.clear();
+}
+
+static int32_t small_entry(const Grid& shape, bool nonzero, SmallBuild*& out) {
+    for (SmallBuild& b : g_small)
+        if (b.nx == shape.nx && b.ny == shape.ny && b.nz == shape.nz && b.format == shape.format &&
+            b.nonzero == nonzero) {
+            out = &b;
+            return VT_OK;
+        }
+    if (g_small.size() >= kSmallGraphs) {  // drop the least recently used shape
+        size_t old = 0;
+        for (size_t i = 1; i < g_small.size(); ++i)
+            if (g_small[i].last_use < g_small[old].last_use) old = i;
+        small_free(g_small[old]);
+        g_small.erase(g_small.begin() + (long)old);
+    }
+    SmallBuild b;
+    b.nx = shape.nx;
+    b.ny = shape.ny;
+    b.nz = shape.nz;
+    b.format = shape.format;
+    b.nonzero = nonzero;
+    const size_t elem = shape.format == VT_PAYLOAD_U8 ? 1 : 4;
+    const BlockLayout L = block_layout(shape.bricks, shape.bricks, shape.format);
+    if (cudaMalloc(&b.in, (size_t)shape.nx * shape.ny * shape.nz * elem) != cudaSuccess ||
+        cudaMalloc(&b.tmpl, L.total) != cudaSuccess ||
+        cudaMalloc(&b.scratch, build_scratch_bytes(shape.bricks)) != cudaSuccess ||
+        cudaMalloc(&b.counts, 16) != cudaSuccess) {
+        cudaGetLastError();
+        small_free(b);
+        return fail(VT_ENOMEM, "cudaMalloc(small grid build) failed");
+    }
+    Grid t;  // the template's view of the layout
+    t.nx = shape.nx;
+    t.ny = shape.ny;
+    t.nz = shape.nz;
+    t.bx = shape.bx;
+    t.by = shape.by;
+    t.bz = shape.bz;
+    t.bricks = shape.bricks;
+    t.format = shape.format;
+    point_into_block(t, b.tmpl, L, shape.bricks);
+    const BuildScratch s = carve_build_scratch(b.scratch, shape.bricks);
+    cudaStream_t cs;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t le = build_launches(b.in, shape.format, t.palette, nonzero, t, s, cs);
+            if (le == cudaSuccess)
+                le = cudaMemcpyAsync(b.counts, s.offsets + (shape.bricks - 1), 4,
+                                     cudaMemcpyDeviceToDevice, cs);
+            if (le == cudaSuccess)
+                le = cudaMemcpyAsync(b.counts + 1, s.flags + (shape.bricks - 1), 4,
+                                     cudaMemcpyDeviceToDevice, cs);
+            if (le == cudaSuccess)
+                le = cudaMemcpyAsync(b.counts + 2, s.occupied, 8, cudaMemcpyDeviceToDevice, cs);
+            e = cudaStreamEndCapture(cs, &graph);
+            if (e == cudaSuccess) e = le;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        cudaStreamDestroy(cs);
+    }
+    t.block = nullptr;  // the template belongs to the cache entry
+    if (e != cudaSuccess) {
+        small_free(b);
+        return cuda_fail(e, "small grid build graph");
+    }
+    g_small.push_back(b);
+    out = &g_small.back();
+    return VT_OK;
+}
+
+static int32_t build_small(const void* d_src, const uint32_t* palette_host, bool nonzero,
+                           std::unique_ptr<Grid>& g, cudaStream_t stream) {
+    std::lock_guard<std::mutex> lk(g_small_mu);
+    SmallBuild* b = nullptr;
+    int32_t rc = small_entry(*g, nonzero, b);
+    if (rc) return rc;
+    b->last_use = ++g_small_clock;
+    const size_t elem = g->format == VT_PAYLOAD_U8 ? 1 : 4;
+    const BlockLayout L = block_layout(g->bricks, g->bricks, g->format);
+    void* block = nullptr;
+    if (cudaMalloc(&block, L.total) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(VT_ENOMEM, "cudaMalloc(brick grid) failed");
+    }
+    point_into_block(*g, block, L, g->bricks);
+    uint32_t hc[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaMemcpyAsync(b->in, d_src, (size_t)g->nx * g->ny * g->nz * elem,
+                                    cudaMemcpyDeviceToDevice, stream);
+    if (e == cudaSuccess && g->format == VT_PAYLOAD_U8)
+        e = cudaMemcpyAsync((char*)b->tmpl + L.pal, palette_host, 1024, cudaMemcpyHostToDevice,
+                            stream);
+    if (e == cudaSuccess) e = cudaGraphLaunch(b->exec, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(block, b->tmpl, L.total, cudaMemcpyDeviceToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hc, b->counts, 16, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_fail(e, "small grid build");
+    g->nonempty = (uint64_t)hc[0] + hc[1];
+    g->occupied = (uint64_t)hc[2] | ((uint64_t)hc[3] << 32);
+    g->bytes = g->block_bytes;
+    g->slots_used = g->nonempty;
+    return VT_OK;
+}
 
 int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_host,
                    uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,
@@ -172,95 +370,76 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
     g->bz = (nz + 7) / 8;
     g->bricks = (uint64_t)g->bx * g->by * g->bz;
     g->format = format;
-    const bool small = g->bricks <= kSmallGridBricks;
-    const size_t psize = format == VT_PAYLOAD_U8 ? 512 : 2048;
-    // one allocation: directory, octant words, long-box words, palette, masks, payloads
-    auto al = [](size_t v) { return (v + 255) / 256 * 256; };
-    auto allocate = [&](uint64_t slots) -> int32_t {
-        const size_t o_oct = al(g->bricks * 4), o_lng = o_oct + al(g->bricks * 4);
-        const size_t o_pal = o_lng + al(g->bricks * 12), o_msk = o_pal + 1024;
-        const size_t o_pay = o_msk + al(slots * 64), total = o_pay + al(slots * psize);
-        if (cudaMalloc(&g->block, total) != cudaSuccess) {
-            cudaGetLastError();
-            return fail(VT_ENOMEM, "cudaMalloc(brick grid) failed");
-        }
-        char* b = (char*)g->block;
-        g->block_bytes = total;
-        g->dir = (uint32_t*)b;
-        g->oct = (uint32_t*)(b + o_oct);
-        g->lng = (uint32_t*)(b + o_lng);
-        g->palette = format == VT_PAYLOAD_U8 ? (uint32_t*)(b + o_pal) : nullptr;
-        g->masks = (uint64_t*)(b + o_msk);
-        g->payload = b + o_pay;
-        g->slot_capacity = slots;
-        if (g->palette &&
-            cudaMemcpyAsync(g->palette, palette_host, 1024, cudaMemcpyHostToDevice, stream) !=
-                cudaSuccess)
-            return cuda_fail(cudaGetLastError(), "cudaMemcpy(palette)");
-        return VT_OK;
-    };
+    // u8 palettes whose only transparent entry is index 0: occupancy is "index != 0"
+    bool nonzero = format == VT_PAYLOAD_U8 && (palette_host[0] >> 24) == 0u;
+    for (int i = 1; nonzero && i < 256; ++i) nonzero = (palette_host[i] >> 24) != 0u;
     int32_t rc = VT_OK;
-    if (small && (rc = allocate(g->bricks))) {
-        g->release();
-        return rc;
+    if (g->bricks <= kSmallGridBricks) {
+        if ((rc = build_small(d_src, palette_host, nonzero, g, stream))) {
+            g->release();
+            return rc;
+        }
+        out = std::move(g);
+        return VT_OK;
     }
-    // the words kernel reads the palette from device memory: a large grid uploads it first
-    uint32_t* d_palette = g->palette;
+    // the words kernel reads the palette from device memory (scratch tail) before the grid's
+    // allocation exists: its size needs the count of occupied bricks
     void* scratch = nullptr;
-    const size_t sbytes = build_scratch_bytes(g->bricks) + (small ? 0 : 1024);
-    cudaError_t e = cudaMallocAsync(&scratch, sbytes, stream);
+    const size_t sbytes = build_scratch_bytes(g->bricks);
+    cudaError_t e = cudaMallocAsync(&scratch, sbytes + 1024, stream);
     if (e != cudaSuccess) {
-        g->release();
         cudaGetLastError();
         return fail(VT_ENOMEM, "cudaMallocAsync(brick build scratch) failed");
     }
     BuildScratch s = carve_build_scratch(scratch, g->bricks);
+    uint32_t* d_palette = (uint32_t*)((char*)scratch + sbytes);
     uint32_t counts[2] = {0, 0};
     unsigned long long occ = 0;
     do {
-        if (!small && format == VT_PAYLOAD_U8) {
-            d_palette = (uint32_t*)((char*)scratch + build_scratch_bytes(g->bricks));
+        if (format == VT_PAYLOAD_U8) {
             e = cudaMemcpyAsync(d_palette, palette_host, 1024, cudaMemcpyHostToDevice, stream);
             if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpy(palette)"); break; }
         }
-        // u8 palettes whose only transparent entry is index 0: occupancy is "index != 0"
-        bool nonzero = format == VT_PAYLOAD_U8 && (palette_host[0] >> 24) == 0u;
-        for (int i = 1; nonzero && i < 256; ++i) nonzero = (palette_host[i] >> 24) != 0u;
         e = launch_brick_words(d_src, format, d_palette, (int32_t)nx, (int32_t)ny, (int32_t)nz, s,
                                stream, nonzero);
-        if (e != cudaSuccess) { rc = cuda_fail(e, "brick words kernel"); break; }
-        e = launch_brick_scan(s, g->bricks, stream);
-        if (e != cudaSuccess) { rc = cuda_fail(e, "brick scan kernel"); break; }
-        if (!small) {  // slot arrays sized by the count of occupied bricks
+        if (e == cudaSuccess) e = launch_brick_scan(s, g->bricks, stream);
+        if (e == cudaSuccess)
             e = cudaMemcpyAsync(&counts[0], s.offsets + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(&counts[1], s.flags + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-            if (e != cudaSuccess) { rc = cuda_fail(e, "brick count readback"); break; }
-            const uint64_t nonempty = (uint64_t)counts[0] + counts[1];
-            if ((rc = allocate(nonempty ? nonempty : 1))) break;
-        }
-        e = launch_brick_compact(d_src, format, (int32_t)nx, (int32_t)ny, (int32_t)nz, s, g->dir,
-                                 g->masks, g->payload, stream);
-        if (e != cudaSuccess) { rc = cuda_fail(e, "brick compact kernel"); break; }
-        e = launch_brick_distance(s, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
-        if (e != cudaSuccess) { rc = cuda_fail(e, "brick distance kernels"); break; }
-        // the occupancy words are no longer needed: their scratch holds the octant passes
-        e = launch_brick_octants(g->dir, (uint8_t*)s.words, (uint16_t*)((uint8_t*)s.words + ((g->bricks + 255) / 256) * 256),
-                                 g->oct, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
-        if (e != cudaSuccess) { rc = cuda_fail(e, "brick octant kernels"); break; }
-        // and then the long-box runs and window minima (13 words per brick of the 16 there)
-        e = launch_brick_long(g->dir, g->oct, (uint32_t*)s.words, g->lng, (int32_t)g->bx,
-                              (int32_t)g->by, (int32_t)g->bz, stream);
-        if (e != cudaSuccess) { rc = cuda_fail(e, "brick long-box kernels"); break; }
-        e = cudaMemcpyAsync(&counts[0], s.offsets + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(&counts[1], s.flags + (g->bricks - 1), 4, cudaMemcpyDeviceToHost, stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(&occ, s.occupied, 8, cudaMemcpyDeviceToHost, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-        if (e != cudaSuccess) { rc = cuda_fail(e, "brick build"); break; }
+        if (e != cudaSuccess) { rc = cuda_fail(e, "brick count"); break; }
         g->nonempty = (uint64_t)counts[0] + counts[1];
         g->occupied = occ;
+        const uint64_t slots = g->nonempty ? g->nonempty : 1;
+        const BlockLayout L = block_layout(g->bricks, slots, format);
+        void* block = nullptr;
+        if (cudaMalloc(&block, L.total) != cudaSuccess) {
+            cudaGetLastError();
+            rc = fail(VT_ENOMEM, "cudaMalloc(brick grid) failed");
+            break;
+        }
+        point_into_block(*g, block, L, slots);
+        if (g->palette) {
+            e = cudaMemcpyAsync(g->palette, d_palette, 1024, cudaMemcpyDeviceToDevice, stream);
+            if (e != cudaSuccess) { rc = cuda_fail(e, "cudaMemcpy(palette)"); break; }
+        }
+        // compaction (from the words and slot offsets in the scratch), then the distance,
+        // octant and long-box passes: build_launches' sequence after its scan
+        e = launch_brick_compact(d_src, format, (int32_t)nx, (int32_t)ny, (int32_t)nz, s, g->dir,
+                                 g->masks, g->payload, stream);
+        if (e == cudaSuccess)
+            e = launch_brick_distance(s, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
+        if (e == cudaSuccess)
+            e = launch_brick_octants(g->dir, (uint8_t*)s.words,
+                                     (uint16_t*)((uint8_t*)s.words + ((g->bricks + 255) / 256) * 256),
+                                     g->oct, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
+        if (e == cudaSuccess)
+            e = launch_brick_long(g->dir, g->oct, (uint32_t*)s.words, g->lng, (int32_t)g->bx,
+                                  (int32_t)g->by, (int32_t)g->bz, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) { rc = cuda_fail(e, "brick build"); break; }
         g->bytes = g->block_bytes;
         g->slots_used = g->nonempty;
     } while (0);
@@ -379,6 +558,7 @@ int32_t vt_init(int32_t device) {
 void vt_shutdown(void) {
     vt_compat_release();
     vt_batch_release_all();
+    vt::release_small_builds();
     State& s = state();
     std::lock_guard<std::mutex> lk(s.mu);
     if (!s.inited) return;
