@@ -136,7 +136,14 @@ void Grid::free_slot_arrays() {
 
 void Grid::release() {
     free_slot_arrays();
-    cudaFree(block);  // directory, octant and long-box words, palette (and the first slot arrays)
+    // directory, octant and long-box words, palette (and the first slot arrays)
+    if (block && pooled) {
+        cudaDeviceSynchronize();
+        cudaFreeAsync(block, state().stream);
+    } else {
+        cudaFree(block);
+    }
+    pooled = false;
     block = nullptr;
     block_bytes = 0;
     dir = nullptr;
@@ -325,8 +332,9 @@ static int32_t small_entry(const Grid& shape, bool nonzero, SmallBuild*& out) {
     return VT_OK;
 }
 
-static int32_t build_small(const void* d_src, const uint32_t* palette_host, bool nonzero,
-                           std::unique_ptr<Grid>& g, cudaStream_t stream) {
+// `src`: the dense voxels, in device memory, or in host memory when `src_host`.
+static int32_t build_small(const void* src, bool src_host, const uint32_t* palette_host,
+                           bool nonzero, std::unique_ptr<Grid>& g, cudaStream_t stream) {
     std::lock_guard<std::mutex> lk(g_small_mu);
     SmallBuild* b = nullptr;
     int32_t rc = small_entry(*g, nonzero, b);
@@ -334,15 +342,19 @@ static int32_t build_small(const void* d_src, const uint32_t* palette_host, bool
     b->last_use = ++g_small_clock;
     const size_t elem = g->format == VT_PAYLOAD_U8 ? 1 : 4;
     const BlockLayout L = block_layout(g->bricks, g->bricks, g->format);
+    // small blocks come from the stream-ordered pool (freed after a device synchronisation, like
+    // cudaFree, so that no launch on another stream can still be reading them)
     void* block = nullptr;
-    if (cudaMalloc(&block, L.total) != cudaSuccess) {
+    if (cudaMallocAsync(&block, L.total, stream) != cudaSuccess) {
         cudaGetLastError();
-        return fail(VT_ENOMEM, "cudaMalloc(brick grid) failed");
+        return fail(VT_ENOMEM, "cudaMallocAsync(brick grid) failed");
     }
     point_into_block(*g, block, L, g->bricks);
+    g->pooled = true;
     uint32_t hc[4] = {0, 0, 0, 0};
-    cudaError_t e = cudaMemcpyAsync(b->in, d_src, (size_t)g->nx * g->ny * g->nz * elem,
-                                    cudaMemcpyDeviceToDevice, stream);
+    cudaError_t e = cudaMemcpyAsync(b->in, src, (size_t)g->nx * g->ny * g->nz * elem,
+                                    src_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                                    stream);
     if (e == cudaSuccess && g->format == VT_PAYLOAD_U8)
         e = cudaMemcpyAsync((char*)b->tmpl + L.pal, palette_host, 1024, cudaMemcpyHostToDevice,
                             stream);
@@ -358,9 +370,7 @@ static int32_t build_small(const void* d_src, const uint32_t* palette_host, bool
     return VT_OK;
 }
 
-int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_host,
-                   uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,
-                   std::unique_ptr<Grid>& out) {
+static std::unique_ptr<Grid> grid_shell(uint32_t format, uint32_t nx, uint32_t ny, uint32_t nz) {
     std::unique_ptr<Grid> g(new Grid());
     g->nx = nx;
     g->ny = ny;
@@ -370,12 +380,42 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
     g->bz = (nz + 7) / 8;
     g->bricks = (uint64_t)g->bx * g->by * g->bz;
     g->format = format;
-    // u8 palettes whose only transparent entry is index 0: occupancy is "index != 0"
+    return g;
+}
+
+// u8 palettes whose only transparent entry is index 0: occupancy is "index != 0"
+static bool nonzero_palette(uint32_t format, const uint32_t* palette_host) {
     bool nonzero = format == VT_PAYLOAD_U8 && (palette_host[0] >> 24) == 0u;
     for (int i = 1; nonzero && i < 256; ++i) nonzero = (palette_host[i] >> 24) != 0u;
+    return nonzero;
+}
+
+bool small_grid(uint32_t nx, uint32_t ny, uint32_t nz) {
+    return (uint64_t)((nx + 7) / 8) * ((ny + 7) / 8) * ((nz + 7) / 8) <= kSmallGridBricks;
+}
+
+int32_t build_small_from_host(const void* voxels, uint32_t format, const uint32_t* palette_host,
+                              uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,
+                              std::unique_ptr<Grid>& out) {
+    std::unique_ptr<Grid> g = grid_shell(format, nx, ny, nz);
+    const int32_t rc = build_small(voxels, true, palette_host, nonzero_palette(format, palette_host),
+                                   g, stream);
+    if (rc) {
+        g->release();
+        return rc;
+    }
+    out = std::move(g);
+    return VT_OK;
+}
+
+int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_host,
+                   uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,
+                   std::unique_ptr<Grid>& out) {
+    std::unique_ptr<Grid> g = grid_shell(format, nx, ny, nz);
+    const bool nonzero = nonzero_palette(format, palette_host);
     int32_t rc = VT_OK;
     if (g->bricks <= kSmallGridBricks) {
-        if ((rc = build_small(d_src, palette_host, nonzero, g, stream))) {
+        if ((rc = build_small(d_src, false, palette_host, nonzero, g, stream))) {
             g->release();
             return rc;
         }
@@ -660,6 +700,11 @@ static int32_t create_from_host(const void* data, size_t elem, uint32_t format, 
     const size_t bytes = (size_t)nx * ny * nz * elem;
     const int nbuf = order == VT_ORDER_Z_FASTEST ? 2 : 1;
     cudaStream_t st = state().stream;
+    if (order == VT_ORDER_X_FASTEST && small_grid(nx, ny, nz)) {  // straight into the build graph's input
+        std::unique_ptr<Grid> g;
+        if ((rc = build_small_from_host(data, format, palette, nx, ny, nz, st, g))) return rc;
+        return register_grid(std::move(g));
+    }
     void* d = nullptr;
     if (cudaMallocAsync(&d, bytes * nbuf, st) != cudaSuccess) {
         cudaGetLastError();

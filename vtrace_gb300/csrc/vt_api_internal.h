@@ -36,6 +36,7 @@ struct Grid {
     // grows the slots into separate allocations
     void* block = nullptr;
     size_t block_bytes = 0;
+    bool pooled = false;  // `block` comes from the stream-ordered pool
     size_t bytes = 0;
     // slots of masks/payload: allocated, handed out (high-water mark), and freed by updates
     uint64_t slot_capacity = 0, slots_used = 0;
