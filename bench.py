@@ -652,7 +652,8 @@ def run_config(args):
         ww, hh = ctypes.c_int32(0), ctypes.c_int32(0)
         lib_stream = torch.cuda.ExternalStream(L.vt_get_stream())
         tick = lambda: vt.check(L.render_tick(ctypes.byref(ww), ctypes.byref(hh), ctypes.byref(info)))
-        # device time of the frame's launches (binning + per-pixel kernel) on the library stream
+        # device time of the frame's launches (instance records, binning, per-pixel kernel) on the
+        # library stream
         ms = autotune.time_ms(tick, lib_stream, repeats=args.steps, warmup=args.warmup, flush=flush)
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -670,7 +671,8 @@ def run_config(args):
                     e2e={"value": px / e2e_ms / 1e3, "unit": "Mpixels/s",
                          "h2d_bytes_per_step": int(insts.nbytes) + 128, "d2h_bytes_per_step": 0,
                          "path": "render_tick (C ABI), host wall clock"},
-                    gpu_launches=2 * args.steps)
+                    # instance records, tile binning, per-pixel compositing
+                    gpu_launches=3 * args.steps)
         if not args.no_cpu_baseline:
             from oracle import pyoracle as po
             grids = [po.Grid(texels=t) for t in world["textures"]]

@@ -497,6 +497,7 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
 int32_t register_grid(std::unique_ptr<Grid> g) {
     State& s = state();
     std::lock_guard<std::mutex> lk(s.mu);
+    s.grid_epoch.fetch_add(1);
     for (size_t i = 0; i < s.grids.size(); ++i)
         if (!s.grids[i]) {
             s.grids[i] = std::move(g);
@@ -759,6 +760,7 @@ int32_t vt_grid_destroy(int32_t grid) {
     cudaStreamSynchronize(s.stream);
     s.grids[grid]->release();
     s.grids[grid].reset();
+    s.grid_epoch.fetch_add(1);
     return VT_OK;
 }
 

@@ -60,6 +60,8 @@ struct State {
     cudaStream_t aux[kAux] = {nullptr, nullptr};
     cudaEvent_t aux_start = nullptr;
     std::vector<std::unique_ptr<Grid>> grids;
+    // bumped whenever a grid is created, destroyed or changed in place (its device views change)
+    std::atomic<uint64_t> grid_epoch{0};
     void* staging = nullptr;
     size_t staging_bytes = 0;
     // work counters of the persistent launches: each launch takes the next slot of the ring

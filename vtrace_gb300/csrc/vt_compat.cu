@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(128) compat_kernel(const GridView* __restrict_
     InstanceCursor cur(bins, ninst, words, (int32_t)((blockIdx.y >> 1) * gridDim.x + blockIdx.x));
     for (int32_t i = cur.next(); i >= 0; i = cur.next()) {
         const CompatInstance& I = inst[i];
+        if (I.texture < 0) continue;  // draws nothing (only reached without bins)
         const GridView g = views[I.texture];
         float om[3], dm[3];
 #pragma unroll
@@ -224,6 +225,8 @@ struct Compat {
     bool mapped = false;
     GridView* d_views = nullptr;
     uint32_t views_capacity = 0;
+    uint32_t views_count = 0;     // texture views on the device, as of grid-table epoch:
+    uint64_t views_epoch = ~0ull;  // re-uploaded only when textures or grids change
     CompatInstance* d_inst = nullptr;
     uint32_t inst_capacity = 0;
     uint32_t* d_bins = nullptr;  // per-tile instance bitmasks
@@ -242,8 +245,9 @@ static uint32_t round_up_p2(uint32_t x) {
     return r;
 }
 
-// 4x4 inverse in double (cofactor expansion), column-major in and out.
-static bool invert4(const double* m, double* inv) {
+// 4x4 inverse in double (cofactor expansion), column-major in and out.  Host and device builds
+// evaluate it identically (IEEE binary64, no contraction).
+static __host__ __device__ bool invert4(const double* m, double* inv) {
     double a[16];
     memcpy(a, m, sizeof(a));
     double r[16];
@@ -346,8 +350,9 @@ static CullFrame cull_frame(const double* dm, const double* cam, int32_t width, 
 
 // Tile rectangle of an instance (model matrix md, column-major; its inverse mi).  Returns false
 // when no pixel can see it.
-static bool instance_tiles(const CullFrame& cf, const double* md, const double* mi, int32_t& tx0,
-                           int32_t& ty0, int32_t& tx1, int32_t& ty1) {
+static __host__ __device__ bool instance_tiles(const CullFrame& cf, const double* md,
+                                               const double* mi, int32_t& tx0, int32_t& ty0,
+                                               int32_t& tx1, int32_t& ty1) {
     const int32_t ntx = (cf.width + kTile - 1) / kTile, nty = (cf.height + kTile - 1) / kTile;
     tx0 = 0;
     ty0 = 0;
@@ -412,6 +417,51 @@ static bool instance_tiles(const CullFrame& cf, const double* md, const double* 
     ty0 = (int32_t)(fmax(py0, 0.0) / kTile);
     ty1 = (int32_t)(fmin(py1, cf.height - 1.0) / kTile);
     return true;
+}
+
+// Device records of the instances (trace.vert:38-40: the texture id in the bits of element
+// [3][3], which reads as 1): inverse model matrix and tile rectangle, one thread per instance,
+// in draw order.  Instances with an unbound texture id or a singular matrix draw nothing
+// (texture -1, empty rectangle).
+__global__ void __launch_bounds__(128) compat_prepare_kernel(const float* __restrict__ insts,
+                                                             uint32_t n, uint32_t ntex, CullFrame cf,
+                                                             CompatInstance* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4* m4 = reinterpret_cast<const float4*>(insts + 16 * (size_t)i);
+    float m[16];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float4 v = m4[k];
+        m[4 * k] = v.x;
+        m[4 * k + 1] = v.y;
+        m[4 * k + 2] = v.z;
+        m[4 * k + 3] = v.w;
+    }
+    const int32_t tid = __float_as_int(m[15]);
+    CompatInstance ci;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) ci.minv[k] = 0.0f;
+    ci.texture = -1;
+    ci.tx0 = ci.ty0 = 1;  // empty rectangle: in no tile
+    ci.tx1 = ci.ty1 = 0;
+    ci.pad[0] = ci.pad[1] = 0;
+    if (tid >= 0 && (uint32_t)tid < ntex) {
+        double md[16], mi[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) md[k] = m[k];
+        md[15] = 1.0;
+        if (invert4(md, mi)) {
+            for (int r = 0; r < 3; ++r)
+                for (int k = 0; k < 4; ++k) ci.minv[4 * r + k] = (float)mi[k * 4 + r];
+            ci.texture = tid;
+            if (!instance_tiles(cf, md, mi, ci.tx0, ci.ty0, ci.tx1, ci.ty1)) {
+                ci.tx0 = ci.ty0 = 1;
+                ci.tx1 = ci.ty1 = 0;
+            }
+        }
+    }
+    out[i] = ci;
 }
 
 static int32_t compat_upload_tables() {
@@ -551,60 +601,47 @@ int32_t render_tick(int32_t* window_width, int32_t* window_height, const render_
     f.height = c.height;
     const CullFrame cf = cull_frame(dm, ic + 12, c.width, c.height);
 
-    // instances -> device records (texture id in the bits of element [3][3], trace.vert:38-40)
-    std::vector<CompatInstance> recs;
-    recs.reserve(c.count);
-    const uint32_t ntex = (uint32_t)c.textures.size();
-    for (uint32_t i = 0; i < c.count; ++i) {
-        const float* m = c.host_instances + 16 * i;
-        int32_t tid;
-        memcpy(&tid, &m[15], 4);
-        if (tid < 0 || (uint32_t)tid >= ntex) continue;  // unbound descriptor: nothing drawn
-        double md[16], mi[16];
-        for (int k = 0; k < 16; ++k) md[k] = m[k];
-        md[15] = 1.0;
-        if (!invert4(md, mi)) continue;
-        CompatInstance ci;
-        memset(&ci, 0, sizeof(ci));
-        for (int r = 0; r < 3; ++r)
-            for (int k = 0; k < 4; ++k) ci.minv[4 * r + k] = (float)mi[k * 4 + r];
-        ci.texture = tid;
-        if (!instance_tiles(cf, md, mi, ci.tx0, ci.ty0, ci.tx1, ci.ty1)) {
-            ci.tx0 = 1;  // empty rectangle: in no tile
-            ci.tx1 = 0;
-        }
-        recs.push_back(ci);
-    }
     cudaStream_t st = state().stream;
-    if (ntex > c.views_capacity) {
-        cudaFree(c.d_views);
-        c.views_capacity = round_up_p2(ntex);
-        if (cudaMalloc(&c.d_views, (size_t)c.views_capacity * sizeof(GridView)) != cudaSuccess) {
-            c.views_capacity = 0;
-            return -1;
+    const uint32_t ntex = (uint32_t)c.textures.size();
+    const uint64_t epoch = state().grid_epoch.load();
+    if (ntex != c.views_count || epoch != c.views_epoch) {  // texture views, when they changed
+        if (ntex > c.views_capacity) {
+            cudaFree(c.d_views);
+            c.views_capacity = round_up_p2(ntex);
+            if (cudaMalloc(&c.d_views, (size_t)c.views_capacity * sizeof(GridView)) != cudaSuccess) {
+                c.views_capacity = 0;
+                return -1;
+            }
         }
+        std::vector<GridView> views(ntex);
+        for (uint32_t t = 0; t < ntex; ++t) {
+            Grid* g = lookup_grid(c.textures[t]);
+            if (!g) return -1;
+            views[t] = g->view();
+        }
+        if (ntex && (cudaMemcpyAsync(c.d_views, views.data(), ntex * sizeof(GridView),
+                                     cudaMemcpyHostToDevice, st) != cudaSuccess ||
+                     cudaStreamSynchronize(st) != cudaSuccess))
+            return -1;
+        c.views_count = ntex;
+        c.views_epoch = epoch;
     }
-    if (recs.size() > c.inst_capacity) {
+    // instance records on the device, from the pinned instance buffer the GPU reads directly
+    const uint32_t n = c.count;
+    if (n > c.inst_capacity) {
         cudaFree(c.d_inst);
-        c.inst_capacity = round_up_p2((uint32_t)recs.size());
+        c.inst_capacity = round_up_p2(n);
         if (cudaMalloc(&c.d_inst, (size_t)c.inst_capacity * sizeof(CompatInstance)) != cudaSuccess) {
             c.inst_capacity = 0;
             return -1;
         }
     }
-    std::vector<GridView> views(ntex);
-    for (uint32_t t = 0; t < ntex; ++t) {
-        Grid* g = lookup_grid(c.textures[t]);
-        if (!g) return -1;
-        views[t] = g->view();
-    }
-    cudaError_t e = cudaSuccess;
-    if (ntex) e = cudaMemcpyAsync(c.d_views, views.data(), ntex * sizeof(GridView), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && !recs.empty())
-        e = cudaMemcpyAsync(c.d_inst, recs.data(), recs.size() * sizeof(CompatInstance), cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return -1;
+    const float* d_src = (const float*)host_mapped(c.host_instances);
+    if (n && !d_src) return -1;
+    if (n)
+        compat_prepare_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_src, n, ntex, cf, c.d_inst);
     dim3 grid((c.width + kTile - 1) / kTile, (c.height + kTile - 1) / kTile);
-    const int32_t ninst = (int32_t)recs.size();
+    const int32_t ninst = (int32_t)n;
     const int32_t words = (ninst + 31) / 32, ntiles = (int32_t)(grid.x * grid.y);
     const size_t bin_bytes = (size_t)ntiles * words * 4;
     uint32_t* bins = nullptr;
@@ -624,7 +661,7 @@ int32_t render_tick(int32_t* window_width, int32_t* window_height, const render_
     const dim3 pgrid(grid.x, (c.height + 7) / 8);
     compat_kernel<<<pgrid, 128, 0, st>>>(c.d_views, c.d_inst, ninst, bins, words, f, c.fb);
     if (cudaGetLastError() != cudaSuccess) return -1;
-    // the host vectors above are staged by the copies: wait before they go out of scope
+    // the frame is complete when render_tick returns (the instance buffer may then change)
     if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
     if (window_width) *window_width = c.width;
     if (window_height) *window_height = c.height;

@@ -149,6 +149,7 @@ static int32_t grow_slots(Grid& g, uint64_t need, cudaStream_t st) {
     g.free_slot_arrays();
     g.masks = m;
     g.payload = p;
+    state().grid_epoch.fetch_add(1);  // the grid's device view changed
     g.slot_capacity = cap;
     return VT_OK;
 }
