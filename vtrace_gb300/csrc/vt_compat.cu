@@ -229,6 +229,8 @@ struct Compat {
     uint64_t views_epoch = ~0ull;  // re-uploaded only when textures or grids change
     CompatInstance* d_inst = nullptr;
     uint32_t inst_capacity = 0;
+    float* d_raw = nullptr;  // device copy of the instance matrices, where pinned memory is not
+    uint32_t raw_capacity = 0;  // addressable from the device
     uint32_t* d_bins = nullptr;  // per-tile instance bitmasks
     size_t bins_capacity = 0;
     user_input input;
@@ -479,6 +481,7 @@ static void compat_release_locked(Compat& c) {
     cudaFree(c.fb);
     cudaFree(c.d_views);
     cudaFree(c.d_inst);
+    cudaFree(c.d_raw);
     cudaFree(c.d_bins);
     cudaFreeHost(c.host_instances);
     for (int32_t g : c.textures) vt_grid_destroy(g);
@@ -486,10 +489,14 @@ static void compat_release_locked(Compat& c) {
     c.fb = nullptr;
     c.d_views = nullptr;
     c.d_inst = nullptr;
+    c.d_raw = nullptr;
+    c.raw_capacity = 0;
     c.d_bins = nullptr;
     c.bins_capacity = 0;
     c.host_instances = nullptr;
     c.capacity = c.count = c.views_capacity = c.inst_capacity = 0;
+    c.views_count = 0;
+    c.views_epoch = ~0ull;
     c.mapped = false;
     c.inited = false;
 }
@@ -637,7 +644,20 @@ int32_t render_tick(int32_t* window_width, int32_t* window_height, const render_
         }
     }
     const float* d_src = (const float*)host_mapped(c.host_instances);
-    if (n && !d_src) return -1;
+    if (n && !d_src) {  // not addressable from the device here: copy the matrices over
+        if (n > c.raw_capacity) {
+            cudaFree(c.d_raw);
+            c.raw_capacity = round_up_p2(n);
+            if (cudaMalloc(&c.d_raw, (size_t)c.raw_capacity * 16 * sizeof(float)) != cudaSuccess) {
+                c.raw_capacity = 0;
+                return -1;
+            }
+        }
+        if (cudaMemcpyAsync(c.d_raw, c.host_instances, (size_t)n * 16 * sizeof(float),
+                            cudaMemcpyHostToDevice, st) != cudaSuccess)
+            return -1;
+        d_src = c.d_raw;
+    }
     if (n)
         compat_prepare_kernel<<<(n + 127) / 128, 128, 0, st>>>(d_src, n, ntex, cf, c.d_inst);
     dim3 grid((c.width + kTile - 1) / kTile, (c.height + kTile - 1) / kTile);
