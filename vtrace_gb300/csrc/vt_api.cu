@@ -162,7 +162,6 @@ int32_t check_dims(uint32_t nx, uint32_t ny, uint32_t nz) {
     return VT_OK;
 }
 
-// Builds the brick layout of a dense device grid on `stream` and waits for it.
 // One device allocation per grid: directory, octant words, long-box words, palette, masks and
 // payloads of `slots` slots, each part 256-byte aligned.
 struct BlockLayout {
@@ -390,13 +389,13 @@ static bool nonzero_palette(uint32_t format, const uint32_t* palette_host) {
     return nonzero;
 }
 
-bool small_grid(uint32_t nx, uint32_t ny, uint32_t nz) {
+static bool small_grid(uint32_t nx, uint32_t ny, uint32_t nz) {
     return (uint64_t)((nx + 7) / 8) * ((ny + 7) / 8) * ((nz + 7) / 8) <= kSmallGridBricks;
 }
 
-int32_t build_small_from_host(const void* voxels, uint32_t format, const uint32_t* palette_host,
-                              uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,
-                              std::unique_ptr<Grid>& out) {
+static int32_t build_small_from_host(const void* voxels, uint32_t format,
+                                     const uint32_t* palette_host, uint32_t nx, uint32_t ny,
+                                     uint32_t nz, cudaStream_t stream, std::unique_ptr<Grid>& out) {
     std::unique_ptr<Grid> g = grid_shell(format, nx, ny, nz);
     const int32_t rc = build_small(voxels, true, palette_host, nonzero_palette(format, palette_host),
                                    g, stream);
@@ -408,6 +407,7 @@ int32_t build_small_from_host(const void* voxels, uint32_t format, const uint32_
     return VT_OK;
 }
 
+// Builds the brick layout of a dense device grid on `stream` and waits for it.
 int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_host,
                    uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,
                    std::unique_ptr<Grid>& out) {
