@@ -56,9 +56,10 @@ struct State {
     int32_t sm_count = 0;
     cudaStream_t stream = nullptr;
     // helper streams of the host-buffer calls: copies of one band overlap the next band's work
-    static constexpr int kAux = 2;
-    cudaStream_t aux[kAux] = {nullptr, nullptr};
+    static constexpr int kAux = 4;
+    cudaStream_t aux[kAux] = {nullptr, nullptr, nullptr, nullptr};
     cudaEvent_t aux_start = nullptr;
+    std::vector<cudaEvent_t> chunk_events;  // ordering of the pipelined host-buffer pieces
     std::vector<std::unique_ptr<Grid>> grids;
     // bumped whenever a grid is created, destroyed or changed in place (its device views change)
     std::atomic<uint64_t> grid_epoch{0};
