@@ -96,6 +96,7 @@ struct ServeReq {
     uint64_t samples = 0;
     void* d_samples = nullptr;
     void* d_image = nullptr;
+    void* h_image = nullptr;  // device address of a page-locked host_rgba, written directly
 };
 
 struct Slot {
@@ -200,8 +201,11 @@ void Service::launch(Slot& slot, const std::vector<uint64_t>& ids) {
         const vt_serve_request& r = q.r;
         const uint64_t px = (uint64_t)r.camera.width * r.camera.height;
         Grid* g = lookup_grid(scenes[r.scene]->grid);
+        // a page-locked output is written by the resolve kernel itself; else a device image and
+        // a copy
+        q.h_image = host_mapped(r.host_rgba);
         cudaError_t e = cudaMallocAsync(&q.d_samples, px * r.spp * 16, slot.stream);
-        if (e == cudaSuccess) e = cudaMallocAsync(&q.d_image, px * 4, slot.stream);
+        if (e == cudaSuccess && !q.h_image) e = cudaMallocAsync(&q.d_image, px * 4, slot.stream);
         if (e != cudaSuccess || !g) {
             cudaGetLastError();
             if (q.d_samples) cudaFreeAsync(q.d_samples, slot.stream);
@@ -213,7 +217,7 @@ void Service::launch(Slot& slot, const std::vector<uint64_t>& ids) {
         slot.h_table[n] = make_batch_view(*g, r.camera, (r.flags & VT_VIEW_LIGHT) ? &r.light : nullptr,
                                           r.spp, r.seed, r.view_id, q.d_samples, item);
         slot.h_resolve[n].samples = (const uint4*)q.d_samples;
-        slot.h_resolve[n].image = (uchar4*)q.d_image;
+        slot.h_resolve[n].image = (uchar4*)(q.h_image ? q.h_image : q.d_image);
         slot.h_resolve[n].pixel_begin = pixel;
         slot.h_resolve[n].pixels = (uint32_t)px;
         slot.h_resolve[n].spp = r.spp;
@@ -235,15 +239,19 @@ void Service::launch(Slot& slot, const std::vector<uint64_t>& ids) {
                     cudaMemcpyHostToDevice, slot.stream);
     launch_batch(slot.d_table, n, item, slot.d_counter, tune, batch_blocks(n, item, tune),
                  slot.stream);
-    const unsigned rblocks = (unsigned)std::min<uint64_t>((pixel + 255) / 256, 152 * 16);
+    const unsigned rblocks =
+        (unsigned)std::min<uint64_t>((pixel + 255) / 256, (uint64_t)state().sm_count * 16);
     resolve_kernel<<<rblocks, 256, 0, slot.stream>>>(slot.d_resolve, n, pixel);
     for (uint64_t id : live) {
         ServeReq& q = reqs[id];
         const uint64_t px = (uint64_t)q.r.camera.width * q.r.camera.height;
-        cudaMemcpyAsync(q.r.host_rgba, q.d_image, px * 4, cudaMemcpyDeviceToHost, slot.stream);
+        if (!q.h_image) {
+            cudaMemcpyAsync(q.r.host_rgba, q.d_image, px * 4, cudaMemcpyDeviceToHost, slot.stream);
+            cudaFreeAsync(q.d_image, slot.stream);
+        }
         cudaFreeAsync(q.d_samples, slot.stream);
-        cudaFreeAsync(q.d_image, slot.stream);
         q.d_samples = q.d_image = nullptr;
+        q.h_image = nullptr;
     }
     cudaEventRecord(slot.done, slot.stream);
     slot.busy = true;
