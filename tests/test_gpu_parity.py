@@ -334,6 +334,43 @@ def expected_long(directory, octants, dims, cap=15):
     return out
 
 
+def test_small_grid_builds_across_many_shapes(torch):
+    """Grids of up to 512 bricks build from a CUDA graph captured per shape, at most 64 shapes
+    kept: 72 shapes (u8 and RGBA8) force evictions and re-captures; every grid's directory,
+    masks, octant and long-box words equal the brute-force restatement, and rays agree with the
+    oracle."""
+    rng = np.random.default_rng(21)
+    pal = vt.gen_palette(2)
+    shapes = [(9 + i % 8 * 5, 12 + (i // 8) % 9 * 4, 10 + i % 5) for i in range(72)]
+    for rep in range(2):  # the second pass rebuilds shapes whose graphs were evicted
+        for i, dims in enumerate(shapes[::9] if rep else shapes):
+            nx, ny, nz = dims
+            vox = np.where(rng.random((nz, ny, nx)) < 0.04,
+                           rng.integers(1, 256, (nz, ny, nx)), 0).astype(np.uint8)
+            if i % 2:
+                g = vt.Grid.from_rgba8(pal[vox])
+                palette = None
+            else:
+                g = vt.Grid.from_u8(vox, pal)
+                palette = pal
+            try:
+                d, m = g.bricks()
+                wd, wm, _ = expected_bricks(vox, pal)
+                np.testing.assert_array_equal(d, wd)
+                full = np.nonzero((d >> 31) == 0)[0]
+                np.testing.assert_array_equal(m[d[full]], wm[wd[full]])
+                oc = g.octants()
+                np.testing.assert_array_equal(oc, expected_octants(d, dims))
+                np.testing.assert_array_equal(g.long_boxes(), expected_long(d, oc, dims))
+                if i % 12 == 0:
+                    rays = vt.gen_rays_uniform(dims, i + 1, 3000)
+                    hits, _, _ = device_trace(torch, g, rays)
+                    og = po.Grid(vox, pal) if palette is not None else po.Grid(texels=pal[vox])
+                    assert_hits_equal(hits, po.trace_rays(og, rays), "shape %r" % (dims,))
+            finally:
+                g.destroy()
+
+
 def special_rays(rng, dims, n):
     """Axis-parallel, planar, exact-diagonal and grazing rays from inside and outside."""
     size = np.array(dims, np.float32)
