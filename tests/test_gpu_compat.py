@@ -83,6 +83,7 @@ def test_reference_call_sequence(lib):
         instance(-20, (0, 0, 1), (6, 6, 6), (-3, 1, -12), 0),
         instance(0, (0, 1, 0), (1, 1, 1), (0, 0, -3), 7),        # unbound texture: not drawn
         instance(0, (0, 1, 0), (50, 50, 50), (0, 0, 0), 1),      # camera inside: culled
+        instance(0, (0, 1, 0), (0, 4, 4), (1, 0, -5), 0),         # singular matrix: not drawn
     ])
     ptr = L.start_update_instances(len(insts))
     assert ptr
