@@ -121,8 +121,9 @@ struct InstanceCursor {
     }
 };
 
-// Blocks of 128 threads cover 16 x 8 pixels, two per 16 x 16 binning tile.
-__global__ void __launch_bounds__(128) compat_kernel(const GridView* __restrict__ views,
+// Blocks of 128 threads cover 16 x 8 pixels, two per 16 x 16 binning tile.  8 blocks per SM
+// (64 registers instead of 72): 3-7% shorter ticks on the pager world.
+__global__ void __launch_bounds__(128, 8) compat_kernel(const GridView* __restrict__ views,
                                                      const CompatInstance* __restrict__ inst,
                                                      int32_t ninst, const uint32_t* __restrict__ bins,
                                                      int32_t words, CompatFrame f,
