@@ -170,7 +170,16 @@ typedef struct vt_tuning {
                            a compacted queue instead of in the primary ray's thread.
                            VT_KERNEL_PATH: advance all paths one vertex at a time through ray
                            queues (the default; faster than either per-path form) */
+    uint32_t tile_shape;  /* VT_KERNEL_RENDER fused tile launch: the pixels of one warp, VT_TILE_* */
+    uint32_t block_warps; /* VT_KERNEL_RENDER fused tile launch: warps per block, 1, 2, 4 or 8
+                             (0 = 4); the block's warp tiles are arranged about twice as wide as
+                             high */
 } vt_tuning;
+
+#define VT_TILE_8X4 0u  /* 8 pixels wide, 4 high (the default) */
+#define VT_TILE_4X8 1u
+#define VT_TILE_16X2 2u
+#define VT_TILE_32X1 3u
 
 #define VT_KERNEL_RENDER 1
 #define VT_KERNEL_TRACE_RAYS 2
@@ -334,8 +343,9 @@ int32_t vt_path_trace_host(int32_t grid, const vt_camera* camera, const vt_path_
 /* One view of a batch: a camera over a grid with `spp` jittered samples per pixel.  Sample s of
  * pixel (px, py) uses the sub-pixel offset Philox4x32-10(counter = {px, py, s, view_id},
  * key = {seed, 0x56544752}) words 0 and 1, each >> 8 and scaled by 2^-24, and is written to
- * d_out[(py * width + px) * spp + s] (device memory, 16-byte aligned; width * height * spp below
- * 2^32, else VT_ELIMIT).  The light is used when flags & VT_VIEW_LIGHT. */
+ * d_out[(py * width + px) * spp + s] (device memory, or page-locked host memory that the kernel
+ * writes over the host link; 16-byte aligned; width * height * spp below 2^32, else VT_ELIMIT;
+ * other host memory is refused with VT_EINVAL).  The light is used when flags & VT_VIEW_LIGHT. */
 typedef struct vt_view {
     int32_t grid;
     uint32_t spp;
@@ -360,6 +370,10 @@ int32_t vt_batch_run(int32_t batch, void* stream);
 int32_t vt_batch_run_direct(int32_t batch, void* stream);
 /* Primary rays (sum of width * height * spp) and work items of a batch. */
 int32_t vt_batch_info(int32_t batch, uint64_t* primary_rays, uint64_t* work_items);
+/* Counting run of a batch (no counterpart in the reference): the same records through a slower
+ * kernel build that walks every reference iteration, plus its traversal counters (for roofline
+ * accounting, not for timing).  Synchronous on the library stream. */
+int32_t vt_batch_stats(int32_t batch, vt_trace_stats* stats);
 int32_t vt_batch_destroy(int32_t batch);
 
 /* ---------------------------------------------------------------- serving */
@@ -405,6 +419,9 @@ typedef struct vt_serve_timing {
 typedef struct vt_serve_stats {
     uint64_t submitted, completed, launches, views_launched, samples;
     uint64_t scene_loads, evictions, resident_bytes, pending;
+    uint64_t device_ns; /* summed device time of the finished launches (kernels, resolves and
+                           copies, timed by events on their streams); with max_inflight 1 the
+                           launches never overlap and this is the time the GPU was busy */
 } vt_serve_stats;
 
 int32_t vt_serve_default_config(vt_serve_config* cfg);

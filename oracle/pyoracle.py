@@ -86,6 +86,8 @@ def lib():
         L.vto_raygen.argtypes = [ctypes.POINTER(Camera), u32, u32, ctypes.c_float,
                                  ctypes.c_float, vp, vp]
         L.vto_hardware_threads.restype = ctypes.c_int
+        L.vto_frame_rays.argtypes = [ctypes.POINTER(Camera), ctypes.POINTER(Light), vp, vp, vp]
+        L.vto_frame_rays.restype = u64
         _lib = L
     return _lib
 
@@ -203,6 +205,19 @@ def philox(ctr, key):
     o = np.zeros(4, dtype=np.uint32)
     lib().vto_philox4x32_10(_ptr(c), _ptr(k), _ptr(o))
     return o
+
+
+def frame_rays(camera, light, hits):
+    """The camera ray of every pixel and the shadow ray of every record of `hits` (the frame's
+    records, [height, width] or flat) that traced one, as [n, 6] float32 ray buffers."""
+    hits = np.ascontiguousarray(hits).reshape(-1)
+    npx = camera.width * camera.height
+    assert hits.shape[0] == npx and hits.dtype.itemsize == 16
+    cam_rays = np.zeros((npx, 6), np.float32)
+    sh_rays = np.zeros((npx, 6), np.float32)
+    ns = lib().vto_frame_rays(ctypes.byref(camera), ctypes.byref(light) if light is not None else None,
+                              _ptr(hits), _ptr(cam_rays), _ptr(sh_rays))
+    return cam_rays, sh_rays[:ns].copy()
 
 
 def raygen(camera, px, py, jx=0.5, jy=0.5):

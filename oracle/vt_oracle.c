@@ -411,6 +411,32 @@ void vto_shade_sample(const vto_grid* g, const vto_camera* cam, const vto_light*
     shade_from_ray(g, light, o, d, out, stats);
 }
 
+/* The shadow-ray origin below is shade_from_ray's, from the record's voxel, face and t. */
+uint64_t vto_frame_rays(const vto_camera* cam, const vto_light* light, const vto_hit* hits,
+                        float* camera_rays, float* shadow_rays) {
+    uint64_t ns = 0;
+    for (uint32_t py = 0; py < cam->height; ++py) {
+        for (uint32_t px = 0; px < cam->width; ++px) {
+            const uint64_t p = (uint64_t)py * cam->width + px;
+            float* r = camera_rays + 6 * p;
+            vto_raygen(cam, px, py, 0.5f, 0.5f, r, r + 3);
+            const vto_hit* h = &hits[p];
+            if (!light || !(h->face & VTO_FLAG_SHADOW_RAY)) continue;
+            const int face = h->face & 7;
+            const int a = (face - 1) / 2;
+            const int npos = (face & 1) != 0;
+            const int32_t hv[3] = {h->x, h->y, h->z};
+            const float plane = (float)(npos ? hv[a] + 1 : hv[a]);
+            float* s = shadow_rays + 6 * ns;
+            for (int b = 0; b < 3; ++b) s[b] = r[b] + h->t * r[3 + b];
+            s[a] = npos ? plane + 0.015625f : plane - 0.015625f;
+            for (int b = 0; b < 3; ++b) s[3 + b] = light->dir[b];
+            ++ns;
+        }
+    }
+    return ns;
+}
+
 /* ------------------------------------------------------------------ path tracing */
 
 /* The library's path-tracing estimator (vt_path.cu's header states it; vtrace itself has none). */

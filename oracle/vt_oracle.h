@@ -150,6 +150,13 @@ void vto_trace_rays(const vto_grid* g, const float* rays, uint64_t n, vto_hit* h
 /* binary64 traversal of a ray buffer (for t accuracy and tie-divergence statistics). */
 void vto_trace_rays_f64(const vto_grid* g, const float* rays, uint64_t n, vto_hit64* hits,
                         int threads);
+/* The rays of a rendered frame as ray-buffer entries (6 floats each): the camera ray of every
+ * pixel (pixel centres, row-major from the top row) into camera_rays, and, for every record of
+ * `hits` (the frame's width * height records) that carries VTO_FLAG_SHADOW_RAY, the shadow ray
+ * shade_from_ray traced for it, in pixel order, into shadow_rays (capacity width * height).
+ * Returns the number of shadow rays written. */
+uint64_t vto_frame_rays(const vto_camera* cam, const vto_light* light, const vto_hit* hits,
+                        float* camera_rays, float* shadow_rays);
 
 /* The reference's multi-instance frame as libvtrace's headless render_tick computes it: RGBA8
  * sRGB pixels, row-major from the top row.  instances: n column-major mat4 (texture id in the bits

@@ -439,7 +439,7 @@ def test_launch_shapes_agree(torch, persistent, refill_min, wavefront):
         assert_hits_equal(hits, po.trace_rays(og, rays), "rays persistent=%d" % persistent)
     finally:
         for k, t in saved.items():
-            vt.set_tuning(k, t["refill_min"], t["blocks_per_sm"], t["persistent"], t["wavefront"])
+            vt.set_tuning(k, **t)
         g.destroy()
 
 
@@ -476,8 +476,7 @@ def test_batched_multiview_matches_oracle(torch, refill):
         assert b.primary_rays == sum(v["camera"].width * v["camera"].height * v["spp"] for v in views)
         b.destroy()
     finally:
-        vt.set_tuning(vt.KERNEL_BATCH, saved["refill_min"], saved["blocks_per_sm"], saved["persistent"],
-                      saved["wavefront"])
+        vt.set_tuning(vt.KERNEL_BATCH, **saved)
         for g in grids:
             if g.id is not None:
                 g.destroy()
@@ -515,8 +514,7 @@ def test_batch_of_the_most_views(torch, refill):
             assert_hits_equal(hits_from_dev(o), want, "view %d" % i)
         b.destroy()
     finally:
-        vt.set_tuning(vt.KERNEL_BATCH, saved["refill_min"], saved["blocks_per_sm"], saved["persistent"],
-                      saved["wavefront"])
+        vt.set_tuning(vt.KERNEL_BATCH, **saved)
         for g in grids:
             g.destroy()
 

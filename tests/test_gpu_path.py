@@ -31,8 +31,7 @@ def form(request, torch):
     saved = vt.get_tuning(vt.KERNEL_PATH)
     vt.set_tuning(vt.KERNEL_PATH, request.param[1], 0, bool(request.param[0]), bool(request.param[2]))
     yield request.param
-    vt.set_tuning(vt.KERNEL_PATH, saved["refill_min"], saved["blocks_per_sm"], saved["persistent"],
-                  saved["wavefront"])
+    vt.set_tuning(vt.KERNEL_PATH, **saved)
 
 
 @pytest.mark.parametrize("case", ["terrain", "shapes", "nosun", "deep"])

@@ -79,7 +79,12 @@ class TraceStats(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("refill_min", ctypes.c_uint32), ("blocks_per_sm", ctypes.c_int32),
-                ("persistent", ctypes.c_uint32), ("wavefront", ctypes.c_uint32)]
+                ("persistent", ctypes.c_uint32), ("wavefront", ctypes.c_uint32),
+                ("tile_shape", ctypes.c_uint32), ("block_warps", ctypes.c_uint32)]
+
+
+TILE_8X4, TILE_4X8, TILE_16X2, TILE_32X1 = 0, 1, 2, 3
+TILE_NAMES = {TILE_8X4: "8x4", TILE_4X8: "4x8", TILE_16X2: "16x2", TILE_32X1: "32x1"}
 
 
 KERNEL_RENDER, KERNEL_TRACE_RAYS, KERNEL_BATCH, KERNEL_PATH = 1, 2, 3, 4
@@ -115,7 +120,7 @@ class ServeTiming(ctypes.Structure):
 class ServeStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "submitted", "completed", "launches", "views_launched", "samples", "scene_loads",
-        "evictions", "resident_bytes", "pending")]
+        "evictions", "resident_bytes", "pending", "device_ns")]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}
@@ -209,6 +214,7 @@ SIGNATURES = [
     ("vt_batch_run", _i32, [_i32, _vp]),
     ("vt_batch_run_direct", _i32, [_i32, _vp]),
     ("vt_batch_info", _i32, [_i32, _vp, _vp]),
+    ("vt_batch_stats", _i32, [_i32, ctypes.POINTER(TraceStats)]),
     ("vt_batch_destroy", _i32, [_i32]),
     ("vt_serve_default_config", _i32, [ctypes.POINTER(ServeConfig)]),
     ("vt_serve_start", _i32, [ctypes.POINTER(ServeConfig), ctypes.POINTER(ctypes.c_int32)]),
@@ -308,11 +314,14 @@ def get_tuning(kernel):
     t = Tuning()
     check(lib().vt_get_tuning(kernel, ctypes.byref(t)))
     return {"refill_min": t.refill_min, "blocks_per_sm": t.blocks_per_sm,
-            "persistent": t.persistent, "wavefront": t.wavefront}
+            "persistent": t.persistent, "wavefront": t.wavefront, "tile_shape": t.tile_shape,
+            "block_warps": t.block_warps}
 
 
-def set_tuning(kernel, refill_min=16, blocks_per_sm=0, persistent=True, wavefront=False):
-    t = Tuning(refill_min, blocks_per_sm, 1 if persistent else 0, 1 if wavefront else 0)
+def set_tuning(kernel, refill_min=16, blocks_per_sm=0, persistent=True, wavefront=False,
+               tile_shape=TILE_8X4, block_warps=4):
+    t = Tuning(refill_min, blocks_per_sm, 1 if persistent else 0, 1 if wavefront else 0,
+               tile_shape, block_warps)
     check(lib().vt_set_tuning(kernel, ctypes.byref(t)))
 
 
@@ -597,6 +606,12 @@ class Batch:
     def run(self, stream=None, graph=True):
         f = lib().vt_batch_run if graph else lib().vt_batch_run_direct
         check(f(self.id, _stream(stream)))
+
+    def stats(self):
+        """Counting run (same records, slower kernel build): traversal counters as a dict."""
+        st = TraceStats()
+        check(lib().vt_batch_stats(self.id, ctypes.byref(st)))
+        return st.as_dict()
 
     def destroy(self):
         if self.id is not None:

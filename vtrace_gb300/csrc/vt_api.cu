@@ -86,7 +86,7 @@ cudaError_t launch_frame(const GridView& g, const vt_camera& cam, const LightVie
         return launch_render_persistent(g, cam, light, out, next_counter(), s.tune_render,
                                         s.sm_count, stream);
     if (s.tune_render.wavefront) return launch_render_wavefront(g, cam, light, out, stream);
-    return launch_render(g, cam, light, out, nullptr, stream);
+    return launch_render(g, cam, light, out, nullptr, stream, 0, 0, &s.tune_render);
 }
 
 cudaError_t launch_rays(const GridView& g, const vt_ray* rays, uint64_t n, uint4* out,
@@ -553,6 +553,17 @@ void* host_mapped(void* p) {
     return a.devicePointer;
 }
 
+void* device_address(void* p) {
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    return nullptr;
+}
+
 int32_t staging(size_t bytes, void** out) {
     State& s = state();
     if (s.staging_bytes < bytes) {
@@ -569,7 +580,7 @@ int32_t staging(size_t bytes, void** out) {
     return VT_OK;
 }
 
-static void stats_from(const Counters& c, vt_trace_stats* st) {
+void stats_from(const Counters& c, vt_trace_stats* st) {
     st->rays = c.rays;
     st->shadow_rays = c.shadow_rays;
     st->hits = c.hits;
@@ -628,7 +639,7 @@ void vt_shutdown(void) {
 
 const char* vt_last_error(void) { return g_last_error.c_str(); }
 
-uint32_t vt_version(void) { return (1u << 16) | 0u; }
+uint32_t vt_version(void) { return (1u << 16) | 1u; }
 
 void* vt_get_stream(void) {
     if (ensure_init()) return nullptr;
@@ -668,6 +679,8 @@ int32_t vt_get_tuning(int32_t kernel, vt_tuning* out) {
     out->blocks_per_sm = t->blocks_per_sm;
     out->persistent = t->persistent;
     out->wavefront = t->wavefront;
+    out->tile_shape = t->tile_shape;
+    out->block_warps = t->block_warps;
     return VT_OK;
 }
 
@@ -676,10 +689,17 @@ int32_t vt_set_tuning(int32_t kernel, const vt_tuning* in) {
     if (!t || !in) return fail(VT_EINVAL, "vt_set_tuning: bad kernel or null input");
     if (in->refill_min < 1 || in->refill_min > 32 || in->blocks_per_sm < 0 || in->blocks_per_sm > 64)
         return fail(VT_EINVAL, "vt_set_tuning: refill_min must be 1..32, blocks_per_sm 0..64");
+    if (in->tile_shape > VT_TILE_32X1 ||
+        (in->block_warps != 0 && in->block_warps != 1 && in->block_warps != 2 &&
+         in->block_warps != 4 && in->block_warps != 8))
+        return fail(VT_EINVAL, "vt_set_tuning: tile_shape must be a VT_TILE_* value, block_warps "
+                               "0, 1, 2, 4 or 8");
     t->refill_min = in->refill_min;
     t->blocks_per_sm = in->blocks_per_sm;
     t->persistent = in->persistent ? 1u : 0u;
     t->wavefront = in->wavefront ? 1u : 0u;
+    t->tile_shape = in->tile_shape;
+    t->block_warps = in->block_warps ? in->block_warps : 4u;
     return VT_OK;
 }
 

@@ -17,6 +17,7 @@ namespace vt {
 
 struct GridView;
 struct LightView;
+struct Counters;
 
 constexpr uint32_t kMaxDim = 65535;
 constexpr size_t kMaxGrids = 1u << 20;
@@ -70,8 +71,8 @@ struct State {
     std::atomic<uint32_t> counter_next{0};
     // defaults from sweeps on GB300: coherent camera rays keep their 8 x 4 tiles (refills would
     // mix tiles), incoherent ray buffers and path tracing refill a warp once 8 lanes are idle
-    TraceTuning tune_render{16, 0, 0, 0}, tune_rays{8, 0, 1, 0}, tune_batch{32, 0, 1, 0},
-        tune_path{8, 0, 1, 1};
+    TraceTuning tune_render{16, 0, 0, 0, VT_TILE_8X4, 4}, tune_rays{8, 0, 1, 0, VT_TILE_8X4, 4},
+        tune_batch{32, 0, 1, 0, VT_TILE_8X4, 4}, tune_path{8, 0, 1, 1, VT_TILE_8X4, 4};
 };
 
 constexpr uint32_t kCounterRing = 4096;
@@ -95,7 +96,13 @@ int32_t check_camera(const vt_camera* cam);
 // Device address of page-locked, 16-byte aligned host memory (kernels write outputs there
 // directly), or nullptr for any other pointer.
 void* host_mapped(void* p);
+// Address a kernel can use for `p`: device or managed memory as is, page-locked host memory
+// through its device mapping; nullptr for memory the device cannot reach (pageable host memory,
+// unknown pointers).
+void* device_address(void* p);
 LightView light_view(const vt_light* light);
+// Traversal counters of a counting launch as the ABI reports them.
+void stats_from(const Counters& c, vt_trace_stats* st);
 int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_host,
                    uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t stream,
                    std::unique_ptr<Grid>& out);

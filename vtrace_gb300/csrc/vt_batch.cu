@@ -166,9 +166,13 @@ __global__ void __launch_bounds__(256, 4) batch_kernel(const BatchView* __restri
 // lane form with whole-warp refills, 23% faster on the 64-view workload.
 constexpr int kBatchTileThreads = 128;
 
+// STATS: the counting build (every reference iteration walked, traversal counters gathered into
+// `counters`; same records), for the roofline's algorithmic bytes.
+template <bool STATS>
 __global__ void __launch_bounds__(kBatchTileThreads) batch_tile_kernel(const BatchView* __restrict__ table,
                                                          uint32_t nviews, uint64_t units,
-                                                         unsigned long long* __restrict__ counter) {
+                                                         unsigned long long* __restrict__ counter,
+                                                         Counters* __restrict__ counters) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     BatchView* views = reinterpret_cast<BatchView*>(smem_raw);
     {
@@ -179,6 +183,7 @@ __global__ void __launch_bounds__(kBatchTileThreads) batch_tile_kernel(const Bat
         __syncthreads();
     }
     const uint32_t lane = threadIdx.x & 31u;
+    Tally<STATS> tl;
     for (;;) {
         unsigned long long u = 0;
         if (lane == 0) u = atomicAdd(counter, 1ull);
@@ -204,11 +209,11 @@ __global__ void __launch_bounds__(kBatchTileThreads) batch_tile_kernel(const Bat
             float jx, jy, o[3], d[3];
             jitter(V.seed, V.view_id, px, py, sample, jx, jy);
             raygen(V.cam, px, py, jx, jy, o, d);
-            Tally<false> tl;
-            const HitRec h = shade_ray<false>(V.g, V.light, o, d, tl);
+            const HitRec h = shade_ray<STATS>(V.g, V.light, o, d, tl);
             V.out[((py * V.cam.width) + px) * V.spp + sample] = make_uint4(h.w0, h.w1, h.w2, h.w3);
         }
     }
+    if (STATS) tl.flush(counters);
 }
 
 static bool batch_tile_form(const TraceTuning& tune) { return tune.refill_min >= 32; }
@@ -275,11 +280,14 @@ unsigned batch_blocks(uint32_t n, uint64_t total, const TraceTuning& tune) {
     const int table_max = (int)(kMaxBatchViews * sizeof(BatchView));
     if (cudaFuncSetAttribute((const void*)batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              table_max) != cudaSuccess ||
-        cudaFuncSetAttribute((const void*)batch_tile_kernel,
+        cudaFuncSetAttribute((const void*)batch_tile_kernel<false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, table_max) != cudaSuccess ||
+        cudaFuncSetAttribute((const void*)batch_tile_kernel<true>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, table_max) != cudaSuccess)
         cudaGetLastError();
     int per_sm = 0;
-    const void* kernel = batch_tile_form(tune) ? (const void*)batch_tile_kernel : (const void*)batch_kernel;
+    const void* kernel =
+        batch_tile_form(tune) ? (const void*)batch_tile_kernel<false> : (const void*)batch_kernel;
     const int threads = batch_tile_form(tune) ? kBatchTileThreads : 256;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) !=
             cudaSuccess ||
@@ -298,8 +306,8 @@ cudaError_t launch_batch(const BatchView* d_table, uint32_t n, uint64_t total,
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     if (batch_tile_form(tune))
-        batch_tile_kernel<<<blocks, kBatchTileThreads, (size_t)n * sizeof(BatchView), stream>>>(d_table, n,
-                                                                                  total / 32, counter);
+        batch_tile_kernel<false><<<blocks, kBatchTileThreads, (size_t)n * sizeof(BatchView), stream>>>(
+            d_table, n, total / 32, counter, nullptr);
     else
         batch_kernel<<<blocks, 256, (size_t)n * sizeof(BatchView), stream>>>(d_table, n, total,
                                                                              counter, tune.refill_min);
@@ -353,10 +361,19 @@ int32_t vt_batch_create(const vt_view* views, uint32_t n, int32_t* batch_out) {
             return fail(VT_ELIMIT, "vt_batch_create: view " + std::to_string(i) +
                                        " has 2^32 or more samples");
         }
+        // device memory as given; page-locked host memory through its device address (the
+        // kernel writes the records over the host link); anything else is refused rather than
+        // handed to a kernel that could not reach it
+        void* out = device_address(v.d_out);
+        if (!out) {
+            batch_free(*b);
+            return fail(VT_EINVAL, "vt_batch_create: view " + std::to_string(i) +
+                                       " output is neither device nor page-locked host memory");
+        }
         g->refs.fetch_add(1);
         b->grids.push_back(v.grid);
         table[i] = make_batch_view(*g, v.camera, (v.flags & VT_VIEW_LIGHT) ? &v.light : nullptr,
-                                   v.spp, v.seed, v.view_id, v.d_out, begin);
+                                   v.spp, v.seed, v.view_id, out, begin);
         begin += batch_view_items(v.camera, v.spp);
         b->rays_primary += (uint64_t)v.camera.width * v.camera.height * v.spp;
     }
@@ -425,6 +442,37 @@ int32_t vt_batch_run_direct(int32_t batch, void* stream) {
     if (!b) return fail(VT_ENOTFOUND, "vt_batch_run_direct: unknown batch");
     cudaError_t e = batch_launch(*b, pick_stream(stream));
     if (e != cudaSuccess) return cuda_fail(e, "vt_batch_run_direct: launch");
+    return VT_OK;
+}
+
+int32_t vt_batch_stats(int32_t batch, vt_trace_stats* stats) {
+    Batch* b = lookup_batch(batch);
+    if (!b) return fail(VT_ENOTFOUND, "vt_batch_stats: unknown batch");
+    if (!stats) return fail(VT_EINVAL, "vt_batch_stats: null output");
+    cudaStream_t st = state().stream;
+    void* buf = nullptr;
+    if (cudaMalloc(&buf, sizeof(Counters) + sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(VT_ENOMEM, "vt_batch_stats: cudaMalloc(counters)");
+    }
+    Counters* dc = (Counters*)buf;
+    unsigned long long* cursor = (unsigned long long*)((char*)buf + sizeof(Counters));
+    Counters hc;
+    cudaError_t e = cudaMemsetAsync(buf, 0, sizeof(Counters) + sizeof(unsigned long long), st);
+    if (e == cudaSuccess) {
+        // the counting build always runs in the tile form (same records as either form)
+        TraceTuning tile = b->tune;
+        tile.refill_min = 32;
+        const unsigned blocks = batch_blocks(b->nviews, b->total, tile);
+        batch_tile_kernel<true><<<blocks, kBatchTileThreads, b->smem, st>>>(
+            b->d_table, b->nviews, b->total / 32, cursor, dc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hc, dc, sizeof(Counters), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_batch_stats");
+    stats_from(hc, stats);
     return VT_OK;
 }
 

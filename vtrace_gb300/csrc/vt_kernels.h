@@ -18,6 +18,8 @@ struct TraceTuning {
     int blocks_per_sm = 0;     // 0: as many 256-thread blocks as fit on an SM
     uint32_t persistent = 1;   // 0: one thread per ray in 8 x 4 pixel tiles, no refill
     uint32_t wavefront = 0;    // render only: shadow rays in a second pass over a compacted queue
+    uint32_t tile_shape = 0;   // render tile launch: VT_TILE_* pixels per warp
+    uint32_t block_warps = 4;  // render tile launch: warps per block (1, 2, 4, 8)
 };
 
 // Render in two passes (primary rays, then the queued shadow rays); stream-ordered scratch.
@@ -34,9 +36,10 @@ cudaError_t launch_trace_rays_persistent(const GridView& g, const vt_ray* rays, 
                                          cudaStream_t stream,
                                          const unsigned int* n_dev = nullptr);
 
+// `tune` selects the warp tile and block shape (nullptr: 8 x 4 pixels per warp, 4 warps).
 cudaError_t launch_render(const GridView& g, const vt_camera& cam, const LightView& light,
                           uint4* out, Counters* counters, cudaStream_t stream, uint32_t row0 = 0,
-                          uint32_t row1 = 0);
+                          uint32_t row1 = 0, const TraceTuning* tune = nullptr);
 // n_dev as for launch_trace_rays_persistent: the device-side ray count (at most n), or nullptr.
 cudaError_t launch_trace_rays(const GridView& g, const vt_ray* rays, uint64_t n, uint4* out,
                               Counters* counters, cudaStream_t stream,

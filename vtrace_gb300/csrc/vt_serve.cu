@@ -102,6 +102,7 @@ struct ServeReq {
 struct Slot {
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
+    cudaEvent_t t_begin = nullptr, t_end = nullptr;  // device time of the slot's launch
     BatchView* d_table = nullptr;
     BatchView* h_table = nullptr;  // pinned staging
     ResolveView* d_resolve = nullptr;
@@ -233,6 +234,7 @@ void Service::launch(Slot& slot, const std::vector<uint64_t>& ids) {
         cv_done.notify_all();
         return;
     }
+    cudaEventRecord(slot.t_begin, slot.stream);
     cudaMemcpyAsync(slot.d_table, slot.h_table, n * sizeof(BatchView), cudaMemcpyHostToDevice,
                     slot.stream);
     cudaMemcpyAsync(slot.d_resolve, slot.h_resolve, n * sizeof(ResolveView),
@@ -253,6 +255,7 @@ void Service::launch(Slot& slot, const std::vector<uint64_t>& ids) {
         q.d_samples = q.d_image = nullptr;
         q.h_image = nullptr;
     }
+    cudaEventRecord(slot.t_end, slot.stream);
     cudaEventRecord(slot.done, slot.stream);
     slot.busy = true;
     stats.launches++;
@@ -261,6 +264,11 @@ void Service::launch(Slot& slot, const std::vector<uint64_t>& ids) {
 
 void Service::retire(Slot& slot) {
     const int64_t t = now_ns();
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, slot.t_begin, slot.t_end) == cudaSuccess)
+        stats.device_ns += (uint64_t)((double)ms * 1e6);
+    else
+        cudaGetLastError();
     for (uint64_t id : slot.reqs) {
         ServeReq& q = reqs[id];
         q.status = VT_OK;
@@ -379,6 +387,8 @@ int32_t vt_serve_start(const vt_serve_config* cfg, int32_t* service_out) {
     for (Slot& sl : s->slots) {
         cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreate(&sl.t_begin);
+        if (e == cudaSuccess) e = cudaEventCreate(&sl.t_end);
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_table, kMaxBatchViews * sizeof(BatchView));
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_resolve, kMaxBatchViews * sizeof(ResolveView));
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_counter, sizeof(unsigned long long));
@@ -519,6 +529,8 @@ int32_t vt_serve_stop(int32_t service) {
     for (Slot& sl : s->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
         if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.t_begin) cudaEventDestroy(sl.t_begin);
+        if (sl.t_end) cudaEventDestroy(sl.t_end);
         if (sl.stream) cudaStreamDestroy(sl.stream);
         cudaFree(sl.d_table);
         cudaFree(sl.d_resolve);

@@ -8,20 +8,52 @@
 
 namespace vt {
 
-// Image tile of one warp: 8 x 4 pixels, so that a warp's rays start together and stay coherent.
-// A 128-thread block covers 16 x 8 pixels (2 x 2 warps): small blocks free their slots soon after
-// their slowest ray ends (6% faster than 256-thread blocks on the 1080p frame).
+// Image tile of one warp: 8 x 4 pixels by default, so that a warp's rays start together and stay
+// coherent.  A 128-thread block covers 16 x 8 pixels (2 x 2 warps): small blocks free their slots
+// soon after their slowest ray ends (6% faster than 256-thread blocks on the 1080p frame).  The
+// fused render launch takes other warp tiles and block sizes from its tuning (the autotuner's
+// search space); the two-pass form keeps the default.
 constexpr int kTileW = 16, kTileH = 8, kTileThreads = 128;
+
+// Warp tile and block arrangement of a render launch: warp tiles of (1 << wx_log) x
+// (32 >> wx_log) pixels, bx x by of them per block.
+struct RenderShape {
+    uint32_t wx_log, bx, by;
+    uint32_t block_w() const { return bx << wx_log; }
+    uint32_t block_h() const { return by * (32u >> wx_log); }
+};
+
+static RenderShape render_shape(const TraceTuning* tune) {
+    static const uint32_t kLog[4] = {3, 2, 4, 5};  // VT_TILE_8X4, 4X8, 16X2, 32X1
+    const uint32_t wx_log = tune && tune->tile_shape < 4 ? kLog[tune->tile_shape] : 3u;
+    uint32_t warps = tune ? tune->block_warps : 4u;
+    if (warps != 1 && warps != 2 && warps != 8) warps = 4;
+    // warps along x: the power of two that brings the block closest to twice as wide as high
+    RenderShape best{wx_log, 1, warps};
+    double best_err = 1e30;
+    for (uint32_t bx = 1; bx <= warps; bx <<= 1) {
+        const RenderShape r{wx_log, bx, warps / bx};
+        const double aspect = (double)r.block_w() / (double)r.block_h();
+        const double err = aspect > 2.0 ? aspect / 2.0 : 2.0 / aspect;
+        if (err < best_err) {
+            best_err = err;
+            best = r;
+        }
+    }
+    return best;
+}
 
 // Rows row0 .. row1 - 1 of the image (a band; the whole image when 0 .. height).
 template <bool STATS>
-__global__ void __launch_bounds__(kTileThreads) render_kernel(GridView g, vt_camera cam, LightView light,
+__global__ void __launch_bounds__(256) render_kernel(GridView g, vt_camera cam, LightView light,
                                                      uint4* __restrict__ out,
                                                      Counters* __restrict__ counters,
-                                                     uint32_t row0, uint32_t row1) {
+                                                     uint32_t row0, uint32_t row1,
+                                                     RenderShape shape) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t px = blockIdx.x * kTileW + (warp & 1u) * 8u + (lane & 7u);
-    const uint32_t py = row0 + blockIdx.y * kTileH + (warp >> 1) * 4u + (lane >> 3);
+    const uint32_t wx = 1u << shape.wx_log, wy = 32u >> shape.wx_log;
+    const uint32_t px = blockIdx.x * (shape.bx * wx) + (warp % shape.bx) * wx + (lane & (wx - 1u));
+    const uint32_t py = row0 + blockIdx.y * (shape.by * wy) + (warp / shape.bx) * wy + (lane >> shape.wx_log);
     if (px >= cam.width || py >= row1) return;
     Tally<STATS> tl;
     tl.bind(counters, g.bricks);
@@ -53,14 +85,17 @@ __global__ void __launch_bounds__(256) trace_rays_kernel(GridView g,
 
 cudaError_t launch_render(const GridView& g, const vt_camera& cam, const LightView& light,
                           uint4* out, Counters* counters, cudaStream_t stream, uint32_t row0,
-                          uint32_t row1) {
+                          uint32_t row1, const TraceTuning* tune) {
     if (row1 == 0 || row1 > cam.height) row1 = cam.height;
     if (row0 >= row1) return cudaSuccess;
-    dim3 grid((cam.width + kTileW - 1) / kTileW, (row1 - row0 + kTileH - 1) / kTileH);
+    const RenderShape sh = render_shape(tune);
+    const unsigned threads = 32u * sh.bx * sh.by;
+    dim3 grid((cam.width + sh.block_w() - 1) / sh.block_w(),
+              (row1 - row0 + sh.block_h() - 1) / sh.block_h());
     if (counters)
-        render_kernel<true><<<grid, kTileThreads, 0, stream>>>(g, cam, light, out, counters, row0, row1);
+        render_kernel<true><<<grid, threads, 0, stream>>>(g, cam, light, out, counters, row0, row1, sh);
     else
-        render_kernel<false><<<grid, kTileThreads, 0, stream>>>(g, cam, light, out, nullptr, row0, row1);
+        render_kernel<false><<<grid, threads, 0, stream>>>(g, cam, light, out, nullptr, row0, row1, sh);
     return cudaGetLastError();
 }
 
