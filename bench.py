@@ -688,18 +688,23 @@ def bench_multiview(args, stream, flush, dev, tuning):
                                  repeats=max(1, args.steps // 4), warmup=1, flush=flush)
     for x in singles:
         x.destroy()
-    # end to end: the same batch writing its records straight into page-locked host memory
+    # end to end: the graph replay, then every view's records copied to page-locked host memory
+    # on the same stream (copy engines; kernel stores over the host link measured slower)
     host = [torch.empty(b.numel(), dtype=torch.uint8, pin_memory=True) for b in bufs]
-    hbatch = vt.Batch(specs(host))
-    hbatch.run(stream)
-    torch.cuda.synchronize()
+
+    def replay_and_copy():
+        batch.run(stream)
+        with torch.cuda.stream(stream):
+            for h, b in zip(host, bufs):
+                h.copy_(b, non_blocking=True)
+        stream.synchronize()
+
+    replay_and_copy()
     reps = max(3, args.steps // 4)
     t0 = time.perf_counter()
     for _ in range(reps):
-        hbatch.run(stream)
-        stream.synchronize()
+        replay_and_copy()
     e2e_s = (time.perf_counter() - t0) / reps
-    hbatch.destroy()
     out = {"metric": "Mrays/s (%d views over 8 scenes, 1-4 spp, one graph replay)" % len(views),
            "value": st["rays"] / ms / 1e3, "unit": "Mrays/s", "ms_per_step": ms, "steps": steps,
            "config": {"workload": "multiview", "views": len(views), "primary_rays": records,
@@ -707,8 +712,9 @@ def bench_multiview(args, stream, flush, dev, tuning):
            "per_view_launches": {"ms": ms_single, "value": st["rays"] / ms_single / 1e3},
            "e2e": {"value": st["rays"] / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 16 * records,
-                   "path": "vt_batch_run (C ABI) of a batch whose views write page-locked host "
-                           "memory, host wall clock; views and cameras are fixed in the graph"},
+                   "path": "vt_batch_run (C ABI), then each view's records copied to page-locked "
+                           "host memory on the launch stream, host wall clock; views and cameras "
+                           "are fixed in the graph"},
            "roofline": roofline(stats_bytes(st, records), ms, "vt::batch_tile_kernel<false>"
                                 if vt.get_tuning(vt.KERNEL_BATCH)["refill_min"] >= 32
                                 else "vt::batch_kernel"),

@@ -244,6 +244,9 @@ int32_t vt_grid_update(int32_t grid, const void* voxels, uint32_t order, uint32_
  * shares that array, so calls whose work overlaps on the GPU (different streams) race; serialise
  * them on one stream.  Asynchronous on `stream` (NULL = the legacy default stream); the first call
  * on each device looks up the array's device address and should come before any stream capture.
+ * The address is kept per device for the runtime's primary context: call it from that context,
+ * and call vt_shutdown before resetting the device (vt_shutdown forgets the address; the next
+ * call looks it up again).
  * Returns VT_OK, VT_EINVAL (null or misaligned pointer, bad size), VT_ELIMIT or VT_ECUDA; it
  * does not set vt_last_error. */
 int32_t vt_grid_build_u8_noalloc(const uint8_t* d_voxels, const uint32_t* d_palette,
@@ -378,20 +381,26 @@ int32_t vt_batch_destroy(int32_t batch);
 
 /* ---------------------------------------------------------------- serving */
 
-/* A continuous-batching render service: requests arrive from any thread; a dispatcher thread keeps
- * up to max_inflight launches on the device (one stream each), packing the oldest pending requests
- * (up to max_views_per_launch views / max_samples_per_launch samples) into one persistent
- * work-stealing launch as launch slots free up; each request's samples are averaged into an RGBA8
- * image copied to the caller's host buffer.  Scene brick grids stay resident in a cache bounded by
- * hbm_budget_bytes, built on first use, least-recently-used unreferenced scenes evicted.
- * max_inflight = 1 with max_views_per_launch = 1 is the plain per-request baseline. */
+/* A continuous-batching render service: requests arrive from any thread and are split into pieces
+ * of whole 4-row bands of at most max_samples_per_piece samples; a dispatcher thread keeps up to
+ * max_inflight launches on the device (one stream each), packing the oldest pending pieces (up to
+ * max_views_per_launch pieces / max_samples_per_launch samples) into one persistent work-stealing
+ * launch as launch slots free up; each piece's samples are averaged into its rows of the request's
+ * RGBA8 image in the caller's host buffer, and a request is done when its last piece is.  Scene
+ * brick grids stay resident in a cache built on first use, least-recently-used unreferenced scenes
+ * evicted.  hbm_budget_bytes bounds the resident grids plus the launch slots' sample buffers
+ * (max_inflight x max_samples_per_launch x 20 bytes, allocated at start) plus the temporary buffer
+ * of any piece larger than a slot's.  max_inflight = 1, max_views_per_launch = 1 and
+ * max_samples_per_piece = 0 is the plain per-request baseline. */
 typedef struct vt_serve_config {
     uint64_t hbm_budget_bytes;
     uint32_t max_inflight;           /* concurrent launches, 1..32 */
     uint32_t max_views_per_launch;   /* 1..256 */
-    uint64_t max_samples_per_launch; /* pack requests up to this many samples per launch */
+    uint64_t max_samples_per_launch; /* pack pieces up to this many samples per launch (1..2^32) */
     uint32_t poll_interval_us;       /* completion polling period of the dispatcher */
     uint32_t refill_min;             /* persistent-warp refill threshold of the launches */
+    uint64_t max_samples_per_piece;  /* split requests into pieces of at most this many samples
+                                        (whole 4-row bands, at least one); 0 = never split */
 } vt_serve_config;
 
 /* One render request.  The image is width*height RGBA8 (row-major from the top row): per pixel
@@ -438,7 +447,9 @@ int32_t vt_serve_submit(int32_t service, const vt_serve_request* req, uint64_t* 
 int32_t vt_serve_poll(int32_t service, uint64_t request_id, uint32_t timeout_us,
                       vt_serve_timing* timing);
 int32_t vt_serve_get_stats(int32_t service, vt_serve_stats* out);
-/* Finish in-flight launches, cancel pending requests, free everything of the service. */
+/* Finish in-flight launches, cancel pending requests, free everything of the service (once no
+ * other thread is inside a call on it).  Safe while other threads submit or poll: their calls
+ * return VT_ECANCELED / VT_ENOTFOUND or the request's final status. */
 int32_t vt_serve_stop(int32_t service);
 
 /* ---------------------------------------------------------------- MagicaVoxel models (host) */

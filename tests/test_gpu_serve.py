@@ -94,11 +94,101 @@ def test_plain_mode_gives_the_same_images(torch):
         svc.stop()
 
 
+def test_split_requests_match_unsplit_ones(torch):
+    """A request cut into many 4-row pieces, packed into shared launches with other requests'
+    pieces, gives the same image as the same request run whole, and the oracle's."""
+    scenes, views = small_world(6)
+    v = dict(views[1], spp=3)
+    v["camera"] = vt.camera_look_at((-30.0, 70.0, -30.0), (32.0, 16.0, 32.0), (0, 1, 0), 60.0,
+                                    203, 131)  # 131 rows: the last piece is a partial tile row
+    whole = vt.Service(max_inflight=1, max_samples_per_piece=0)
+    split = vt.Service(max_inflight=2, max_samples_per_piece=203 * 3 * 8,
+                       max_samples_per_launch=203 * 3 * 20)
+    try:
+        out = []
+        for svc in (whole, split):
+            sids = [svc.add_scene(s["voxels"], s["palette"]) for s in scenes]
+            buf = pinned(torch, v["camera"])
+            others = [pinned(torch, w["camera"]) for w in views]
+            rids = [svc.submit(sids[w["scene"]], w["camera"], b, w["spp"], w["seed"], w["view_id"],
+                               w["light"]) for w, b in zip(views[:3], others)]
+            rid = svc.submit(sids[v["scene"]], v["camera"], buf, v["spp"], v["seed"], v["view_id"],
+                             v["light"])
+            rids += [svc.submit(sids[w["scene"]], w["camera"], b, w["spp"], w["seed"],
+                                w["view_id"], w["light"]) for w, b in zip(views[3:], others[3:])]
+            t = svc.wait(rid)
+            assert t["samples"] == 203 * 131 * 3
+            for r in rids:
+                svc.wait(r)
+            out.append((buf.numpy().copy(), [o.numpy().copy() for o in others]))
+        assert split.stats()["views_launched"] >= 131 // 8  # the big request ran as pieces
+        np.testing.assert_array_equal(out[0][0], out[1][0])
+        for a, b in zip(out[0][1], out[1][1]):
+            np.testing.assert_array_equal(a, b)
+        img = out[1][0].reshape(131, 203, 4)
+        np.testing.assert_array_equal(img, oracle_image(scenes[v["scene"]], v))
+    finally:
+        whole.stop()
+        split.stop()
+
+
+def test_stop_while_other_threads_submit_and_poll(torch):
+    """vt_serve_stop while other threads are inside submit and poll calls on the same service:
+    every call returns (a request id, VT_ECANCELED or VT_ENOTFOUND), nothing is left waiting."""
+    import threading
+    scenes, views = small_world(4)
+    for round_ in range(3):
+        svc = vt.Service(max_inflight=2)
+        sid = svc.add_scene(scenes[0]["voxels"], scenes[0]["palette"])
+        v = views[0]
+        stop_flag = threading.Event()
+        codes = []
+        bufs = [pinned(torch, v["camera"]) for _ in range(8)]
+        service = svc.id  # the raw id: the workers keep calling after stop() has released it
+
+        def worker(k):
+            n = 0
+            while not stop_flag.is_set() or n < 4:
+                r = vt.ServeRequest()
+                r.scene, r.spp, r.seed, r.camera = sid, 1, n, v["camera"]
+                r.host_rgba = bufs[(k + n) % len(bufs)].data_ptr()
+                rid = ctypes.c_uint64(0)
+                rc = vt.lib().vt_serve_submit(service, ctypes.byref(r), ctypes.byref(rid))
+                if rc == 0:
+                    rc = vt.lib().vt_serve_poll(service, rid.value, 2000, None)
+                if rc not in (0, -8):  # VT_ENOTREADY: still running
+                    codes.append(rc)
+                    if rc in (-4, -7):
+                        return
+                n += 1
+
+        threads = [threading.Thread(target=worker, args=(k,)) for k in range(4)]
+        for t in threads:
+            t.start()
+        import time
+        time.sleep(0.05 * (round_ + 1))
+        stop_flag.set()
+        svc.stop()
+        for t in threads:
+            t.join(timeout=60)
+        assert not any(t.is_alive() for t in threads)
+        assert set(codes) <= {-4, -7}, codes  # VT_ENOTFOUND, VT_ECANCELED only
+
+
+def test_start_refuses_slots_beyond_the_budget(torch):
+    with pytest.raises(vt.VtError) as e:
+        vt.Service(hbm_budget_bytes=1 << 20, max_samples_per_launch=1 << 20)
+    assert e.value.code == -2
+
+
 def test_cache_evicts_least_recently_used_under_its_budget(torch):
     scenes, views = small_world(8)
-    # room for the largest scene's bound only: alternating scenes force evictions
+    # room for the largest scene's bound only (beside the one slot's sample buffer): alternating
+    # scenes force evictions
     bound = max(((s["n"] + 7) // 8) ** 3 * (4 + 64 + 512) + 1024 for s in scenes)
-    svc = vt.Service(hbm_budget_bytes=bound + 1024)
+    cap = 160 * 120 * 4
+    svc = vt.Service(hbm_budget_bytes=bound + 1024 + cap * 20, max_inflight=1,
+                     max_samples_per_launch=cap)
     try:
         sids = [svc.add_scene(s["voxels"], s["palette"]) for s in scenes]
         for v in views:
@@ -115,7 +205,9 @@ def test_cache_evicts_least_recently_used_under_its_budget(torch):
 
 def test_failures_are_reported_per_request(torch):
     scenes, views = small_world(4)
-    svc = vt.Service(hbm_budget_bytes=64 << 10)  # smaller than any scene's bound
+    # 64 KB beside the slot's buffer: smaller than any scene's bound
+    svc = vt.Service(hbm_budget_bytes=(64 << 10) + 4096 * 20, max_inflight=1,
+                     max_samples_per_launch=4096)
     try:
         sid = svc.add_scene(scenes[1]["voxels"], scenes[1]["palette"])
         v = views[0]

@@ -49,7 +49,10 @@ def test_noalloc_build_matches_allocating_build():
                                       d_counts.data_ptr(), None) == 0
     vt.Grid.from_u8(cases[1], pal).destroy()
     torch.cuda.synchronize()
+    # the window holds the no-allocation calls and the copies of their outputs to host memory
+    # only; the allocating builds they are compared with run after it
     free_before = vt.device_info()["free_bytes"]
+    results = []
     for vox, d_vox in zip(cases, inputs):
         nz, ny, nx = vox.shape
         rc = L.vt_grid_build_u8_noalloc(d_vox.data_ptr(), d_pal.data_ptr(), nx, ny, nz,
@@ -57,9 +60,17 @@ def test_noalloc_build_matches_allocating_build():
                                         d_payload.data_ptr(), d_counts.data_ptr(), None)
         assert rc == 0
         torch.cuda.synchronize()
+        results.append((d_counts.cpu().numpy().view(np.uint64).copy(),
+                        d_dir.cpu().numpy().view(np.uint32).copy(),
+                        d_masks.cpu().numpy().view(np.uint64).copy(),
+                        d_payload.cpu().numpy().copy()))
+    torch.cuda.synchronize()
+    free_after = vt.device_info()["free_bytes"]
+    assert free_after == free_before
+    for vox, (counts, dirs, masks, payload) in zip(cases, results):
+        nz, ny, nx = vox.shape
         bricks = ((nx + 7) // 8) * ((ny + 7) // 8) * ((nz + 7) // 8)
-        counts = d_counts.cpu().numpy().view(np.uint64)
-        got_dir = d_dir.cpu().numpy().view(np.uint32)[:bricks]
+        got_dir = dirs[:bricks]
         g = vt.Grid.from_u8(vox, pal)  # the allocating path (test side only)
         try:
             want_dir, want_masks = g.bricks()
@@ -69,12 +80,9 @@ def test_noalloc_build_matches_allocating_build():
         np.testing.assert_array_equal(got_dir, want_dir)
         n = info["bricks_nonempty"]
         assert int(counts[0]) == n and int(counts[1]) == info["voxels_occupied"]
-        got_masks = d_masks.cpu().numpy().view(np.uint64)[: n * 8].reshape(-1, 8)
-        np.testing.assert_array_equal(got_masks, want_masks)
-        got_payload = d_payload.cpu().numpy()[: n * 512].reshape(-1, 512)
-        np.testing.assert_array_equal(got_payload, expected_payload(vox, got_dir))
-    torch.cuda.synchronize()
-    assert vt.device_info()["free_bytes"] == free_before
+        np.testing.assert_array_equal(masks[: n * 8].reshape(-1, 8), want_masks)
+        np.testing.assert_array_equal(payload[: n * 512].reshape(-1, 512),
+                                      expected_payload(vox, got_dir))
 
 
 def test_noalloc_build_rejects_grids_beyond_its_scratch():

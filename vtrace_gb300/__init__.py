@@ -637,7 +637,11 @@ class Service:
     """Continuous-batching render service (see vt_serve_* in include/vtrace.h)."""
 
     def __init__(self, hbm_budget_bytes=None, max_inflight=None, max_views_per_launch=None,
-                 max_samples_per_launch=None, plain=False, refill_min=None):
+                 max_samples_per_launch=None, plain=False, refill_min=None,
+                 max_samples_per_piece=None):
+        """plain: the per-request baseline (one unsplit request per launch, one launch at a time,
+        a slot buffer of 32M samples so that requests up to 1920x1080 x 16 spp need no
+        temporary)."""
         cfg = ServeConfig()
         check(lib().vt_serve_default_config(ctypes.byref(cfg)))
         if hbm_budget_bytes is not None:
@@ -650,8 +654,12 @@ class Service:
             cfg.max_samples_per_launch = max_samples_per_launch
         if refill_min is not None:
             cfg.refill_min = refill_min
+        if max_samples_per_piece is not None:
+            cfg.max_samples_per_piece = max_samples_per_piece
         if plain:
-            cfg.max_inflight, cfg.max_views_per_launch = 1, 1
+            cfg.max_inflight, cfg.max_views_per_launch, cfg.max_samples_per_piece = 1, 1, 0
+            if max_samples_per_launch is None:
+                cfg.max_samples_per_launch = 32 << 20
         sid = ctypes.c_int32(-1)
         check(lib().vt_serve_start(ctypes.byref(cfg), ctypes.byref(sid)))
         self.id = sid.value

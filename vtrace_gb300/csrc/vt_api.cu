@@ -608,6 +608,8 @@ int32_t vt_init(int32_t device) {
 }
 
 void vt_shutdown(void) {
+    vt_serve_release_all();
+    vt::noalloc_forget_addresses();
     vt_compat_release();
     vt_batch_release_all();
     vt::release_small_builds();

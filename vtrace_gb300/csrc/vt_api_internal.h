@@ -112,3 +112,8 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
 // Release hooks of the other subsystems, called by vt_shutdown.
 void vt_compat_release();
 void vt_batch_release_all();
+void vt_serve_release_all();
+namespace vt {
+// Forget the cached device addresses of vt_grid_build_u8_noalloc's scratch (vt_shutdown).
+void noalloc_forget_addresses();
+}  // namespace vt

@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(256, 4) batch_kernel(const BatchView* __restri
                         hi = mid - 1;
                 }
                 const BatchView& V = views[lo];
-                const uint64_t local = item - V.begin;
+                const uint64_t local = item - V.begin + V.first_item;
                 const uint64_t ts = local >> 5;
                 const uint32_t l = (uint32_t)local & 31u;
                 const uint64_t tile = ts / V.spp;
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256, 4) batch_kernel(const BatchView* __restri
                     s.px = px;
                     s.py = py;
                     s.sample = sample;
-                    s.pix = ((py * V.cam.width) + px) * V.spp + sample;
+                    s.pix = ((py * V.cam.width) + px) * V.spp + sample - V.rec_offset;
                     s.kind = 1;
                     s.pend = 1;
                     st = kRayQueued;
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kBatchTileThreads) batch_tile_kernel(const Bat
                 hi = mid - 1;
         }
         const BatchView& V = views[lo];
-        const uint64_t local = item - V.begin;
+        const uint64_t local = item - V.begin + V.first_item;
         const uint64_t ts = local >> 5;
         const uint64_t tile = ts / V.spp;
         const uint32_t sample = (uint32_t)(ts - tile * V.spp);
@@ -210,7 +210,8 @@ __global__ void __launch_bounds__(kBatchTileThreads) batch_tile_kernel(const Bat
             jitter(V.seed, V.view_id, px, py, sample, jx, jy);
             raygen(V.cam, px, py, jx, jy, o, d);
             const HitRec h = shade_ray<STATS>(V.g, V.light, o, d, tl);
-            V.out[((py * V.cam.width) + px) * V.spp + sample] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+            V.out[((py * V.cam.width) + px) * V.spp + sample - V.rec_offset] =
+                make_uint4(h.w0, h.w1, h.w2, h.w3);
         }
     }
     if (STATS) tl.flush(counters);
@@ -252,13 +253,17 @@ static void batch_free(Batch& b) {
 }
 
 uint64_t batch_view_items(const vt_camera& cam, uint32_t spp) {
-    const uint64_t tiles = (uint64_t)((cam.width + 7) / 8) * ((cam.height + 3) / 4);
-    return tiles * spp * 32;
+    return batch_rows_items(cam, spp, 0, cam.height);
+}
+
+uint64_t batch_rows_items(const vt_camera& cam, uint32_t spp, uint32_t row0, uint32_t row1) {
+    const uint64_t tile_rows = (uint64_t)((row1 + 3) / 4) - row0 / 4;
+    return tile_rows * ((cam.width + 7) / 8) * spp * 32;
 }
 
 BatchView make_batch_view(const Grid& g, const vt_camera& cam, const vt_light* light,
                           uint32_t spp, uint32_t seed, uint32_t view_id, void* out,
-                          uint64_t begin) {
+                          uint64_t begin, uint32_t row0) {
     BatchView T;
     memset(&T, 0, sizeof(T));
     T.g = g.view();
@@ -266,6 +271,8 @@ BatchView make_batch_view(const Grid& g, const vt_camera& cam, const vt_light* l
     T.light = light_view(light);
     T.out = (uint4*)out;
     T.begin = begin;
+    T.first_item = batch_rows_items(cam, spp, 0, row0);
+    T.rec_offset = row0 * cam.width * spp;
     T.tiles_x = (cam.width + 7) / 8;
     T.spp = spp;
     T.seed = seed;

@@ -25,7 +25,10 @@ constexpr size_t kNoAllocScratchBytes = 2621440;
 
 static __device__ __align__(256) unsigned char g_build_scratch[kNoAllocScratchBytes];
 
-// Device address of g_build_scratch per device (its host-side name is only a stand-in).
+// Device address of g_build_scratch per device (its host-side name is only a stand-in), looked up
+// by the first call on each device in the device's primary context (the runtime's), and
+// forgotten by vt_shutdown.  A context the runtime did not create, or a device reset without
+// vt_shutdown first, would leave a stale address here.
 constexpr int kNoAllocMaxDevices = 64;
 static std::mutex g_scratch_mu;
 static void* g_scratch_addr[kNoAllocMaxDevices] = {};
@@ -44,6 +47,11 @@ static cudaError_t scratch_address(void** out) {
     }
     *out = g_scratch_addr[dev];
     return cudaSuccess;
+}
+
+void noalloc_forget_addresses() {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    for (int d = 0; d < kNoAllocMaxDevices; ++d) g_scratch_addr[d] = nullptr;
 }
 
 __global__ void noalloc_counts_kernel(const uint32_t* __restrict__ flags,

@@ -1,20 +1,28 @@
 // vt_serve.cu — continuous-batching render service.
 //
 // Requests (scene, camera, resolution, spp, light) arrive from any thread through
-// vt_serve_submit.  A dispatcher thread keeps up to `max_inflight` launches on the device at once,
-// each on its own stream: whenever a launch slot is free it packs the oldest pending requests
-// (up to `max_views_per_launch` views and `max_samples_per_launch` samples) into one persistent
-// work-stealing launch of the batched kernel (vt_batch.cu), resolves every request's samples to an
-// RGBA8 image, copies the images to the callers' host buffers and records an event.  Requests
-// that arrive while launches are running are admitted into the next free slot, so work of
-// different requests overlaps on the GPU.  Brick grids of the scenes stay resident in a cache
-// bounded by an HBM budget: a scene is built on first use, and least-recently-used scenes that no
-// in-flight request references are evicted to make room.  Every request's image depends only on
-// its own parameters (per-sample Philox jitter keyed by seed and view id), so it is the same alone
-// and in any mix of requests.
+// vt_serve_submit, which splits each image into pieces of whole 8 x 4 tile rows of at most
+// `max_samples_per_piece` samples (a small request is one piece).  A dispatcher thread keeps up to
+// `max_inflight` launches on the device at once, each on its own stream: whenever a launch slot is
+// free it packs the oldest pending pieces, in arrival order, up to `max_views_per_launch` pieces
+// and `max_samples_per_launch` samples, into one persistent work-stealing launch of the batched
+// kernel (vt_batch.cu), followed by one resolve kernel that averages every piece's samples
+// straight into its rows of the caller's image (page-locked host memory is written by the kernel
+// itself, other memory through a device staging area and a copy).  Big requests thus run as a
+// sequence of bounded launches that small requests arriving meanwhile interleave with, every
+// launch is bounded in duration, and requests complete in arrival order as their last piece
+// retires.  Sample records live in buffers each slot allocates once, at start.
 //
-// With max_inflight = 1 and max_views_per_launch = 1 the same machinery is the plain baseline:
-// one launch per request, one launch at a time, in arrival order.
+// Brick grids of the scenes stay resident in a cache bounded by an HBM budget that also counts
+// the slots' buffers and any temporary buffer of a piece larger than a slot's: a scene is built
+// on first use, and least-recently-used scenes that no in-flight piece references are evicted to
+// make room.  Every request's image depends only on its own parameters (per-sample Philox jitter
+// keyed by seed and view id, pixels resolved in sample order), so it is the same alone, split
+// into pieces, and in any mix of requests.
+//
+// With max_inflight = 1, max_views_per_launch = 1 and max_samples_per_piece = 0 (no splitting)
+// the same machinery is the plain baseline: one launch per request, one launch at a time, in
+// arrival order.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -83,7 +91,7 @@ struct ServeScene {
     uint32_t palette[256];
     uint32_t nx = 0, ny = 0, nz = 0;
     int32_t grid = -1;
-    int32_t refs = 0;
+    int32_t refs = 0;  // in-flight and packed pieces
     bool loading = false;
     uint64_t last_use = 0;
     uint64_t bytes = 0;
@@ -92,11 +100,21 @@ struct ServeScene {
 struct ServeReq {
     vt_serve_request r;
     int32_t status = VT_ENOTREADY;
+    int32_t error = VT_OK;  // first failure of one of its pieces
+    bool cancelled = false;
     int64_t t_submit = 0, t_launch = 0, t_done = 0;
     uint64_t samples = 0;
-    void* d_samples = nullptr;
-    void* d_image = nullptr;
+    uint32_t pieces_pending = 0, pieces_inflight = 0;
+    bool mapped_known = false;
     void* h_image = nullptr;  // device address of a page-locked host_rgba, written directly
+};
+
+// Rows row0 .. row1 - 1 of a request's image; row0 is a multiple of 4 (the tile height) and so is
+// row1 unless it is the image's last row.
+struct Piece {
+    uint64_t req;
+    uint32_t row0, row1;
+    uint64_t samples;
 };
 
 struct Slot {
@@ -108,7 +126,12 @@ struct Slot {
     ResolveView* d_resolve = nullptr;
     ResolveView* h_resolve = nullptr;
     unsigned long long* d_counter = nullptr;
-    std::vector<uint64_t> reqs;
+    // sample records (16 B each) of up to `cap` samples, then an RGBA8 staging image of `cap`
+    // pixels for outputs the resolve cannot write directly
+    void* buf = nullptr;
+    uint64_t cap = 0;
+    uint64_t extra_bytes = 0;  // budget reserved for a temporary of an oversized piece
+    std::vector<Piece> pieces;
     bool busy = false;
 };
 
@@ -120,29 +143,63 @@ struct Service {
     std::thread worker;
     bool stop = false;
     std::vector<std::unique_ptr<ServeScene>> scenes;
-    std::deque<uint64_t> pending;
+    std::deque<Piece> pending;
     std::unordered_map<uint64_t, ServeReq> reqs;
     uint64_t next_id = 1;
     std::vector<Slot> slots;
-    uint64_t resident_bytes = 0, tick = 0;
+    // device bytes counted against the budget: resident grids, the slots' buffers, and the
+    // temporaries of oversized pieces in flight
+    uint64_t resident_bytes = 0, slot_bytes = 0, extra_bytes = 0, tick = 0;
     vt_serve_stats stats;
     TraceTuning tune;
-    std::atomic<int> pollers{0};  // threads inside vt_serve_poll (stop waits for them to leave)
 
+    ~Service();
     void run();
     int32_t admit_scene(std::unique_lock<std::mutex>& lk, int32_t scene);
-    void evict_for(uint64_t need);
-    void launch(Slot& slot, const std::vector<uint64_t>& ids);
-    void retire(Slot& slot);
+    bool evict_for(uint64_t need);
+    uint64_t used() const { return resident_bytes + slot_bytes + extra_bytes; }
+    bool pack(Slot& slot, std::unique_lock<std::mutex>& lk);
+    void launch(Slot& slot);
+    void retire(Slot& slot, int32_t error);
+    void fail_request(ServeReq& q, int32_t error);
+    void finalize(ServeReq& q);
 };
 
+// Services are held by shared pointers: an entry point copies the pointer under g_serve_mu and
+// keeps the service alive while it works on it, even if vt_serve_stop removes it meanwhile.
 static std::mutex g_serve_mu;
-static std::vector<std::unique_ptr<Service>> g_services;
+static std::vector<std::shared_ptr<Service>> g_services;
 
-static Service* lookup_service(int32_t id) {
+static std::shared_ptr<Service> lookup_service(int32_t id) {
     std::lock_guard<std::mutex> lk(g_serve_mu);
-    if (id < 0 || (size_t)id >= g_services.size() || !g_services[id]) return nullptr;
-    return g_services[id].get();
+    if (id < 0 || (size_t)id >= g_services.size()) return nullptr;
+    return g_services[id];
+}
+
+Service::~Service() {
+    if (worker.joinable()) {  // never stopped (library shutdown): stop the dispatcher first
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+            cv.notify_all();
+        }
+        worker.join();
+    }
+    for (Slot& sl : slots) {
+        if (sl.stream) cudaStreamSynchronize(sl.stream);
+        if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.t_begin) cudaEventDestroy(sl.t_begin);
+        if (sl.t_end) cudaEventDestroy(sl.t_end);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+        cudaFree(sl.d_table);
+        cudaFree(sl.d_resolve);
+        cudaFree(sl.d_counter);
+        cudaFree(sl.buf);
+        cudaFreeHost(sl.h_table);
+        cudaFreeHost(sl.h_resolve);
+    }
+    for (auto& sc : scenes)
+        if (sc->grid >= 0) vt_grid_destroy(sc->grid);
 }
 
 // Upper bound of a scene's resident bytes: directory + masks + payloads of every brick.
@@ -151,20 +208,23 @@ static uint64_t scene_bound(const ServeScene& s) {
     return bricks * (4 + 64 + 512) + 1024;
 }
 
-void Service::evict_for(uint64_t need) {
-    while (resident_bytes + need > cfg.hbm_budget_bytes) {
+// Evicts least-recently-used unreferenced scenes until `need` more bytes fit the budget; false
+// if they do not.
+bool Service::evict_for(uint64_t need) {
+    while (used() + need > cfg.hbm_budget_bytes) {
         ServeScene* victim = nullptr;
         for (auto& s : scenes)
             if (s->grid >= 0 && s->refs == 0 && !s->loading &&
                 (!victim || s->last_use < victim->last_use))
                 victim = s.get();
-        if (!victim) return;
+        if (!victim) return false;
         vt_grid_destroy(victim->grid);
         victim->grid = -1;
         resident_bytes -= victim->bytes;
         victim->bytes = 0;
         stats.evictions++;
     }
+    return true;
 }
 
 // Makes `scene` resident.  VT_OK, VT_EBUSY (no room until in-flight work ends), or an error.
@@ -173,9 +233,8 @@ int32_t Service::admit_scene(std::unique_lock<std::mutex>& lk, int32_t scene) {
     s.last_use = ++tick;
     if (s.grid >= 0) return VT_OK;
     const uint64_t need = scene_bound(s);
-    if (need > cfg.hbm_budget_bytes) return VT_ENOMEM;
-    evict_for(need);
-    if (resident_bytes + need > cfg.hbm_budget_bytes) return VT_EBUSY;
+    if (need + slot_bytes > cfg.hbm_budget_bytes) return VT_ENOMEM;
+    if (!evict_for(need)) return VT_EBUSY;
     s.loading = true;
     resident_bytes += need;  // reserved while the grid is built outside the lock
     lk.unlock();
@@ -193,93 +252,182 @@ int32_t Service::admit_scene(std::unique_lock<std::mutex>& lk, int32_t scene) {
     return VT_OK;
 }
 
-void Service::launch(Slot& slot, const std::vector<uint64_t>& ids) {
-    uint64_t item = 0, pixel = 0;
-    uint32_t n = 0;
-    std::vector<uint64_t> live;
-    for (uint64_t id : ids) {
-        ServeReq& q = reqs[id];
-        const vt_serve_request& r = q.r;
-        const uint64_t px = (uint64_t)r.camera.width * r.camera.height;
-        Grid* g = lookup_grid(scenes[r.scene]->grid);
-        // a page-locked output is written by the resolve kernel itself; else a device image and
-        // a copy
-        q.h_image = host_mapped(r.host_rgba);
-        cudaError_t e = cudaMallocAsync(&q.d_samples, px * r.spp * 16, slot.stream);
-        if (e == cudaSuccess && !q.h_image) e = cudaMallocAsync(&q.d_image, px * 4, slot.stream);
-        if (e != cudaSuccess || !g) {
-            cudaGetLastError();
-            if (q.d_samples) cudaFreeAsync(q.d_samples, slot.stream);
-            q.d_samples = nullptr;
-            q.status = VT_ENOMEM;
-            q.t_done = now_ns();
+// A request whose pieces are all finished or dropped gets its final status.
+void Service::finalize(ServeReq& q) {
+    if (q.status != VT_ENOTREADY || q.pieces_inflight || q.pieces_pending) return;
+    q.status = q.error != VT_OK ? q.error : (q.cancelled ? VT_ECANCELED : VT_OK);
+    q.t_done = now_ns();
+    if (q.status == VT_OK) {
+        stats.completed++;
+        stats.samples += q.samples;
+    }
+    cv_done.notify_all();
+}
+
+// Marks a request failed; its pending pieces are dropped as the dispatcher meets them.
+void Service::fail_request(ServeReq& q, int32_t error) {
+    if (q.error == VT_OK) q.error = error;
+    finalize(q);
+}
+
+// Moves the oldest pending pieces into the free `slot`; false when nothing could be packed.
+bool Service::pack(Slot& slot, std::unique_lock<std::mutex>& lk) {
+    uint64_t samples = 0;
+    slot.pieces.clear();
+    while (!pending.empty() && slot.pieces.size() < cfg.max_views_per_launch) {
+        const Piece pc = pending.front();
+        ServeReq& q = reqs[pc.req];
+        if (q.error != VT_OK || q.cancelled) {  // a failed request: drop its remaining pieces
+            pending.pop_front();
+            q.pieces_pending--;
+            finalize(q);
             continue;
         }
-        slot.h_table[n] = make_batch_view(*g, r.camera, (r.flags & VT_VIEW_LIGHT) ? &r.light : nullptr,
-                                          r.spp, r.seed, r.view_id, q.d_samples, item);
-        slot.h_resolve[n].samples = (const uint4*)q.d_samples;
-        slot.h_resolve[n].image = (uchar4*)(q.h_image ? q.h_image : q.d_image);
-        slot.h_resolve[n].pixel_begin = pixel;
-        slot.h_resolve[n].pixels = (uint32_t)px;
-        slot.h_resolve[n].spp = r.spp;
-        item += batch_view_items(r.camera, r.spp);
-        pixel += px;
-        ++n;
-        scenes[r.scene]->refs++;
-        q.t_launch = now_ns();
-        live.push_back(id);
+        if (!slot.pieces.empty() && samples + pc.samples > slot.cap) break;
+        uint64_t extra = 0;
+        if (pc.samples > slot.cap) {  // alone, and larger than the slot's buffers
+            extra = pc.samples * 20;
+            if (extra + slot_bytes > cfg.hbm_budget_bytes) {
+                pending.pop_front();
+                q.pieces_pending--;
+                fail_request(q, VT_ENOMEM);
+                continue;
+            }
+            if (!evict_for(extra)) break;  // wait for in-flight work to free memory
+        }
+        const int32_t rc = admit_scene(lk, q.r.scene);
+        if (rc == VT_EBUSY) break;  // wait for memory (the head of the line keeps its place)
+        if (pending.empty() || pending.front().req != pc.req || pending.front().row0 != pc.row0)
+            break;  // the service was stopped while the scene was built
+        pending.pop_front();
+        q.pieces_pending--;
+        if (rc != VT_OK) {
+            fail_request(q, rc);
+            continue;
+        }
+        if (extra) {
+            if (used() + extra > cfg.hbm_budget_bytes && !evict_for(extra)) {
+                pending.push_front(pc);  // the grid build took the room: try again later
+                q.pieces_pending++;
+                break;
+            }
+            slot.extra_bytes = extra;
+            extra_bytes += extra;
+        }
+        scenes[q.r.scene]->refs++;  // held until the piece retires
+        q.pieces_inflight++;
+        slot.pieces.push_back(pc);
+        samples += pc.samples;
+        if (extra) break;
     }
-    slot.reqs = live;
-    if (n == 0) {
-        cv_done.notify_all();
-        return;
+    return !slot.pieces.empty();
+}
+
+void Service::launch(Slot& slot) {
+    uint64_t samples = 0, pixels = 0;
+    for (const Piece& pc : slot.pieces) {
+        samples += pc.samples;
+        pixels += (uint64_t)(pc.row1 - pc.row0) * reqs[pc.req].r.camera.width;
     }
     cudaEventRecord(slot.t_begin, slot.stream);
-    cudaMemcpyAsync(slot.d_table, slot.h_table, n * sizeof(BatchView), cudaMemcpyHostToDevice,
-                    slot.stream);
-    cudaMemcpyAsync(slot.d_resolve, slot.h_resolve, n * sizeof(ResolveView),
-                    cudaMemcpyHostToDevice, slot.stream);
-    launch_batch(slot.d_table, n, item, slot.d_counter, tune, batch_blocks(n, item, tune),
-                 slot.stream);
-    const unsigned rblocks =
-        (unsigned)std::min<uint64_t>((pixel + 255) / 256, (uint64_t)state().sm_count * 16);
-    resolve_kernel<<<rblocks, 256, 0, slot.stream>>>(slot.d_resolve, n, pixel);
-    for (uint64_t id : live) {
-        ServeReq& q = reqs[id];
-        const uint64_t px = (uint64_t)q.r.camera.width * q.r.camera.height;
-        if (!q.h_image) {
-            cudaMemcpyAsync(q.r.host_rgba, q.d_image, px * 4, cudaMemcpyDeviceToHost, slot.stream);
-            cudaFreeAsync(q.d_image, slot.stream);
-        }
-        cudaFreeAsync(q.d_samples, slot.stream);
-        q.d_samples = q.d_image = nullptr;
-        q.h_image = nullptr;
+    char* base = (char*)slot.buf;
+    char* staging = base + slot.cap * 16;
+    void* temp = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (slot.extra_bytes) {
+        e = cudaMallocAsync(&temp, samples * 16 + pixels * 4, slot.stream);
+        base = (char*)temp;
+        staging = base + samples * 16;
     }
+    uint64_t item = 0, pix = 0, off = 0;
+    uint32_t n = 0;
+    for (const Piece& pc : slot.pieces) {
+        if (e != cudaSuccess) break;
+        ServeReq& q = reqs[pc.req];
+        const vt_serve_request& r = q.r;
+        const uint32_t W = r.camera.width;
+        Grid* g = lookup_grid(scenes[r.scene]->grid);
+        if (!g) {
+            e = cudaErrorInvalidValue;
+            break;
+        }
+        if (!q.mapped_known) {
+            q.h_image = host_mapped(r.host_rgba);
+            q.mapped_known = true;
+        }
+        if (!q.t_launch) q.t_launch = now_ns();
+        const uint64_t px = (uint64_t)(pc.row1 - pc.row0) * W;
+        void* out = base + off * 16;
+        slot.h_table[n] = make_batch_view(*g, r.camera, (r.flags & VT_VIEW_LIGHT) ? &r.light : nullptr,
+                                          r.spp, r.seed, r.view_id, out, item, pc.row0);
+        slot.h_resolve[n].samples = (const uint4*)out;
+        slot.h_resolve[n].image = q.h_image ? (uchar4*)q.h_image + (uint64_t)pc.row0 * W
+                                            : (uchar4*)(staging + pix * 4);
+        slot.h_resolve[n].pixel_begin = pix;
+        slot.h_resolve[n].pixels = (uint32_t)px;
+        slot.h_resolve[n].spp = r.spp;
+        item += batch_rows_items(r.camera, r.spp, pc.row0, pc.row1);
+        pix += px;
+        off += pc.samples;
+        ++n;
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(slot.d_table, slot.h_table, n * sizeof(BatchView), cudaMemcpyHostToDevice,
+                            slot.stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(slot.d_resolve, slot.h_resolve, n * sizeof(ResolveView),
+                            cudaMemcpyHostToDevice, slot.stream);
+    if (e == cudaSuccess)
+        e = launch_batch(slot.d_table, n, item, slot.d_counter, tune, batch_blocks(n, item, tune),
+                         slot.stream);
+    if (e == cudaSuccess) {
+        const unsigned rblocks =
+            (unsigned)std::min<uint64_t>((pix + 255) / 256, (uint64_t)state().sm_count * 16);
+        resolve_kernel<<<rblocks, 256, 0, slot.stream>>>(slot.d_resolve, n, pix);
+        e = cudaGetLastError();
+    }
+    pix = 0;
+    for (const Piece& pc : slot.pieces) {
+        if (e != cudaSuccess) break;
+        const ServeReq& q = reqs[pc.req];
+        const uint64_t px = (uint64_t)(pc.row1 - pc.row0) * q.r.camera.width;
+        if (!q.h_image)
+            e = cudaMemcpyAsync(q.r.host_rgba + (uint64_t)pc.row0 * q.r.camera.width * 4,
+                                staging + pix * 4, px * 4, cudaMemcpyDeviceToHost, slot.stream);
+        pix += px;
+    }
+    if (temp) cudaFreeAsync(temp, slot.stream);
     cudaEventRecord(slot.t_end, slot.stream);
     cudaEventRecord(slot.done, slot.stream);
     slot.busy = true;
     stats.launches++;
     stats.views_launched += n;
+    if (e != cudaSuccess) {  // nothing waits on a failed launch: retire it now
+        cudaGetLastError();
+        cudaStreamSynchronize(slot.stream);
+        retire(slot, VT_ECUDA);
+    }
 }
 
-void Service::retire(Slot& slot) {
-    const int64_t t = now_ns();
-    float ms = 0.0f;
-    if (cudaEventElapsedTime(&ms, slot.t_begin, slot.t_end) == cudaSuccess)
-        stats.device_ns += (uint64_t)((double)ms * 1e6);
-    else
-        cudaGetLastError();
-    for (uint64_t id : slot.reqs) {
-        ServeReq& q = reqs[id];
-        q.status = VT_OK;
-        q.t_done = t;
-        scenes[q.r.scene]->refs--;
-        stats.completed++;
-        stats.samples += q.samples;
+void Service::retire(Slot& slot, int32_t error) {
+    if (error == VT_OK) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, slot.t_begin, slot.t_end) == cudaSuccess)
+            stats.device_ns += (uint64_t)((double)ms * 1e6);
+        else
+            cudaGetLastError();
     }
-    slot.reqs.clear();
+    for (const Piece& pc : slot.pieces) {
+        ServeReq& q = reqs[pc.req];
+        scenes[q.r.scene]->refs--;
+        q.pieces_inflight--;
+        if (error != VT_OK && q.error == VT_OK) q.error = error;
+        finalize(q);
+    }
+    extra_bytes -= slot.extra_bytes;
+    slot.extra_bytes = 0;
+    slot.pieces.clear();
     slot.busy = false;
-    cv_done.notify_all();
 }
 
 void Service::run() {
@@ -290,54 +438,29 @@ void Service::run() {
         for (Slot& sl : slots) {
             if (!sl.busy) continue;
             const cudaError_t q = cudaEventQuery(sl.done);
-            if (q == cudaSuccess)
-                retire(sl);
-            else if (q == cudaErrorNotReady)
+            if (q == cudaSuccess) {
+                retire(sl, VT_OK);
+            } else if (q == cudaErrorNotReady) {
                 busy = true;
-            else {  // a failed launch: report it on its requests
-                for (uint64_t id : sl.reqs) {
-                    reqs[id].status = VT_ECUDA;
-                    reqs[id].t_done = now_ns();
-                    scenes[reqs[id].r.scene]->refs--;
-                }
-                sl.reqs.clear();
-                sl.busy = false;
-                cv_done.notify_all();
+            } else {  // a failed launch: report it on its requests
+                cudaGetLastError();
+                retire(sl, VT_ECUDA);
             }
         }
         if (stop) {
-            for (uint64_t id : pending) {
-                reqs[id].status = VT_ECANCELED;
-                reqs[id].t_done = now_ns();
+            for (const Piece& pc : pending) {
+                ServeReq& q = reqs[pc.req];
+                q.cancelled = true;
+                q.pieces_pending--;
             }
-            if (!pending.empty()) cv_done.notify_all();
+            for (const Piece& pc : pending) finalize(reqs[pc.req]);
             pending.clear();
             if (!busy) break;
         }
-        // admit the oldest pending requests into free slots
+        // admit the oldest pending pieces into free slots
         for (Slot& sl : slots) {
             if (sl.busy || pending.empty() || stop) continue;
-            std::vector<uint64_t> pack;
-            uint64_t samples = 0;
-            while (!pending.empty() && pack.size() < cfg.max_views_per_launch) {
-                const uint64_t id = pending.front();
-                ServeReq& q = reqs[id];
-                if (!pack.empty() && samples + q.samples > cfg.max_samples_per_launch) break;
-                const int32_t rc = admit_scene(lk, q.r.scene);
-                if (rc == VT_EBUSY) break;  // wait for memory (head of line keeps its place)
-                pending.pop_front();
-                if (rc != VT_OK) {
-                    q.status = rc;
-                    q.t_done = now_ns();
-                    cv_done.notify_all();
-                    continue;
-                }
-                scenes[q.r.scene]->refs++;  // held while packed; launch() takes its own
-                pack.push_back(id);
-                samples += q.samples;
-            }
-            for (uint64_t id : pack) scenes[reqs[id].r.scene]->refs--;
-            if (!pack.empty()) launch(sl, pack);
+            if (pack(sl, lk)) launch(sl);
             if (sl.busy) busy = true;
         }
         stats.pending = pending.size();
@@ -354,6 +477,27 @@ void Service::run() {
 
 using namespace vt;
 
+// Stops every service (vt_shutdown): their dispatchers finish in-flight launches and cancel the
+// rest before the grids they reference are freed.
+void vt_serve_release_all() {
+    std::vector<std::shared_ptr<Service>> all;
+    {
+        std::lock_guard<std::mutex> lk(g_serve_mu);
+        all.swap(g_services);
+    }
+    for (auto& s : all) {
+        if (!s) continue;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stop = true;
+            s->cv.notify_all();
+        }
+        if (s->worker.joinable()) s->worker.join();
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->cv_done.notify_all();
+    }
+}
+
 extern "C" {
 
 int32_t vt_serve_default_config(vt_serve_config* cfg) {
@@ -361,9 +505,10 @@ int32_t vt_serve_default_config(vt_serve_config* cfg) {
     cfg->hbm_budget_bytes = 120ull << 30;
     cfg->max_inflight = 4;
     cfg->max_views_per_launch = 64;
-    cfg->max_samples_per_launch = 64ull << 20;
+    cfg->max_samples_per_launch = 16ull << 20;
     cfg->poll_interval_us = 20;
     cfg->refill_min = 32;
+    cfg->max_samples_per_piece = 4ull << 20;
     return VT_OK;
 }
 
@@ -371,20 +516,25 @@ int32_t vt_serve_start(const vt_serve_config* cfg, int32_t* service_out) {
     if (!cfg || !service_out) return fail(VT_EINVAL, "vt_serve_start: null argument");
     if (cfg->max_inflight < 1 || cfg->max_inflight > 32 || cfg->max_views_per_launch < 1 ||
         cfg->max_views_per_launch > kMaxBatchViews || cfg->refill_min < 1 || cfg->refill_min > 32 ||
-        cfg->max_samples_per_launch == 0)
+        cfg->max_samples_per_launch == 0 || cfg->max_samples_per_launch > (1ull << 32))
         return fail(VT_EINVAL, "vt_serve_start: max_inflight 1..32, max_views_per_launch 1..256, "
-                               "refill_min 1..32, max_samples_per_launch > 0");
+                               "refill_min 1..32, max_samples_per_launch 1..2^32");
     int32_t rc = ensure_init();
     if (rc) return rc;
-    std::unique_ptr<Service> s(new Service());
+    std::shared_ptr<Service> s(new Service());
     s->cfg = *cfg;
     if (s->cfg.poll_interval_us == 0) s->cfg.poll_interval_us = 20;
     memset(&s->stats, 0, sizeof(s->stats));
     s->tune.refill_min = cfg->refill_min;
     s->tune.blocks_per_sm = 0;
     s->tune.persistent = 1;
+    s->slot_bytes = cfg->max_inflight * cfg->max_samples_per_launch * 20;
+    if (s->slot_bytes > cfg->hbm_budget_bytes)
+        return fail(VT_ENOMEM, "vt_serve_start: the launch slots' sample buffers (max_inflight x "
+                               "max_samples_per_launch x 20 B) exceed the HBM budget");
     s->slots.resize(cfg->max_inflight);
     for (Slot& sl : s->slots) {
+        sl.cap = cfg->max_samples_per_launch;
         cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreate(&sl.t_begin);
@@ -392,15 +542,21 @@ int32_t vt_serve_start(const vt_serve_config* cfg, int32_t* service_out) {
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_table, kMaxBatchViews * sizeof(BatchView));
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_resolve, kMaxBatchViews * sizeof(ResolveView));
         if (e == cudaSuccess) e = cudaMalloc(&sl.d_counter, sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc(&sl.buf, sl.cap * 20);
         if (e == cudaSuccess) e = cudaMallocHost(&sl.h_table, kMaxBatchViews * sizeof(BatchView));
         if (e == cudaSuccess) e = cudaMallocHost(&sl.h_resolve, kMaxBatchViews * sizeof(ResolveView));
-        if (e != cudaSuccess) return cuda_fail(e, "vt_serve_start: slot resources");
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return e == cudaErrorMemoryAllocation
+                       ? fail(VT_ENOMEM, "vt_serve_start: slot buffers")
+                       : cuda_fail(e, "vt_serve_start: slot resources");
+        }
     }
     Service* raw = s.get();
     int32_t id;
     {
         std::lock_guard<std::mutex> lk(g_serve_mu);
-        g_services.push_back(std::move(s));
+        g_services.push_back(s);
         id = (int32_t)g_services.size() - 1;
     }
     raw->worker = std::thread([raw] { raw->run(); });
@@ -410,7 +566,7 @@ int32_t vt_serve_start(const vt_serve_config* cfg, int32_t* service_out) {
 
 int32_t vt_serve_add_scene(int32_t service, const uint8_t* voxels, const uint32_t* palette,
                            uint32_t nx, uint32_t ny, uint32_t nz, int32_t* scene_out) {
-    Service* s = lookup_service(service);
+    std::shared_ptr<Service> s = lookup_service(service);
     if (!s) return fail(VT_ENOTFOUND, "vt_serve_add_scene: unknown service");
     if (!voxels || !palette || !scene_out) return fail(VT_EINVAL, "vt_serve_add_scene: null argument");
     int32_t rc = check_dims(nx, ny, nz);
@@ -422,6 +578,7 @@ int32_t vt_serve_add_scene(int32_t service, const uint8_t* voxels, const uint32_
     sc->ny = ny;
     sc->nz = nz;
     std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return fail(VT_ECANCELED, "vt_serve_add_scene: service stopping");
     s->scenes.push_back(std::move(sc));
     *scene_out = (int32_t)s->scenes.size() - 1;
     return VT_OK;
@@ -429,13 +586,14 @@ int32_t vt_serve_add_scene(int32_t service, const uint8_t* voxels, const uint32_
 
 int32_t vt_serve_submit(int32_t service, const vt_serve_request* req, uint64_t* request_id) {
     const int64_t t = now_ns();
-    Service* s = lookup_service(service);
+    std::shared_ptr<Service> s = lookup_service(service);
     if (!s) return fail(VT_ENOTFOUND, "vt_serve_submit: unknown service");
     if (!req || !request_id || !req->host_rgba) return fail(VT_EINVAL, "vt_serve_submit: null argument");
     int32_t rc = check_camera(&req->camera);
     if (rc) return rc;
     if (req->spp == 0 || req->spp > 64) return fail(VT_EINVAL, "vt_serve_submit: spp must be 1..64");
-    if ((uint64_t)req->camera.width * req->camera.height * req->spp >= (1ull << 32))
+    const uint64_t row_samples = (uint64_t)req->camera.width * req->spp;
+    if (row_samples * req->camera.height >= (1ull << 32))
         return fail(VT_ELIMIT, "vt_serve_submit: 2^32 or more samples in one request");
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) return fail(VT_ECANCELED, "vt_serve_submit: service stopping");
@@ -445,8 +603,17 @@ int32_t vt_serve_submit(int32_t service, const vt_serve_request* req, uint64_t* 
     ServeReq& q = s->reqs[id];
     q.r = *req;
     q.t_submit = t;
-    q.samples = (uint64_t)req->camera.width * req->camera.height * req->spp;
-    s->pending.push_back(id);
+    q.samples = row_samples * req->camera.height;
+    // pieces of whole tile rows (4 image rows) of at most max_samples_per_piece samples
+    const uint32_t H = req->camera.height;
+    uint32_t rows = H;
+    if (s->cfg.max_samples_per_piece)
+        rows = (uint32_t)std::max<uint64_t>(4, s->cfg.max_samples_per_piece / row_samples / 4 * 4);
+    for (uint32_t r0 = 0; r0 < H; r0 += rows) {
+        const uint32_t r1 = std::min(H, r0 + rows);
+        s->pending.push_back(Piece{id, r0, r1, (uint64_t)(r1 - r0) * row_samples});
+        q.pieces_pending++;
+    }
     s->stats.submitted++;
     *request_id = id;
     s->cv.notify_one();
@@ -455,19 +622,8 @@ int32_t vt_serve_submit(int32_t service, const vt_serve_request* req, uint64_t* 
 
 int32_t vt_serve_poll(int32_t service, uint64_t request_id, uint32_t timeout_us,
                       vt_serve_timing* timing) {
-    Service* s = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_serve_mu);
-        if (service >= 0 && (size_t)service < g_services.size() && g_services[service]) {
-            s = g_services[service].get();
-            s->pollers.fetch_add(1);
-        }
-    }
+    std::shared_ptr<Service> s = lookup_service(service);
     if (!s) return fail(VT_ENOTFOUND, "vt_serve_poll: unknown service");
-    struct Leave {
-        Service* s;
-        ~Leave() { s->pollers.fetch_sub(1); }
-    } leave{s};
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->reqs.find(request_id);
     if (it == s->reqs.end()) return fail(VT_ENOTFOUND, "vt_serve_poll: unknown request");
@@ -494,7 +650,7 @@ int32_t vt_serve_poll(int32_t service, uint64_t request_id, uint32_t timeout_us,
 }
 
 int32_t vt_serve_get_stats(int32_t service, vt_serve_stats* out) {
-    Service* s = lookup_service(service);
+    std::shared_ptr<Service> s = lookup_service(service);
     if (!s) return fail(VT_ENOTFOUND, "vt_serve_get_stats: unknown service");
     if (!out) return fail(VT_EINVAL, "vt_serve_get_stats: null output");
     std::lock_guard<std::mutex> lk(s->mu);
@@ -505,7 +661,7 @@ int32_t vt_serve_get_stats(int32_t service, vt_serve_stats* out) {
 }
 
 int32_t vt_serve_stop(int32_t service) {
-    std::unique_ptr<Service> s;
+    std::shared_ptr<Service> s;
     {
         std::lock_guard<std::mutex> lk(g_serve_mu);
         if (service < 0 || (size_t)service >= g_services.size() || !g_services[service])
@@ -518,28 +674,12 @@ int32_t vt_serve_stop(int32_t service) {
         s->cv.notify_all();
     }
     if (s->worker.joinable()) s->worker.join();
-    // every request is now done or cancelled: wake pollers and wait for them to leave
-    while (s->pollers.load() > 0) {
-        {
-            std::lock_guard<std::mutex> lk(s->mu);
-            s->cv_done.notify_all();
-        }
-        std::this_thread::sleep_for(std::chrono::microseconds(100));
+    {
+        // every request is now done or cancelled: wake pollers (they hold the service alive
+        // until they return; its streams and grids go with the last reference)
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->cv_done.notify_all();
     }
-    for (Slot& sl : s->slots) {
-        if (sl.stream) cudaStreamSynchronize(sl.stream);
-        if (sl.done) cudaEventDestroy(sl.done);
-        if (sl.t_begin) cudaEventDestroy(sl.t_begin);
-        if (sl.t_end) cudaEventDestroy(sl.t_end);
-        if (sl.stream) cudaStreamDestroy(sl.stream);
-        cudaFree(sl.d_table);
-        cudaFree(sl.d_resolve);
-        cudaFree(sl.d_counter);
-        cudaFreeHost(sl.h_table);
-        cudaFreeHost(sl.h_resolve);
-    }
-    for (auto& sc : s->scenes)
-        if (sc->grid >= 0) vt_grid_destroy(sc->grid);
     return VT_OK;
 }
 
