@@ -15,8 +15,20 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE = os.environ.get("VTRACE_REFERENCE", "/root/reference")
-SHADER = os.path.join(REFERENCE, "shaders", "trace.frag")
+# The reference source tree: VTRACE_REFERENCE when set, else where this build's recipe finds it in
+# the build container.  It is read here only (the GPU machine has no copy); tests that need it ask
+# reference_root() and skip when it returns None.
+_DEFAULT_REFERENCE = "/root/reference"
+
+
+def reference_root():
+    """The reference source tree's root, or None where it is absent."""
+    root = os.environ.get("VTRACE_REFERENCE") or _DEFAULT_REFERENCE
+    return root if os.path.isdir(root) else None
+
+
+REFERENCE = reference_root()
+SHADER = os.path.join(REFERENCE, "shaders", "trace.frag") if REFERENCE else ""
 
 ORACLE_SO = os.path.join(BUILD, "libvt_oracle.so")
 
@@ -48,7 +60,7 @@ def build_oracle(force=False):
 
 def build_ref(force=False):
     """Returns the list of built libraries, or [] when the reference tree is absent."""
-    if not os.path.exists(SHADER):
+    if not SHADER or not os.path.exists(SHADER):
         return []
     compat = os.path.join(HERE, "glsl_compat.hpp")
     harness = os.path.join(HERE, "ref_harness.cpp")

@@ -2,7 +2,7 @@
  * glsl_compat.hpp — just enough of GLSL 4.60 in C++ to compile vtrace's fragment shader
  * (shaders/trace.frag) as a host function (TEST INFRASTRUCTURE ONLY).
  *
- * The build recipe (oracle/Makefile, target `ref`) feeds the shader text, minus its `#version`
+ * The build recipe (oracle/build.py, build_ref()) feeds the shader text, minus its `#version`
  * and `#extension` directives, to g++ with this header force-included, so the traversal that runs
  * is the reference's own source.  The header fixes the semantics GLSL leaves to the driver:
  *  - arithmetic is IEEE binary32, round to nearest, no contraction (-ffp-contract=off);

@@ -112,3 +112,38 @@ def test_camera_look_at():
     assert np.allclose(c.right, [2 * th, 0, 0], atol=1e-7)
     with pytest.raises(vt.VtError):
         vt.camera_look_at((0, 0, 0), (0, 0, 0))
+
+
+STRUCTS = [("vt_camera", "Camera"), ("vt_light", "Light"), ("vt_grid_info", "GridInfo"),
+           ("vt_trace_stats", "TraceStats"), ("vt_tuning", "Tuning"), ("vt_view", "View"),
+           ("vt_serve_config", "ServeConfig"), ("vt_serve_request", "ServeRequest"),
+           ("vt_serve_timing", "ServeTiming"), ("vt_serve_stats", "ServeStats"),
+           ("vt_path_params", "PathParams"), ("vt_footprint", "Footprint"),
+           ("vt_vox_info", "VoxInfo"), ("vt_vox_model", "VoxModel"),
+           ("render_tick_info", "RenderTickInfo"), ("user_input", "UserInput")]
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every ctypes mirror has the size and field offsets the C compiler gives the header's
+    struct (a mirror that is too small lets the library write past it)."""
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "vtrace.h"', "int main(void) {"]
+    for cname, pyname in STRUCTS:
+        cls = getattr(vt, pyname)
+        lines.append('printf("%s @sizeof %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in cls._fields_:
+            lines.append('printf("%s %s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.check_call(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                           str(exe)])
+    got = {}
+    for line in subprocess.check_output([str(exe)], text=True).splitlines():
+        c, f, v = line.split()
+        got[(c, f)] = int(v)
+    for cname, pyname in STRUCTS:
+        cls = getattr(vt, pyname)
+        assert ctypes.sizeof(cls) == got[(cname, "@sizeof")], cname
+        for fname, _ in cls._fields_:
+            assert getattr(cls, fname).offset == got[(cname, fname)], (cname, fname)

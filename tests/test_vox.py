@@ -6,9 +6,10 @@ import numpy as np
 import pytest
 
 import vtrace_gb300 as vt
+from oracle import build as obuild
 from oracle import vox as ovox
 
-REF = os.environ.get("VTRACE_REFERENCE", "/root/reference")
+REF = obuild.reference_root()
 
 
 def random_model(rng, size, count, ymax=None, zmax=None):
@@ -83,9 +84,9 @@ def test_malformed_files_are_rejected():
 
 @pytest.mark.parametrize("name", ["AncientTemple", "Treasure"])
 def test_vtrace_assets(name):
-    path = os.path.join(REF, "assets", name + ".vox")
-    if not os.path.exists(path):
+    if REF is None or not os.path.exists(os.path.join(REF, "assets", name + ".vox")):
         pytest.skip("vtrace's assets are not on this machine")
+    path = os.path.join(REF, "assets", name + ".vox")
     buf = open(path, "rb").read()
     info = vt.vox_inspect(buf)
     assert info["models"] >= 1 and info["has_palette"]

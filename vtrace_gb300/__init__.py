@@ -103,7 +103,7 @@ class ServeConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
                 ("max_views_per_launch", ctypes.c_uint32),
                 ("max_samples_per_launch", ctypes.c_uint64), ("poll_interval_us", ctypes.c_uint32),
-                ("refill_min", ctypes.c_uint32)]
+                ("refill_min", ctypes.c_uint32), ("max_samples_per_piece", ctypes.c_uint64)]
 
 
 class ServeRequest(ctypes.Structure):

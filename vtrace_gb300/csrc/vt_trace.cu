@@ -239,85 +239,29 @@ __global__ void __launch_bounds__(256) render_persistent_kernel(
 
 constexpr int kUnitWait = 4;
 
-// Ray staging of the persistent ray-buffer tracer: each warp claims rays in chunks of 32 with one
-// atomic and copies them into shared memory with cp.async, two chunks ahead of use (one being
-// consumed, one in flight), so that lanes refilled with new rays read them from shared memory
-// instead of waiting on a global load.
-constexpr uint32_t kStageRays = 32;
-constexpr int kPersistentWarps = 8;  // 256-thread blocks
-
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-
-// Claims the next kStageRays rays of the buffer for the warp and starts copying them (three
-// 8-byte words each) into `buf`; `num` is how many exist (0 once the buffer is used up).
-__device__ __forceinline__ uint64_t stage_chunk(unsigned long long* counter,
-                                                const float2* __restrict__ rays, uint64_t n,
-                                                float2* buf, uint32_t lane, uint32_t& num) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(counter, (unsigned long long)kStageRays);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    num = base < n ? (n - base < kStageRays ? (uint32_t)(n - base) : kStageRays) : 0u;
-    for (uint32_t k = lane; k < num * 3u; k += 32u) cp_async8(buf + k, rays + base * 3u + k);
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-    return base;
-}
-
-__device__ __forceinline__ void stage_wait() {
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    __syncwarp();
-}
-
 // n_dev: nullptr, or the device-side ray count (at most n), read at the start (ray queues whose
 // length the host does not know).
-__global__ void __launch_bounds__(256, 4) trace_rays_persistent_kernel(
+__global__ void __launch_bounds__(256) trace_rays_persistent_kernel(
     GridView g, const float2* __restrict__ rays, uint64_t n, uint4* __restrict__ out,
     unsigned long long* __restrict__ counter, uint32_t refill_min,
     const unsigned int* __restrict__ n_dev) {
-    __shared__ __align__(16) float2 stage[kPersistentWarps][2][kStageRays * 3];
     if (n_dev) n = min((uint64_t)*n_dev, n);
     const uint32_t lane = threadIdx.x & 31u;
-    // warp-uniform staging state: the chunk being handed out (buffer, first ray, size, rays
-    // handed out so far) and the chunk staged behind it
-    float2* cur_buf = stage[threadIdx.x >> 5][0];
-    float2* nxt_buf = stage[threadIdx.x >> 5][1];
-    uint32_t cur_num, nxt_num;
-    uint64_t cur_base = stage_chunk(counter, rays, n, cur_buf, lane, cur_num);
-    uint64_t nxt_base = stage_chunk(counter, rays, n, nxt_buf, lane, nxt_num);
-    stage_wait();
-    uint32_t used = 0;
-    bool more = cur_num != 0;
     LaneRay R;
     bool busy = false;
     uint64_t idx = 0;
+    bool more = true;
     int wait_w = 0, wait_c = 0;  // warp-uniform: iterations a unit kind was passed over
     for (;;) {
         uint32_t idle = __ballot_sync(0xFFFFFFFFu, !busy);
         while (more && __popc(idle) >= (int)refill_min) {
-            if (used == cur_num) {
-                // the chunk in use is spent: move to the staged one and refill the spent buffer
-                if (nxt_num == 0) {
-                    more = false;
-                    break;
-                }
-                stage_wait();
-                float2* spent = cur_buf;
-                cur_buf = nxt_buf;
-                cur_base = nxt_base;
-                cur_num = nxt_num;
-                used = 0;
-                nxt_buf = spent;
-                nxt_base = stage_chunk(counter, rays, n, nxt_buf, lane, nxt_num);
-            }
-            const uint32_t avail = cur_num - used;
-            const uint32_t rank = __popc(idle & ((1u << lane) - 1u));
-            if (!busy && rank < avail) {
-                const float2* r = cur_buf + 3u * (used + rank);
-                const float2 a = r[0], b = r[1], c = r[2];
+            uint64_t item;
+            const uint64_t base = warp_fetch(counter, idle, lane, item);
+            if (base + __popc(idle) >= n) more = false;
+            if (!busy && item < n) {
+                const float2 a = __ldg(rays + 3 * item), b = __ldg(rays + 3 * item + 1),
+                             c = __ldg(rays + 3 * item + 2);
                 const float o[3] = {a.x, a.y, b.x}, d[3] = {b.y, c.x, c.y};
-                const uint64_t item = cur_base + used + rank;
                 const int st = ray_begin(g, o, d, R);
                 if (st == kRayRunning) {
                     busy = true;
@@ -327,7 +271,6 @@ __global__ void __launch_bounds__(256, 4) trace_rays_persistent_kernel(
                     out[item] = make_uint4(h.w0, h.w1, h.w2, h.w3);
                 }
             }
-            used += min((uint32_t)__popc(idle), avail);
             idle = __ballot_sync(0xFFFFFFFFu, !busy);
         }
         if (!more && idle == 0xFFFFFFFFu) break;
@@ -356,7 +299,6 @@ __global__ void __launch_bounds__(256, 4) trace_rays_persistent_kernel(
             }
         }
     }
-    stage_wait();  // no copy may still target this block's shared memory when it exits
 }
 
 static int resident_blocks(const void* kernel) {
