@@ -318,10 +318,12 @@ __device__ __forceinline__ float add_chain(float s, float d, int32_t k) {
         const float lim = __fsub_rn(top, u);  // the largest value of the binade
         float take = __int2float_rn(k);
         if (__fmaf_rn(take, dp, s) > lim) {
-            // fewer than k steps stay in the binade: the largest j with s + j dp <= lim
-            take = floorf(__fdiv_rn(__fsub_rn(lim, s), dp));
-            if (__fmaf_rn(take, dp, s) > lim) take = __fsub_rn(take, 1.0f);
-            else if (__fmaf_rn(__fadd_rn(take, 1.0f), dp, s) <= lim) take = __fadd_rn(take, 1.0f);
+            // fewer than k steps stay in the binade: the largest j with s + j dp <= lim, from an
+            // estimate settled by exact comparisons (both loops end: s <= lim, s + k dp > lim)
+            take = fminf(fmaxf(floorf(__fdividef(__fsub_rn(lim, s), dp)), 0.0f),
+                         __int2float_rn(k - 1));
+            while (__fmaf_rn(take, dp, s) > lim) take = __fsub_rn(take, 1.0f);
+            while (__fmaf_rn(__fadd_rn(take, 1.0f), dp, s) <= lim) take = __fadd_rn(take, 1.0f);
         }
         s = __fmaf_rn(take, dp, s);
         k -= __float2int_rn(take);
