@@ -799,9 +799,12 @@ def serve_run(vt, svc_kwargs, scenes, reqs, torch):
            "msamples_per_s": samples / makespan / 1e6,
            "launches": st["launches"] - st0["launches"], "requests": len(reqs)}
     busy = (st["device_ns"] - st0["device_ns"]) / 1e9
-    if busy > 0:
+    if svc_kwargs.get("plain"):
+        # one launch at a time: the launches' summed device time is the time the GPU was busy
         out["device_busy_s"] = busy
         out["device_busy_fraction"] = busy / makespan
+    else:
+        out["launch_device_s_sum"] = busy  # concurrent launches overlap: not a busy time
     return out
 
 

@@ -505,7 +505,7 @@ int32_t vt_serve_default_config(vt_serve_config* cfg) {
     cfg->hbm_budget_bytes = 120ull << 30;
     cfg->max_inflight = 4;
     cfg->max_views_per_launch = 64;
-    cfg->max_samples_per_launch = 16ull << 20;
+    cfg->max_samples_per_launch = 8ull << 20;
     cfg->poll_interval_us = 20;
     cfg->refill_min = 32;
     cfg->max_samples_per_piece = 4ull << 20;
