@@ -167,7 +167,9 @@ typedef struct vt_tuning {
     int32_t blocks_per_sm;
     uint32_t persistent;
     uint32_t wavefront; /* VT_KERNEL_RENDER tile launches: trace shadow rays in a second pass over
-                           a compacted queue instead of in the primary ray's thread.
+                           a compacted queue instead of in the primary ray's thread; with
+                           persistent = 1: resident warps take whole 8 x 4 tiles and queue their
+                           shadow rays per warp, tracing them 32 at a time.
                            VT_KERNEL_PATH: advance all paths one vertex at a time through ray
                            queues (the default; faster than either per-path form) */
     uint32_t tile_shape;  /* VT_KERNEL_RENDER fused tile launch: the pixels of one warp, VT_TILE_* */

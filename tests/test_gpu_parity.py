@@ -417,7 +417,7 @@ def test_empty_space_skipping_is_exact(torch, dims, count):
 
 
 @pytest.mark.parametrize("persistent,refill_min,wavefront",
-                         [(0, 16, 0), (0, 16, 1), (1, 1, 0), (1, 8, 0), (1, 32, 0)])
+                         [(0, 16, 0), (0, 16, 1), (1, 1, 0), (1, 8, 0), (1, 32, 0), (1, 32, 1)])
 def test_launch_shapes_agree(torch, persistent, refill_min, wavefront):
     """Tile launches (shadow rays fused or in a second pass) and persistent launches at any refill
     threshold give identical records."""

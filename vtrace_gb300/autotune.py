@@ -6,8 +6,9 @@ fastest and installs it with vt_set_tuning.  The search spaces:
 
   render       the fused tile launch over warp tiles of 8x4, 4x8, 16x2 and 32x1 pixels and blocks
                of 1, 2, 4 and 8 warps (the pixel-tile shape and rays per block); the two-pass form
-               (shadow rays compacted into full warps); persistent warps refilled once 8, 16 or 32
-               lanes are idle (the compaction interval)
+               (shadow rays compacted into full warps by a second kernel); persistent warps
+               refilled once 8, 16 or 32 lanes are idle (the compaction interval); persistent
+               warps taking whole tiles and tracing their queued shadow rays 32 at a time
   trace_rays   one thread per ray, or persistent warps with a refill threshold of 1, 4, 8, 16, 24
                or 32 idle lanes and 2 or as many as fit resident blocks per SM
   batch        whole 8x4 tile units per warp, or per-lane refill at 4, 8 or 16 idle lanes, with 2
@@ -40,6 +41,7 @@ def render_candidates(tiles=(TILE_8X4, TILE_4X8, TILE_16X2, TILE_32X1), warps=(1
     out = [tuning(tile_shape=t, block_warps=w) for t, w in itertools.product(tiles, warps)]
     out.append(tuning(wavefront=True))
     out += [tuning(refill_min=r, persistent=True) for r in refill]
+    out.append(tuning(persistent=True, wavefront=True))  # whole tiles, shadow rays in full warps
     return out
 
 
@@ -67,6 +69,8 @@ def key(kernel, c):
     if kernel == KERNEL_BATCH:
         form = "tiles" if c["refill_min"] >= 32 else "lanes_r%d" % c["refill_min"]
         return "%s_b%d" % (form, c["blocks_per_sm"])
+    if c["persistent"] and c["wavefront"] and kernel == KERNEL_RENDER:
+        return "queued_shadows_b%d" % c["blocks_per_sm"]
     if c["persistent"]:
         return "persistent_r%d_b%d" % (c["refill_min"], c["blocks_per_sm"])
     if c["wavefront"]:

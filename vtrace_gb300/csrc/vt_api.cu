@@ -82,6 +82,9 @@ unsigned long long* next_counter() {
 cudaError_t launch_frame(const GridView& g, const vt_camera& cam, const LightView& light,
                          uint4* out, cudaStream_t stream) {
     State& s = state();
+    if (s.tune_render.persistent && s.tune_render.wavefront)
+        return launch_render_queued(g, cam, light, out, next_counter(), s.tune_render, s.sm_count,
+                                    stream);
     if (s.tune_render.persistent)
         return launch_render_persistent(g, cam, light, out, next_counter(), s.tune_render,
                                         s.sm_count, stream);

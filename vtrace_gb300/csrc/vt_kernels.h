@@ -26,6 +26,10 @@ struct TraceTuning {
 cudaError_t launch_render_wavefront(const GridView& g, const vt_camera& cam,
                                     const LightView& light, uint4* out, cudaStream_t stream);
 
+// Persistent whole-tile render whose shadow rays are queued per warp and traced in full warps.
+cudaError_t launch_render_queued(const GridView& g, const vt_camera& cam, const LightView& light,
+                                 uint4* out, unsigned long long* counter, const TraceTuning& tune,
+                                 int sm_count, cudaStream_t stream);
 cudaError_t launch_render_persistent(const GridView& g, const vt_camera& cam,
                                      const LightView& light, uint4* out,
                                      unsigned long long* counter, const TraceTuning& tune,

@@ -446,3 +446,147 @@ cudaError_t launch_render_wavefront(const GridView& g, const vt_camera& cam,
 }
 
 }  // namespace vt
+
+// ---------------------------------------------------------------------------------------------
+// Queued-shadow render: resident warps take whole 8 x 4 pixel tiles from a work counter and trace
+// their camera rays to the end, one per lane, as the tile launch does; a pixel that needs a shadow
+// ray queues it (its primary record and the ray's origin) in its warp's queue in shared memory
+// instead of tracing it in the lane, and the warp traces queued shadow rays 32 at a time,
+// whenever 32 are waiting, so that shadow rays run in full warps.  No barrier and no per-lane
+// state machine: a warp only ever waits for its own lanes.  The remainder of each queue is traced
+// when the counter runs dry.  Same records as the fused render.
+// ---------------------------------------------------------------------------------------------
+namespace vt {
+
+constexpr int kQueueWarps = 4;     // 128-thread blocks
+constexpr uint32_t kQueueCap = 64;  // entries per warp: up to 31 left over + 32 from one tile
+
+struct QueuedShadow {
+    HitRec prim;  // the unshaded primary record
+    float so[3];  // shadow ray origin
+    uint32_t pix;
+};
+
+// One traversal call site serves both kinds of unit (a tile of camera rays, or up to 32 queued
+// shadow rays), so that the kernel holds the traversal's registers once.
+__global__ void __launch_bounds__(kQueueWarps * 32, 10) render_queue_kernel(
+    GridView g, vt_camera cam, LightView L, uint4* __restrict__ out,
+    unsigned long long* __restrict__ counter, uint32_t tiles_x, uint64_t tiles) {
+    __shared__ QueuedShadow queue[kQueueWarps][kQueueCap];
+    const uint32_t lane = threadIdx.x & 31u;
+    QueuedShadow* q = queue[threadIdx.x >> 5];
+    uint32_t qn = 0;     // warp-uniform: queued shadow rays
+    bool tiles_left = true;  // warp-uniform
+    for (;;) {
+        // warp-uniform choice of the unit: 32 queued shadow rays, else a tile, else the rest of
+        // the queue
+        bool shadow_unit = qn >= 32u;
+        uint64_t u = 0;
+        if (!shadow_unit && tiles_left) {
+            unsigned long long v = 0;
+            if (lane == 0) v = atomicAdd(counter, 1ull);
+            u = __shfl_sync(0xFFFFFFFFu, v, 0);
+            if (u >= tiles) tiles_left = false;
+        }
+        if (!shadow_unit && !tiles_left) {
+            if (qn == 0) break;
+            shadow_unit = true;
+        }
+        const uint32_t n = shadow_unit ? min(qn, 32u) : 32u;
+        uint32_t px = 0, py = 0;
+        bool active;
+        float o[3], d[3];
+        if (shadow_unit) {
+            active = lane < n;
+            if (active) {
+                o[0] = q[lane].so[0];
+                o[1] = q[lane].so[1];
+                o[2] = q[lane].so[2];
+            }
+            d[0] = L.dx;
+            d[1] = L.dy;
+            d[2] = L.dz;
+        } else {
+            px = (uint32_t)(u % tiles_x) * 8u + (lane & 7u);
+            py = (uint32_t)(u / tiles_x) * 4u + (lane >> 3);
+            active = px < cam.width && py < cam.height;
+            if (active) raygen(cam, px, py, 0.5f, 0.5f, o, d);
+        }
+        HitRec h;
+        if (active) {
+            Tally<false> tl;
+            h = trace_ray<false>(g, o, d, tl);
+        }
+        __syncwarp();
+        if (shadow_unit) {
+            if (active) {
+                const bool shadowed = ((h.w1 >> 24) & VT_HIT_FLAG_HIT) != 0u;
+                HitRec p = q[lane].prim;
+                float ndl = 0.0f;
+                face_lit(p, L, ndl);
+                p.w3 = shade_rgba(p.w3, ndl, shadowed ? 0.0f : 1.0f, L.ambient);
+                p.w1 |= (VT_HIT_FLAG_SHADOW_RAY | (shadowed ? VT_HIT_FLAG_SHADOWED : 0u)) << 24;
+                out[q[lane].pix] = make_uint4(p.w0, p.w1, p.w2, p.w3);
+            }
+            // move the rest (at most 31 entries) down to the front
+            QueuedShadow rest;
+            const bool mv = lane + n < qn;
+            if (mv) rest = q[lane + n];
+            __syncwarp();
+            if (mv) q[lane] = rest;
+            __syncwarp();
+            qn -= n;
+            continue;
+        }
+        bool need = false;
+        if (active) {
+            const uint32_t pix = py * cam.width + px;
+            float ndl;
+            if (!((h.w1 >> 24) & VT_HIT_FLAG_HIT)) {
+                h.w3 = VT_SKY_RGBA;
+            } else if (L.enabled && face_lit(h, L, ndl)) {
+                if (ndl > 0.0f && L.shadows) {
+                    need = true;
+                } else {
+                    h.w3 = shade_rgba(h.w3, ndl, 1.0f, L.ambient);
+                }
+            }
+            if (!need) out[pix] = make_uint4(h.w0, h.w1, h.w2, h.w3);
+        }
+        const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, need);
+        if (need) {
+            QueuedShadow& e = q[qn + __popc(ballot & ((1u << lane) - 1u))];
+            e.prim = h;
+            e.pix = py * cam.width + px;
+            shadow_origin(h, o, d, e.so);
+        }
+        __syncwarp();
+        qn += __popc(ballot);
+    }
+}
+
+cudaError_t launch_render_queued(const GridView& g, const vt_camera& cam, const LightView& light,
+                                 uint4* out, unsigned long long* counter, const TraceTuning& tune,
+                                 int sm_count, cudaStream_t stream) {
+    static int per_sm = [] {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)render_queue_kernel,
+                                                          kQueueWarps * 32, 0) != cudaSuccess) {
+            cudaGetLastError();
+            n = 1;
+        }
+        return n < 1 ? 1 : n;
+    }();
+    const uint32_t tiles_x = (cam.width + 7) / 8, tiles_y = (cam.height + 3) / 4;
+    const uint64_t tiles = (uint64_t)tiles_x * tiles_y;
+    const int bps = tune.blocks_per_sm > 0 ? min(tune.blocks_per_sm, per_sm) : per_sm;
+    const uint64_t need = (tiles + kQueueWarps - 1) / kQueueWarps;
+    const unsigned blocks = (unsigned)std::min<uint64_t>((uint64_t)sm_count * bps, need);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    render_queue_kernel<<<blocks, kQueueWarps * 32, 0, stream>>>(g, cam, light, out, counter,
+                                                                 tiles_x, tiles);
+    return cudaGetLastError();
+}
+
+}  // namespace vt
