@@ -124,8 +124,10 @@ def profiled_traffic(workload):
     if not m:
         return None
     when = re.search(r"^Captured: (.+)$", text, re.M)
+    inst = re.search(r"\| warp_instructions_per_launch \| (\d+) \|", text)
     return {"bytes": int(m.group(1)), "source": "profiles/render_%s.md" % workload,
-            "captured": when.group(1).strip() if when else None}
+            "captured": when.group(1).strip() if when else None,
+            "warp_instructions": int(inst.group(1)) if inst else None}
 
 
 def measured_peak():
@@ -482,6 +484,19 @@ def run_ours(args):
     metric = METRIC if args.config == "shapes1024" else "Mrays/s (%dx%d, %d^3 grid)" % (
         cam.width, cam.height, w["voxels"].shape[0])
     traffic = profiled_traffic("shapes1024_1080p") if args.config == "shapes1024" else None
+    issue = None
+    if traffic and traffic.get("warp_instructions") and clocks and clocks.get("sm_mhz"):
+        # the kernel's real bound: warp instructions issued per second (count from the committed
+        # ncu capture of the same launch, time from this run) against 4 issue slots per SM per
+        # clock at the SM clock sampled during the timed region
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        achieved_gips = traffic["warp_instructions"] / (ms * 1e-3) / 1e9
+        peak_gips = 4 * sms * clocks["sm_mhz"] * 1e6 / 1e9
+        issue = {"bound": "issue", "achieved": achieved_gips, "peak": peak_gips,
+                 "unit": "G warp instructions/s", "frac": achieved_gips / peak_gips,
+                 "warp_instructions_per_launch": traffic["warp_instructions"],
+                 "source": "instruction count of the default 8x4-tile launch from %s; 4 issue "
+                           "slots x %d SMs x the SM clock sampled here" % (traffic["source"], sms)}
     line = {
         "metric": metric, "value": value, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -509,7 +524,8 @@ def run_ours(args):
                 "achieved": unique_bytes / (ms * 1e-3) / 1e9,
                 "frac": unique_bytes / (ms * 1e-3) / 1e9 / measured_peak()[0],
                 "bricks": fp, "note": "distinct directory entries x 4 B + masks x 64 B + hit "
-                "bricks' payload x 512 B + 16 B records, along the reference's iteration path"}),
+                "bricks' payload x 512 B + 16 B records, along the reference's iteration path"},
+            issue=issue),
         "clocks": clocks,
         "grid_info": grid.info(),
     }
