@@ -132,6 +132,27 @@ def test_split_requests_match_unsplit_ones(torch):
         split.stop()
 
 
+def test_pageable_outputs_through_the_staging_area(torch):
+    """Outputs in ordinary (pageable) host memory: the resolve writes each piece's rows into the
+    slot's device staging area and they are copied out; same images as the oracle's, whether
+    the request is split into pieces or not."""
+    scenes, views = small_world(5)
+    svc = vt.Service(max_inflight=2, max_samples_per_piece=1500, max_samples_per_launch=6000)
+    try:
+        sids = [svc.add_scene(s["voxels"], s["palette"]) for s in scenes]
+        outs = [np.zeros(v["camera"].width * v["camera"].height * 4, np.uint8) for v in views]
+        rids = [svc.submit(sids[v["scene"]], v["camera"], o, v["spp"], v["seed"], v["view_id"],
+                           v["light"]) for v, o in zip(views, outs)]
+        for r in rids:
+            svc.wait(r)
+        for o, v in zip(outs, views):
+            img = o.reshape(v["camera"].height, v["camera"].width, 4)
+            np.testing.assert_array_equal(img, oracle_image(scenes[v["scene"]], v))
+        assert svc.stats()["views_launched"] > len(views)  # some requests ran as pieces
+    finally:
+        svc.stop()
+
+
 def test_stop_while_other_threads_submit_and_poll(torch):
     """vt_serve_stop while other threads are inside submit and poll calls on the same service:
     every call returns (a request id, VT_ECANCELED or VT_ENOTFOUND), nothing is left waiting."""
