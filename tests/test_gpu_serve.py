@@ -263,6 +263,48 @@ def test_failures_are_reported_per_request(torch):
     assert got.get("code") == -7  # VT_ECANCELED
 
 
+def test_oversized_piece_and_its_scene_must_fit_together(torch):
+    """A piece larger than a slot's buffer takes a temporary counted against the budget.  When
+    the scene fits alone and the temporary fits alone but not both, the request fails with
+    VT_ENOMEM (its scene is never evicted from under it); with room for both it renders."""
+    scenes, _ = small_world(2)
+    sc = scenes[0]
+    n = sc["n"]
+    bound = ((n + 7) // 8) ** 3 * (4 + 64 + 512) + 1024
+    g = vt.Grid.from_u8(sc["voxels"], sc["palette"])
+    actual = g.info()["device_bytes"]
+    g.destroy()
+    assert actual < bound
+    cap = 1024  # samples per slot: 20 KiB of slot buffers
+    # a request whose temporary (20 B per sample) lies between bound - actual and bound
+    width = 64
+    height = max(4, int((bound - (bound - actual) // 2) // 20 // width))
+    extra = width * height * 20
+    assert bound - actual < extra < bound
+    cam = vt.camera_look_at((-1.5 * n, 2.0 * n, -1.5 * n), (n / 2, n / 4, n / 2), (0, 1, 0), 60.0,
+                            width, height)
+    for budget, ok in ((cap * 20 + bound, False), (cap * 20 + actual + extra + 4096, True)):
+        svc = vt.Service(hbm_budget_bytes=budget, max_inflight=1, max_samples_per_launch=cap,
+                         max_samples_per_piece=0)
+        try:
+            sid = svc.add_scene(sc["voxels"], sc["palette"])
+            buf = pinned(torch, cam)
+            rid = svc.submit(sid, cam, buf, 1, 3, 9)
+            if ok:
+                svc.wait(rid)
+                img = buf.numpy().reshape(height, width, 4)
+                og = po.Grid(sc["voxels"], sc["palette"])
+                hits = po.render_view(og, po.make_camera(cam.as_dict()), None, 1, 3, 9)
+                want = hits["rgba"].view(np.uint8).reshape(height, width, 4)
+                np.testing.assert_array_equal(img, want)
+            else:
+                with pytest.raises(vt.VtError) as e:
+                    svc.wait(rid)
+                assert e.value.code == -2  # VT_ENOMEM
+        finally:
+            svc.stop()
+
+
 def test_protocol_errors(torch):
     """Requests are consumed by the poll that reports them; a poll with no wait on a running
     request says "not ready"; bad arguments and unknown ids fail without disturbing the service."""

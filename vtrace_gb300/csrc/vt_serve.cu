@@ -305,16 +305,23 @@ bool Service::pack(Slot& slot, std::unique_lock<std::mutex>& lk) {
             fail_request(q, rc);
             continue;
         }
+        scenes[q.r.scene]->refs++;  // held until the piece retires (and never evicted below)
         if (extra) {
             if (used() + extra > cfg.hbm_budget_bytes && !evict_for(extra)) {
-                pending.push_front(pc);  // the grid build took the room: try again later
+                scenes[q.r.scene]->refs--;
+                const bool idle = std::none_of(slots.begin(), slots.end(),
+                                               [](const Slot& s) { return s.busy; });
+                if (idle) {  // its scene and its temporary never fit together
+                    fail_request(q, VT_ENOMEM);
+                    continue;
+                }
+                pending.push_front(pc);  // in-flight work holds the room: try again later
                 q.pieces_pending++;
                 break;
             }
             slot.extra_bytes = extra;
             extra_bytes += extra;
         }
-        scenes[q.r.scene]->refs++;  // held until the piece retires
         q.pieces_inflight++;
         slot.pieces.push_back(pc);
         samples += pc.samples;
