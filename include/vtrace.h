@@ -172,7 +172,8 @@ typedef struct vt_tuning {
                            shadow rays per warp, tracing them 32 at a time.
                            VT_KERNEL_PATH: advance all paths one vertex at a time through ray
                            queues (the default; faster than either per-path form) */
-    uint32_t tile_shape;  /* VT_KERNEL_RENDER fused tile launch: the pixels of one warp, VT_TILE_* */
+    uint32_t tile_shape;  /* VT_KERNEL_RENDER fused tile launch and VT_KERNEL_BATCH work units
+                             (batches created afterwards): the pixels of one warp, VT_TILE_* */
     uint32_t block_warps; /* VT_KERNEL_RENDER fused tile launch: warps per block, 1, 2, 4 or 8
                              (0 = 4); the block's warp tiles are arranged about twice as wide as
                              high */

@@ -60,6 +60,41 @@ def test_render_tile_shapes_agree(torch, frame_case, tile, warps):
         vt.set_tuning(vt.KERNEL_RENDER, **saved)
 
 
+@pytest.mark.parametrize("tile", [vt.TILE_8X4, vt.TILE_4X8, vt.TILE_16X2, vt.TILE_32X1])
+def test_batch_tile_shapes_agree(torch, tile):
+    """Batch work units of every pixel-tile shape give the oracle's sample records (odd view
+    sizes: partial tiles on both edges)."""
+    scenes, views = workloads.multiview(n_scenes=2, n_views=4, sizes=(64, 48), min_px=37 * 23,
+                                        max_px=141 * 77, seed=9)
+    grids = [vt.Grid.from_u8(s["voxels"], s["palette"]) for s in scenes]
+    saved = vt.get_tuning(vt.KERNEL_BATCH)
+    try:
+        vt.set_tuning(vt.KERNEL_BATCH, 32, 0, True, False, tile, 4)
+        outs, specs = [], []
+        for v in views:
+            c = v["camera"]
+            buf = torch.zeros(c.width * c.height * v["spp"] * 16, dtype=torch.uint8, device="cuda")
+            outs.append(buf)
+            specs.append(vt.make_view(grids[v["scene"]], c, buf, v["spp"], v["seed"],
+                                      v["view_id"], v["light"]))
+        b = vt.Batch(specs)
+        b.run()
+        torch.cuda.synchronize()
+        ogrids = [po.Grid(s["voxels"], s["palette"]) for s in scenes]
+        for v, o in zip(views, outs):
+            L = v["light"]
+            want = po.render_view(ogrids[v["scene"]], po.make_camera(v["camera"].as_dict()),
+                                  po.make_light(list(L.dir), L.ambient, bool(L.shadows)),
+                                  v["spp"], v["seed"], v["view_id"])
+            assert_same(o.cpu().numpy().view(vt.HIT_DTYPE), want,
+                        "batch tile %s view %d" % (vt.TILE_NAMES[tile], v["view_id"]))
+        b.destroy()
+    finally:
+        vt.set_tuning(vt.KERNEL_BATCH, **saved)
+        for g in grids:
+            g.destroy()
+
+
 def test_set_tuning_rejects_bad_shapes(torch):
     with pytest.raises(vt.VtError):
         vt.set_tuning(vt.KERNEL_RENDER, 16, 0, False, False, 4, 4)

@@ -11,8 +11,8 @@ fastest and installs it with vt_set_tuning.  The search spaces:
                warps taking whole tiles and tracing their queued shadow rays 32 at a time
   trace_rays   one thread per ray, or persistent warps with a refill threshold of 1, 4, 8, 16, 24
                or 32 idle lanes and 2 or as many as fit resident blocks per SM
-  batch        whole 8x4 tile units per warp, or per-lane refill at 4, 8 or 16 idle lanes, with 2
-               or as many as fit resident blocks per SM
+  batch        whole tile units per warp over 8x4, 4x8, 16x2 and 32x1-pixel tiles, or per-lane
+               refill at 4, 8 or 16 idle lanes, with 2 or as many as fit resident blocks per SM
 
 The brick size is part of the grid layout (8^3, a 512-bit occupancy mask and a 512-byte payload
 per brick: the mask is one 64-bit word per z-slice), and a warp traces one ray per lane, so
@@ -52,8 +52,10 @@ def rays_candidates(refill=(1, 4, 8, 16, 24, 32), blocks=(0, 2)):
     return out
 
 
-def batch_candidates(refill=(4, 8, 16), blocks=(0, 2)):
-    out = [tuning(refill_min=32, blocks_per_sm=b, persistent=True) for b in blocks]
+def batch_candidates(refill=(4, 8, 16), blocks=(0, 2),
+                     tiles=(TILE_8X4, TILE_4X8, TILE_16X2, TILE_32X1)):
+    out = [tuning(refill_min=32, blocks_per_sm=b, persistent=True, tile_shape=t)
+           for t, b in itertools.product(tiles, blocks)]
     out += [tuning(refill_min=r, blocks_per_sm=b, persistent=True)
             for r, b in itertools.product(refill, blocks)]
     return out
@@ -67,7 +69,8 @@ def candidates(kernel):
 def key(kernel, c):
     """A short name of candidate `c` of `kernel`."""
     if kernel == KERNEL_BATCH:
-        form = "tiles" if c["refill_min"] >= 32 else "lanes_r%d" % c["refill_min"]
+        form = ("tiles_%s" % TILE_NAMES[c["tile_shape"]] if c["refill_min"] >= 32
+                else "lanes_r%d" % c["refill_min"])
         return "%s_b%d" % (form, c["blocks_per_sm"])
     if c["persistent"] and c["wavefront"] and kernel == KERNEL_RENDER:
         return "queued_shadows_b%d" % c["blocks_per_sm"]

@@ -3,7 +3,8 @@
 //
 // A batch flattens all its views into one item space: view v owns items [begin_v, begin_v +
 // tiles_v * spp_v * 32), item = ((tile * spp + sample) * 32 + lane-in-tile), so a warp refill
-// hands out neighbouring pixels of one tile and one sample.  Resident warps fetch items with one
+// hands out neighbouring pixels of one tile and one sample (tiles of 8 x 4 pixels, or the tile
+// shape the VT_KERNEL_BATCH tuning names).  Resident warps fetch items with one
 // atomic per refill — whole 32-item units in the default tile form, per idle lane in the lane
 // form (vt_lane.cuh) — find the item's view by binary search over the view table (held in shared
 // memory), and trace it with the view's grid, camera and light.  Samples are
@@ -117,8 +118,8 @@ __global__ void __launch_bounds__(256, 4) batch_kernel(const BatchView* __restri
                 const uint32_t l = (uint32_t)local & 31u;
                 const uint64_t tile = ts / V.spp;
                 const uint32_t sample = (uint32_t)(ts - tile * V.spp);
-                const uint32_t px = (uint32_t)(tile % V.tiles_x) * 8u + (l & 7u);
-                const uint32_t py = (uint32_t)(tile / V.tiles_x) * 4u + (l >> 3);
+                const uint32_t px = ((uint32_t)(tile % V.tiles_x) << V.wx_log) + (l & ((1u << V.wx_log) - 1u));
+                const uint32_t py = (uint32_t)(tile / V.tiles_x) * (32u >> V.wx_log) + (l >> V.wx_log);
                 if (px < V.cam.width && py < V.cam.height) {
                     s.view = lo;
                     s.px = px;
@@ -159,8 +160,9 @@ __global__ void __launch_bounds__(256, 4) batch_kernel(const BatchView* __restri
     }
 }
 
-// Tile form (refill_min 32, the default): resident warps take whole (8 x 4 tile, sample) units —
-// 32 items of one view — from the counter, one atomic per unit, and trace each lane's camera ray
+// Tile form (refill_min 32, the default): resident warps take whole (pixel tile, sample) units —
+// 32 items of one view; 8 x 4 pixels unless the VT_KERNEL_BATCH tuning names another tile shape
+// when the batch is created — from the counter, one atomic per unit, and trace each lane's camera ray
 // and shadow ray to the end in the lane (the render kernel's traversal), so that a warp's rays
 // start together and no lane state is kept between units.  Same item order and records as the
 // lane form with whole-warp refills, 23% faster on the 64-view workload.
@@ -203,8 +205,8 @@ __global__ void __launch_bounds__(kBatchTileThreads) batch_tile_kernel(const Bat
         const uint64_t ts = local >> 5;
         const uint64_t tile = ts / V.spp;
         const uint32_t sample = (uint32_t)(ts - tile * V.spp);
-        const uint32_t px = (uint32_t)(tile % V.tiles_x) * 8u + (lane & 7u);
-        const uint32_t py = (uint32_t)(tile / V.tiles_x) * 4u + (lane >> 3);
+        const uint32_t px = ((uint32_t)(tile % V.tiles_x) << V.wx_log) + (lane & ((1u << V.wx_log) - 1u));
+        const uint32_t py = (uint32_t)(tile / V.tiles_x) * (32u >> V.wx_log) + (lane >> V.wx_log);
         if (px < V.cam.width && py < V.cam.height) {
             float jx, jy, o[3], d[3];
             jitter(V.seed, V.view_id, px, py, sample, jx, jy);
@@ -252,18 +254,25 @@ static void batch_free(Batch& b) {
     b.grids.clear();
 }
 
-uint64_t batch_view_items(const vt_camera& cam, uint32_t spp) {
-    return batch_rows_items(cam, spp, 0, cam.height);
+uint32_t tile_wx_log(uint32_t tile_shape) {
+    static const uint32_t kLog[4] = {3, 2, 4, 5};  // VT_TILE_8X4, 4X8, 16X2, 32X1
+    return tile_shape < 4 ? kLog[tile_shape] : 3u;
 }
 
-uint64_t batch_rows_items(const vt_camera& cam, uint32_t spp, uint32_t row0, uint32_t row1) {
-    const uint64_t tile_rows = (uint64_t)((row1 + 3) / 4) - row0 / 4;
-    return tile_rows * ((cam.width + 7) / 8) * spp * 32;
+uint64_t batch_view_items(const vt_camera& cam, uint32_t spp, uint32_t wx_log) {
+    return batch_rows_items(cam, spp, 0, cam.height, wx_log);
+}
+
+uint64_t batch_rows_items(const vt_camera& cam, uint32_t spp, uint32_t row0, uint32_t row1,
+                          uint32_t wx_log) {
+    const uint32_t th = 32u >> wx_log, tw = 1u << wx_log;
+    const uint64_t tile_rows = (uint64_t)((row1 + th - 1) / th) - row0 / th;
+    return tile_rows * ((cam.width + tw - 1) / tw) * spp * 32;
 }
 
 BatchView make_batch_view(const Grid& g, const vt_camera& cam, const vt_light* light,
                           uint32_t spp, uint32_t seed, uint32_t view_id, void* out,
-                          uint64_t begin, uint32_t row0) {
+                          uint64_t begin, uint32_t row0, uint32_t wx_log) {
     BatchView T;
     memset(&T, 0, sizeof(T));
     T.g = g.view();
@@ -271,9 +280,10 @@ BatchView make_batch_view(const Grid& g, const vt_camera& cam, const vt_light* l
     T.light = light_view(light);
     T.out = (uint4*)out;
     T.begin = begin;
-    T.first_item = batch_rows_items(cam, spp, 0, row0);
+    T.first_item = batch_rows_items(cam, spp, 0, row0, wx_log);
     T.rec_offset = row0 * cam.width * spp;
-    T.tiles_x = (cam.width + 7) / 8;
+    T.wx_log = wx_log;
+    T.tiles_x = (cam.width + (1u << wx_log) - 1) >> wx_log;
     T.spp = spp;
     T.seed = seed;
     T.view_id = view_id;
@@ -347,6 +357,7 @@ int32_t vt_batch_create(const vt_view* views, uint32_t n, int32_t* batch_out) {
     std::unique_ptr<Batch> b(new Batch());
     std::vector<BatchView> table(n);
     uint64_t begin = 0;
+    const uint32_t wx_log = tile_wx_log(st.tune_batch.tile_shape);
     for (uint32_t i = 0; i < n; ++i) {
         const vt_view& v = views[i];
         Grid* g = lookup_grid(v.grid);
@@ -380,8 +391,8 @@ int32_t vt_batch_create(const vt_view* views, uint32_t n, int32_t* batch_out) {
         g->refs.fetch_add(1);
         b->grids.push_back(v.grid);
         table[i] = make_batch_view(*g, v.camera, (v.flags & VT_VIEW_LIGHT) ? &v.light : nullptr,
-                                   v.spp, v.seed, v.view_id, out, begin);
-        begin += batch_view_items(v.camera, v.spp);
+                                   v.spp, v.seed, v.view_id, out, begin, 0, wx_log);
+        begin += batch_view_items(v.camera, v.spp, wx_log);
         b->rays_primary += (uint64_t)v.camera.width * v.camera.height * v.spp;
     }
     b->nviews = n;
