@@ -393,8 +393,11 @@ int32_t vt_batch_destroy(int32_t batch);
  * brick grids stay resident in a cache built on first use, least-recently-used unreferenced scenes
  * evicted.  hbm_budget_bytes bounds the resident grids plus the launch slots' sample buffers
  * (max_inflight x max_samples_per_launch x 20 bytes, allocated at start) plus the temporary buffer
- * of any piece larger than a slot's.  max_inflight = 1, max_views_per_launch = 1 and
- * max_samples_per_piece = 0 is the plain per-request baseline. */
+ * of any piece larger than a slot's; a scene is admitted against the size its grid would have with
+ * every brick occupied, then counted at its real size.  While a scene's grid is built the device
+ * also holds its voxel array and the build's scratch for a moment; those are outside the budget.
+ * max_inflight = 1, max_views_per_launch = 1 and max_samples_per_piece = 0 is the plain
+ * per-request baseline. */
 typedef struct vt_serve_config {
     uint64_t hbm_budget_bytes;
     uint32_t max_inflight;           /* concurrent launches, 1..32 */

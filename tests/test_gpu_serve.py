@@ -34,6 +34,15 @@ def oracle_image(scene, v):
     return out.reshape(v["camera"].height, v["camera"].width, 4)
 
 
+def grid_bound(n):
+    """The service's bound of an n^3 u8 scene's device bytes: a grid allocation with every brick
+    occupied (directory, octant and long-box words, palette, masks, payloads), each part rounded
+    up to 256 bytes."""
+    b = ((n + 7) // 8) ** 3
+    al = lambda v: (v + 255) // 256 * 256
+    return al(4 * b) + al(4 * b) + al(12 * b) + 1024 + al(64 * b) + al(512 * b)
+
+
 def small_world(n_views=12):
     return workloads.multiview(n_scenes=3, n_views=n_views, sizes=(64, 96, 48), min_px=40 * 30,
                                max_px=160 * 120)
@@ -206,7 +215,7 @@ def test_cache_evicts_least_recently_used_under_its_budget(torch):
     scenes, views = small_world(8)
     # room for the largest scene's bound only (beside the one slot's sample buffer): alternating
     # scenes force evictions
-    bound = max(((s["n"] + 7) // 8) ** 3 * (4 + 64 + 512) + 1024 for s in scenes)
+    bound = max(grid_bound(s["n"]) for s in scenes)
     cap = 160 * 120 * 4
     svc = vt.Service(hbm_budget_bytes=bound + 1024 + cap * 20, max_inflight=1,
                      max_samples_per_launch=cap)
@@ -270,7 +279,7 @@ def test_oversized_piece_and_its_scene_must_fit_together(torch):
     scenes, _ = small_world(2)
     sc = scenes[0]
     n = sc["n"]
-    bound = ((n + 7) // 8) ** 3 * (4 + 64 + 512) + 1024
+    bound = grid_bound(n)
     g = vt.Grid.from_u8(sc["voxels"], sc["palette"])
     actual = g.info()["device_bytes"]
     g.destroy()

@@ -184,6 +184,10 @@ static BlockLayout block_layout(uint64_t bricks, uint64_t slots, uint32_t format
     return L;
 }
 
+uint64_t grid_bytes_bound(uint64_t bricks, uint32_t format) {
+    return block_layout(bricks, bricks, format).total;
+}
+
 static void point_into_block(Grid& g, void* block, const BlockLayout& L, uint64_t slots) {
     char* b = (char*)block;
     g.block = block;

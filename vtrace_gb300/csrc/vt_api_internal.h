@@ -92,6 +92,9 @@ cudaStream_t pick_stream(void* stream);
 Grid* lookup_grid(int32_t id);
 int32_t register_grid(std::unique_ptr<Grid> g);
 int32_t check_dims(uint32_t nx, uint32_t ny, uint32_t nz);
+// Device bytes of a grid of `bricks` bricks when every brick is occupied: the most its one
+// allocation can hold (directory, octant and long-box words, palette, masks, payloads).
+uint64_t grid_bytes_bound(uint64_t bricks, uint32_t format);
 int32_t check_camera(const vt_camera* cam);
 // Device address of page-locked, 16-byte aligned host memory (kernels write outputs there
 // directly), or nullptr for any other pointer.

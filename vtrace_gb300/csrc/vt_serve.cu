@@ -202,10 +202,10 @@ Service::~Service() {
         if (sc->grid >= 0) vt_grid_destroy(sc->grid);
 }
 
-// Upper bound of a scene's resident bytes: directory + masks + payloads of every brick.
+// Upper bound of a scene's resident bytes: its grid's allocation with every brick occupied.
 static uint64_t scene_bound(const ServeScene& s) {
     const uint64_t bricks = (uint64_t)((s.nx + 7) / 8) * ((s.ny + 7) / 8) * ((s.nz + 7) / 8);
-    return bricks * (4 + 64 + 512) + 1024;
+    return grid_bytes_bound(bricks, VT_PAYLOAD_U8);
 }
 
 // Evicts least-recently-used unreferenced scenes until `need` more bytes fit the budget; false
