@@ -283,7 +283,7 @@ def test_oversized_piece_and_its_scene_must_fit_together(torch):
     g = vt.Grid.from_u8(sc["voxels"], sc["palette"])
     actual = g.info()["device_bytes"]
     g.destroy()
-    assert actual < bound
+    assert actual <= bound  # equal for grids small enough to get a slot for every brick
     cap = 1024  # samples per slot: 20 KiB of slot buffers
     # a request whose temporary (20 B per sample) lies between bound - actual and bound
     width = 64
