@@ -304,7 +304,7 @@ def test_oversized_piece_and_its_scene_must_fit_together(torch):
                 img = buf.numpy().reshape(height, width, 4)
                 og = po.Grid(sc["voxels"], sc["palette"])
                 hits = po.render_view(og, po.make_camera(cam.as_dict()), None, 1, 3, 9)
-                want = hits["rgba"].view(np.uint8).reshape(height, width, 4)
+                want = np.ascontiguousarray(hits["rgba"]).view(np.uint8).reshape(height, width, 4)
                 np.testing.assert_array_equal(img, want)
             else:
                 with pytest.raises(vt.VtError) as e:
