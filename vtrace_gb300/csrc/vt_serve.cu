@@ -293,12 +293,11 @@ bool Service::pack(Slot& slot, std::unique_lock<std::mutex>& lk) {
                 fail_request(q, VT_ENOMEM);
                 continue;
             }
-            if (!evict_for(extra)) break;  // wait for in-flight work to free memory
         }
+        // (admit_scene may release the lock while it builds a grid; only this thread pops
+        // `pending`, so its front is still `pc` afterwards)
         const int32_t rc = admit_scene(lk, q.r.scene);
         if (rc == VT_EBUSY) break;  // wait for memory (the head of the line keeps its place)
-        if (pending.empty() || pending.front().req != pc.req || pending.front().row0 != pc.row0)
-            break;  // the service was stopped while the scene was built
         pending.pop_front();
         q.pieces_pending--;
         if (rc != VT_OK) {
