@@ -543,13 +543,18 @@ __global__ void __launch_bounds__(128) wave_primary_kernel(
     bool bounce = false;
     uint32_t p = 0, nrays = 0;
     float so[3] = {0.0f, 0.0f, 0.0f}, nd[3] = {0.0f, 0.0f, 0.0f};
+    float o[3], d[3];
+    HitRec h;
+    Tally<false> tl;
     if (valid) {
         p = (py * cam.width + px) * sn + smp;
-        float jx, jy, o[3], d[3];
+        float jx, jy;
         jitter(P.seed, 0u, px, py, s0 + smp, jx, jy);
         raygen(cam, px, py, jx, jy, o, d);
-        Tally<false> tl;
-        const HitRec h = trace_ray<false>(g, o, d, tl);
+        h = trace_ray<false>(g, o, d, tl);
+    }
+    __syncwarp();  // the warp's sun rays start together (fuller traversal passes)
+    if (valid) {
         nrays = 1;
         float T[3] = {1.0f, 1.0f, 1.0f}, L[3] = {0.0f, 0.0f, 0.0f};
         const uint32_t flags = h.w1 >> 24;
