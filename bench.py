@@ -535,9 +535,12 @@ def run_ours(args):
         frame = d_hits.cpu().numpy().view(vt.HIT_DTYPE).reshape(cam.height, cam.width)
         line["cpu_baseline"] = cpu_frame(w, frame)
         line["parity"] = frame_parity(w, grid, frame)
+    extras = rank == 0 and world == 1 and args.config == "shapes1024" and not args.no_extras
+    digest = grid_digest(grid) if extras else None
     grid.destroy()
     del d_hits
-    if rank == 0 and world == 1 and args.config == "shapes1024" and not args.no_extras:
+    if extras:
+        line["grid_build"] = bench_build(w, digest, stream, dev)
         line["terrain256"] = bench_frame(args, workloads.terrain256(), stream, flush, dev)
         line["cave512"] = bench_rays(args, stream, flush, dev, tuning)
         line["multiview"] = bench_multiview(args, stream, flush, dev, tuning)
@@ -551,6 +554,53 @@ def run_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def grid_digest(grid):
+    """SHA-256 of a grid's directory, masks and payloads (its brick layout)."""
+    import hashlib
+    h = hashlib.sha256()
+    d, m = grid.bricks()
+    for a in (d, m, grid.payload()):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def bench_build(w, digest, stream, dev, repeats=10, warmup=3):
+    """The brick build of the headline grid from voxels already in device memory
+    (vt_grid_create_u8_device, a synchronous call: words, scan, count readback, the grid's one
+    allocation, compaction, distance, octant and long-box passes), timed by the host clock per call
+    with the grid destroyed between calls; the layout must equal the host-input build's."""
+    import torch
+    import vtrace_gb300 as vt
+    vox = w["voxels"]
+    nz, ny, nx = vox.shape
+    d_vox = torch.from_numpy(np.ascontiguousarray(vox).reshape(-1)).to("cuda")
+    torch.cuda.synchronize()
+    for _ in range(warmup):
+        vt.Grid.from_u8_device(d_vox, (nx, ny, nz), w["palette"], stream).destroy()
+    sampler = ClockSampler(dev)
+    sampler.start()
+    times = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        g = vt.Grid.from_u8_device(d_vox, (nx, ny, nz), w["palette"], stream)
+        times.append((time.perf_counter() - t0) * 1e3)
+        g.destroy()
+    clocks = sampler.stop()
+    g = vt.Grid.from_u8_device(d_vox, (nx, ny, nz), w["palette"], stream)
+    same = grid_digest(g) == digest
+    info = g.info()
+    g.destroy()
+    del d_vox
+    ms = float(np.median(times))
+    return {"ms": ms, "ms_min": min(times), "repeats": repeats,
+            "input_gbs": vox.nbytes / (ms * 1e-3) / 1e9, "input_bytes": int(vox.nbytes),
+            "bricks_nonempty": info["bricks_nonempty"], "device_bytes": info["device_bytes"],
+            "layout_equal_to_host_input_build": same,
+            "path": "vt_grid_create_u8_device (C ABI), synchronous, host wall clock, grid destroyed "
+                    "between calls (its allocation included)",
+            "clocks": clocks}
 
 
 def bench_frame(args, w, stream, flush, dev):

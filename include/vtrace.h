@@ -201,8 +201,12 @@ int32_t vt_set_tuning(int32_t kernel, const vt_tuning* in);
  * `texture(...).w > 0.0` rule (shaders/trace.frag:78).  Returns a grid id >= 0 or an error. */
 int32_t vt_grid_create_u8(const uint8_t* voxels, const uint32_t* palette,
                           uint32_t nx, uint32_t ny, uint32_t nz);
-/* Same, with the voxel array already in device memory (x-fastest, nx*ny*nz bytes); the palette is
- * host memory.  The build runs on `stream`; the call returns after the build has finished. */
+/* Same, with the voxel array already in device memory (x-fastest, nx*ny*nz bytes, left unchanged);
+ * the palette is host memory.  The build runs on `stream`; the call returns after the build has
+ * finished.  Device memory during any build of more than 512 bricks: besides the grid, about 75
+ * bytes of scratch per brick and, when it fits, a staging buffer as large as the dense array
+ * padded to whole bricks, released (to the stream-ordered pool) when the call returns; without
+ * room for the staging buffer the build reads the dense array twice instead. */
 int32_t vt_grid_create_u8_device(const uint8_t* d_voxels, const uint32_t* palette,
                                  uint32_t nx, uint32_t ny, uint32_t nz, void* stream);
 /* Build a brick grid from an x-fastest RGBA8 texel array (host), the format of the reference's
@@ -272,6 +276,10 @@ int32_t vt_grid_download_octants(int32_t grid, uint32_t* octants);
  * L <= 15 such that the box L bricks long along axis a and K x K across (K = the octant word's
  * nibble o), from the brick toward octant o, holds no occupied brick. */
 int32_t vt_grid_download_long(int32_t grid, uint32_t* words);
+/* Copy the grid's brick payloads: vt_grid_info.slots blocks of 512 voxels by slot, each x fastest,
+ * then y, then z (one byte per voxel for VT_PAYLOAD_U8, four for VT_PAYLOAD_RGBA8), zero past the
+ * grid's edge.  VT_EINVAL if capacity_bytes is smaller than slots * 512 * that size. */
+int32_t vt_grid_download_payload(int32_t grid, void* payload, uint64_t capacity_bytes);
 
 /* ---------------------------------------------------------------- tracing */
 

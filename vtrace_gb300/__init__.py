@@ -197,6 +197,7 @@ SIGNATURES = [
     ("vt_grid_download_bricks", _i32, [_i32, _vp, _vp]),
     ("vt_grid_download_octants", _i32, [_i32, _vp]),
     ("vt_grid_download_long", _i32, [_i32, _vp]),
+    ("vt_grid_download_payload", _i32, [_i32, _vp, _u64]),
     ("vt_trace_rays", _i32, [_i32, _vp, _u64, _vp, _vp]),
     ("vt_trace_rays_host", _i32, [_i32, _vp, _u64, _vp]),
     ("vt_render", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp, _vp]),
@@ -501,6 +502,16 @@ class Grid:
         out = np.zeros(3 * self.info()["bricks_total"], np.uint32)
         check(lib().vt_grid_download_long(self.id, out.ctypes.data))
         return out.reshape(3, -1)
+
+    def payload(self):
+        """Brick payloads by slot: [slots, 8, 8, 8] u8 indices (z, y, x), or [slots, 8, 8, 8, 4]
+        RGBA8 texels."""
+        inf = self.info()
+        rgba = inf["payload_format"] == PAYLOAD_RGBA8
+        out = np.zeros(max(1, inf["slots"]) * 512 * (4 if rgba else 1), np.uint8)
+        check(lib().vt_grid_download_payload(self.id, out.ctypes.data, out.nbytes))
+        out = out[: inf["slots"] * 512 * (4 if rgba else 1)]
+        return out.reshape(-1, 8, 8, 8, 4) if rgba else out.reshape(-1, 8, 8, 8)
 
     def destroy(self):
         if self.id is not None and self.id >= 0:

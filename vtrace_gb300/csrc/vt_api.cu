@@ -431,14 +431,24 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
     }
     // the words kernel reads the palette from device memory (scratch tail) before the grid's
     // allocation exists: its size needs the count of occupied bricks
+    // The scratch is followed by the palette and, when it fits, the staging buffer that lets the
+    // compaction copy whole brick blocks instead of re-reading the dense grid (as large again as
+    // the padded grid, for the duration of the build; without it the build is the same, slower).
     void* scratch = nullptr;
     const size_t sbytes = build_scratch_bytes(g->bricks);
-    cudaError_t e = cudaMallocAsync(&scratch, sbytes + 1024, stream);
+    const size_t staged_at = sbytes + 1024;  // 256-aligned: sbytes is
+    cudaError_t e = cudaMallocAsync(&scratch, staged_at + build_staging_bytes(g->bricks, format), stream);
+    bool staging = e == cudaSuccess;
+    if (!staging) {
+        cudaGetLastError();
+        e = cudaMallocAsync(&scratch, staged_at, stream);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
         return fail(VT_ENOMEM, "cudaMallocAsync(brick build scratch) failed");
     }
     BuildScratch s = carve_build_scratch(scratch, g->bricks);
+    if (staging) s.staged = (char*)scratch + staged_at;
     uint32_t* d_palette = (uint32_t*)((char*)scratch + sbytes);
     uint32_t counts[2] = {0, 0};
     unsigned long long occ = 0;
@@ -648,7 +658,7 @@ void vt_shutdown(void) {
 
 const char* vt_last_error(void) { return g_last_error.c_str(); }
 
-uint32_t vt_version(void) { return (1u << 16) | 1u; }
+uint32_t vt_version(void) { return (1u << 16) | 2u; }
 
 void* vt_get_stream(void) {
     if (ensure_init()) return nullptr;
@@ -824,6 +834,20 @@ int32_t vt_grid_download_bricks(int32_t grid, uint32_t* directory, uint64_t* mas
         e = cudaMemcpyAsync(masks, g->masks, g->slots_used * 64, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_grid_download_bricks");
+    return VT_OK;
+}
+
+int32_t vt_grid_download_payload(int32_t grid, void* payload, uint64_t capacity_bytes) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_grid_download_payload: unknown grid");
+    const uint64_t bytes = g->slots_used * 512 * (g->format == VT_PAYLOAD_RGBA8 ? 4 : 1);
+    if (!payload || capacity_bytes < bytes)
+        return fail(VT_EINVAL, "vt_grid_download_payload: null output or capacity below slots * 512 voxels");
+    if (!bytes) return VT_OK;
+    cudaStream_t st = state().stream;
+    cudaError_t e = cudaMemcpyAsync(payload, g->payload, bytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_grid_download_payload");
     return VT_OK;
 }
 

@@ -58,8 +58,12 @@ struct BuildScratch {
     unsigned long long* occupied = nullptr;
     uint8_t* dist_a = nullptr;      // bricks: distance transform, first pass
     uint8_t* dist_b = nullptr;      // bricks: distance transform, second pass
+    // nullptr, or build_staging_bytes(): the voxels of each occupied brick as a 512-voxel block
+    // at brick * 512, written by the words pass and copied by the compaction
+    void* staged = nullptr;
 };
 size_t build_scratch_bytes(uint64_t bricks);
+size_t build_staging_bytes(uint64_t bricks, uint32_t format);
 // Carves BuildScratch out of one buffer of build_scratch_bytes(bricks) bytes.
 BuildScratch carve_build_scratch(void* base, uint64_t bricks);
 
