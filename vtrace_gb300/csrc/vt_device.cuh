@@ -220,6 +220,21 @@ __device__ __forceinline__ void dda_literal(const GridView& g, int32_t vx, int32
         ++steps;                                                             \
     }
 
+// VT_DDA_STEP on brick-local voxel coordinates (lx, ly, lz).
+#define VT_DDA_STEP_LOCAL                                                    \
+    {                                                                        \
+        const float mn = fminf(fminf(sx, sy), sz);                          \
+        mx = sx == mn;                                                       \
+        my = sy == mn;                                                       \
+        mz = sz == mn;                                                       \
+        if (mx) sx = __fadd_rn(sx, dlx);                                     \
+        if (my) sy = __fadd_rn(sy, dly);                                     \
+        if (mz) sz = __fadd_rn(sz, dlz);                                     \
+        if (mx) lx += stx;                                                   \
+        if (my) ly += sty;                                                   \
+        if (mz) lz += stz;                                                   \
+    }
+
 // The reference DDA (trace.frag:68-87) from grid-space point (px,py,pz) along (dx,dy,dz).
 //
 // Same voxel sequence, step count and hit as the literal loop; the work is organised by brick:
@@ -514,21 +529,25 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
         if (!brick_empty(e)) {
             slot = e;
             const uint64_t* mk = g.masks + (size_t)slot * 8;
-            const int32_t ex = stx > 0 ? min((bxi << 3) + 8, g.nx) : (stx < 0 ? (bxi << 3) - 1 : INT_MIN);
-            const int32_t ey = sty > 0 ? min((byi << 3) + 8, g.ny) : (sty < 0 ? (byi << 3) - 1 : INT_MIN);
-            const int32_t ez = stz > 0 ? min((bzi << 3) + 8, g.nz) : (stz < 0 ? (bzi << 3) - 1 : INT_MIN);
-            // Ends: with no side distance NaN, every iteration steps an axis whose step is not 0
-            // (an axis with step 0 has side +inf, the minimum only when all three are), so the
-            // brick is left within 22 iterations.
+            // Brick-local coordinates; the walk ends when one leaves 0..7.  Where a grid face cuts
+            // the brick, the voxels past the face have no occupancy bits, so walking on to the
+            // brick's face only defers the loop's grid-exit test: the ray misses either way, and a
+            // miss keeps none of the walk's state.  Ends: with no side distance NaN, every
+            // iteration steps an axis whose step is not 0 (an axis with step 0 has side +inf, the
+            // minimum only when all three are), so the brick is left within 22 iterations.
+            int32_t lx = vx & 7, ly = vy & 7, lz = vz & 7;
             for (;;) {
-                const uint64_t w = __ldg(mk + (vz & 7));
-                if ((w >> (((vy & 7) << 3) | (vx & 7))) & 1ull) {
+                const uint64_t w = __ldg(mk + lz);
+                if ((w >> ((ly << 3) | lx)) & 1ull) {
                     hit = true;
                     break;
                 }
-                VT_DDA_STEP
-                if (vx == ex || vy == ey || vz == ez) break;
+                VT_DDA_STEP_LOCAL
+                if ((lx | ly | lz) & ~7) break;
             }
+            vx = (bxi << 3) + lx;
+            vy = (byi << 3) + ly;
+            vz = (bzi << 3) + lz;
             if (hit) break;
         } else {
             int32_t nxe, nye, nze;

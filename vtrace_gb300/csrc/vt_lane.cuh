@@ -91,21 +91,21 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
     const uint32_t lw = lp ? __ldg(lp + bidx) : 0u;
     if (!brick_empty(e)) {
         const uint64_t* mk = g.masks + (size_t)e * 8;
-        const int32_t ex = stx > 0 ? min((bxi << 3) + 8, g.nx) : (stx < 0 ? (bxi << 3) - 1 : INT_MIN);
-        const int32_t ey = sty > 0 ? min((byi << 3) + 8, g.ny) : (sty < 0 ? (byi << 3) - 1 : INT_MIN);
-        const int32_t ez = stz > 0 ? min((bzi << 3) + 8, g.nz) : (stz < 0 ? (bzi << 3) - 1 : INT_MIN);
-        // a brick is left within 22 iterations (dda_skip's walk, same argument)
-        uint32_t steps = 0;  // counted by VT_DDA_STEP, not used here
+        // brick-local walk to the brick's face, as in dda_skip (left within 22 iterations)
+        int32_t lx = vx & 7, ly = vy & 7, lz = vz & 7;
         for (;;) {
-            const uint64_t w = __ldg(mk + (vz & 7));
-            if ((w >> (((vy & 7) << 3) | (vx & 7))) & 1ull) {
+            const uint64_t w = __ldg(mk + lz);
+            if ((w >> ((ly << 3) | lx)) & 1ull) {
                 status = kRayHit;
                 R.slot = e;
                 break;
             }
-            VT_DDA_STEP
-            if (vx == ex || vy == ey || vz == ez) break;
+            VT_DDA_STEP_LOCAL
+            if ((lx | ly | lz) & ~7) break;
         }
+        vx = (bxi << 3) + lx;
+        vy = (byi << 3) + ly;
+        vz = (bzi << 3) + lz;
     } else {
         int32_t nxe, nye, nze;
         empty_moves(g, e, ow, lw, bxi, byi, bzi, vx, vy, vz, stx, sty, stz, R.oshift, R.dom, nxe,
