@@ -425,6 +425,17 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
     }
 }
 
+// Moves along one axis from voxel v (in brick bi) to the far face of a box reaching r bricks
+// forward (this brick included) in step direction st, clipped to the grid's n voxels: the face is
+// the first voxel past the box for st = +1 (at most n) and the first voxel before it for st = -1
+// (at least -1).  0 for st = 0 (unused).
+__device__ __forceinline__ int32_t axis_moves(int32_t bi, int32_t r, int32_t v, int32_t st,
+                                              int32_t n) {
+    const int32_t neg = st < 0 ? 1 : 0;
+    const int32_t f = min(max(((bi + st * r + neg) << 3) - neg, -1), n);
+    return (f - v) * st;
+}
+
 // Voxel moves to the far face, along each stepping axis, of the empty box the ray crosses next
 // from the empty brick (bxi, byi, bzi).  Three boxes are known empty: the cube of bricks within
 // Chebyshev distance D - 1 (D from the directory entry `e`), which reaches D bricks forward along
@@ -432,7 +443,7 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
 // the octant word `ow`); and, when K >= D, the box that is K bricks across and L >= K bricks
 // long along the ray's dominant axis `dom` (L from the long-box word `lw`).  The ray only moves
 // forward, so the crossing uses the forward reach of the chosen box per axis, clipped to the
-// grid.  Axes with no step get 1 (unused by cross_region).
+// grid.  Axes with no step get 0 (unused by cross_region).
 __device__ __forceinline__ void empty_moves(const GridView& g, uint32_t e, uint32_t ow,
                                             uint32_t lw, int32_t bxi, int32_t byi, int32_t bzi,
                                             int32_t vx, int32_t vy, int32_t vz, int32_t stx,
@@ -448,9 +459,9 @@ __device__ __forceinline__ void empty_moves(const GridView& g, uint32_t e, uint3
         ry = dom == 1 ? L : K;
         rz = dom == 2 ? L : K;
     }
-    nxe = stx > 0 ? min((bxi + rx) << 3, g.nx) - vx : (stx < 0 ? vx - max((bxi - rx + 1) << 3, 0) + 1 : 1);
-    nye = sty > 0 ? min((byi + ry) << 3, g.ny) - vy : (sty < 0 ? vy - max((byi - ry + 1) << 3, 0) + 1 : 1);
-    nze = stz > 0 ? min((bzi + rz) << 3, g.nz) - vz : (stz < 0 ? vz - max((bzi - rz + 1) << 3, 0) + 1 : 1);
+    nxe = axis_moves(bxi, rx, vx, stx, g.nx);
+    nye = axis_moves(byi, ry, vy, sty, g.ny);
+    nze = axis_moves(bzi, rz, vz, stz, g.nz);
 }
 
 // Dominant axis of a direction (largest |component|; ties to the lower axis).
