@@ -389,15 +389,17 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
     const float ax = stx ? __fadd_rn(sx, __fmul_rn(__int2float_rn(nxe - 1), dlx)) : INFINITY;
     const float ay = sty ? __fadd_rn(sy, __fmul_rn(__int2float_rn(nye - 1), dly)) : INFINITY;
     const float az = stz ? __fadd_rn(sz, __fmul_rn(__int2float_rn(nze - 1), dlz)) : INFINITY;
-    const float ex = __fmul_rn(__fmul_rn(__int2float_rn(nxe + 2), ax), 0x1p-22f);
-    const float ey = __fmul_rn(__fmul_rn(__int2float_rn(nye + 2), ay), 0x1p-22f);
-    const float ez = __fmul_rn(__fmul_rn(__int2float_rn(nze + 2), az), 0x1p-22f);
-    // candidate leaving axis and its error bound
+    // Candidates: an axis within 2 * amin of the smallest approximation carries at most
+    // (Nmax + 2) * 2 * amin * 2^-24 of error, so (Nmax + 2) * amin * 2^-20 bounds the errors of
+    // both sides of its comparison with the smallest (with the 4x margin above); axes beyond it
+    // cannot leave first.
     const float amin = fminf(fminf(ax, ay), az);
-    const float emin = amin == ax ? ex : (amin == ay ? ey : ez);
-    const bool cx = stx && ax <= __fadd_rn(amin, __fadd_rn(emin, ex));
-    const bool cy = sty && ay <= __fadd_rn(amin, __fadd_rn(emin, ey));
-    const bool cz = stz && az <= __fadd_rn(amin, __fadd_rn(emin, ez));
+    const int32_t nmax = max(max(nxe, nye), nze);
+    const float lim =
+        __fadd_rn(amin, __fmul_rn(__fmul_rn(__int2float_rn(nmax + 2), amin), 0x1p-20f));
+    const bool cx = stx && ax <= lim;
+    const bool cy = sty && ay <= lim;
+    const bool cz = stz && az <= lim;
     const float tx = cx ? add_chain(sx, dlx, nxe - 1) : INFINITY;
     const float ty = cy ? add_chain(sy, dly, nye - 1) : INFINITY;
     const float tz = cz ? add_chain(sz, dlz, nze - 1) : INFINITY;
@@ -519,8 +521,6 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
         // fewer than 2^31 bricks (vt_grid_create checks): the index fits 32 bits
         const uint32_t bidx = (uint32_t)bxi + (uint32_t)g.bx * ((uint32_t)byi + (uint32_t)g.by * (uint32_t)bzi);
         const uint32_t e = __ldg(g.dir + bidx);
-        const uint32_t ow = octant_word(g, bidx);
-        const uint32_t lw = lp ? __ldg(lp + bidx) : 0u;
         {
             // One kind of unit per pass among the lanes running this loop together: the kind
             // more of them need (walk or crossing) runs while the others wait, and a kind passed
@@ -561,6 +561,8 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
             vz = (bzi << 3) + lz;
             if (hit) break;
         } else {
+            const uint32_t ow = octant_word(g, bidx);
+            const uint32_t lw = lp ? __ldg(lp + bidx) : 0u;
             int32_t nxe, nye, nze;
             empty_moves(g, e, ow, lw, bxi, byi, bzi, vx, vy, vz, stx, sty, stz, oshift, dom, nxe,
                         nye, nze);
