@@ -74,9 +74,16 @@ __device__ __forceinline__ int ray_begin(const GridView& g, const float o[3], co
     return grid_inside(g, R.vx, R.vy, R.vz) ? kRayRunning : kRayMiss;
 }
 
+// Directory entry of the lane's current brick.
+__device__ __forceinline__ uint32_t ray_entry(const GridView& g, const LaneRay& R) {
+    const uint32_t bidx = (uint32_t)(R.vx >> 3) + (uint32_t)g.bx * ((uint32_t)(R.vy >> 3) + (uint32_t)g.by * (uint32_t)(R.vz >> 3));
+    return __ldg(g.dir + bidx);
+}
+
 // One unit of traversal: the rest of the current occupied brick voxel by voxel, or the crossing
-// of the empty region around the current brick.  Same arithmetic as dda_skip().
-__device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
+// of the empty region around the current brick (`e`: its directory entry, ray_entry()).  Same
+// arithmetic as dda_skip().
+__device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R, uint32_t e) {
     int32_t vx = R.vx, vy = R.vy, vz = R.vz;
     const int32_t stx = R.stx, sty = R.sty, stz = R.stz;
     float sx = R.sx, sy = R.sy, sz = R.sz;
@@ -84,11 +91,6 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
     bool mx = R.mx, my = R.my, mz = R.mz;
     int status = kRayRunning;
     const int32_t bxi = vx >> 3, byi = vy >> 3, bzi = vz >> 3;
-    const uint32_t bidx = (uint32_t)bxi + (uint32_t)g.bx * ((uint32_t)byi + (uint32_t)g.by * (uint32_t)bzi);
-    const uint32_t e = __ldg(g.dir + bidx);
-    const uint32_t ow = octant_word(g, bidx);
-    const uint32_t* lp = long_words(g, R.dom);
-    const uint32_t lw = lp ? __ldg(lp + bidx) : 0u;
     if (!brick_empty(e)) {
         const uint64_t* mk = g.masks + (size_t)e * 8;
         // brick-local walk to the brick's face, as in dda_skip (left within 22 iterations)
@@ -107,6 +109,10 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
         vy = (byi << 3) + ly;
         vz = (bzi << 3) + lz;
     } else {
+        const uint32_t bidx = (uint32_t)bxi + (uint32_t)g.bx * ((uint32_t)byi + (uint32_t)g.by * (uint32_t)bzi);
+        const uint32_t ow = octant_word(g, bidx);
+        const uint32_t* lp = long_words(g, R.dom);
+        const uint32_t lw = lp ? __ldg(lp + bidx) : 0u;
         int32_t nxe, nye, nze;
         empty_moves(g, e, ow, lw, bxi, byi, bzi, vx, vy, vz, stx, sty, stz, R.oshift, R.dom, nxe,
                     nye, nze);
@@ -126,10 +132,8 @@ __device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
     return status;
 }
 
-// Whether the lane's next unit is an occupied-brick walk (else an empty-region crossing).
-__device__ __forceinline__ bool ray_next_walk(const GridView& g, const LaneRay& R) {
-    const uint32_t bidx = (uint32_t)(R.vx >> 3) + (uint32_t)g.bx * ((uint32_t)(R.vy >> 3) + (uint32_t)g.by * (uint32_t)(R.vz >> 3));
-    return !brick_empty(__ldg(g.dir + bidx));
+__device__ __forceinline__ int ray_unit(const GridView& g, LaneRay& R) {
+    return ray_unit(g, R, ray_entry(g, R));
 }
 
 // Record of a finished ray (unshaded colour; misses carry `miss_rgba`).

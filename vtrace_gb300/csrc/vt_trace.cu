@@ -308,7 +308,8 @@ __global__ void __launch_bounds__(256) trace_rays_persistent_kernel(
         // crossing) run it, the others wait, unless their kind has already waited kUnitWait
         // passes.  A warp then issues one kind's instructions per pass instead of both; every
         // pass with busy lanes runs at least one unit.  2% faster on the 16M incoherent rays.
-        const bool walk = busy && ray_next_walk(g, R);
+        const uint32_t e = busy ? ray_entry(g, R) : kEmptyBit;
+        const bool walk = busy && !brick_empty(e);
         const uint32_t wb = __ballot_sync(0xFFFFFFFFu, walk);
         const uint32_t cb = __ballot_sync(0xFFFFFFFFu, busy && !walk);
         bool run_walk = __popc(wb) >= __popc(cb);
@@ -321,7 +322,7 @@ __global__ void __launch_bounds__(256) trace_rays_persistent_kernel(
             wait_w = wb ? wait_w + 1 : 0;
         }
         if (busy && walk == run_walk) {
-            const int st = ray_unit(g, R);
+            const int st = ray_unit(g, R, e);
             if (st != kRayRunning) {
                 const HitRec h = ray_record(g, R, st, 0u);
                 out[idx] = make_uint4(h.w0, h.w1, h.w2, h.w3);
