@@ -271,7 +271,7 @@ constexpr int kUnitWait = 4;
 
 // n_dev: nullptr, or the device-side ray count (at most n), read at the start (ray queues whose
 // length the host does not know).
-__global__ void __launch_bounds__(256) trace_rays_persistent_kernel(
+__global__ void __launch_bounds__(256, 5) trace_rays_persistent_kernel(
     GridView g, const float2* __restrict__ rays, uint64_t n, uint4* __restrict__ out,
     unsigned long long* __restrict__ counter, uint32_t refill_min,
     const unsigned int* __restrict__ n_dev) {
