@@ -343,12 +343,12 @@ __device__ __forceinline__ float add_chain(float s, float d, int32_t k) {
 // floor((t_star - s) / delta) and settles it with exact additions and comparisons.
 __device__ __forceinline__ void advance_axis(float& s, int32_t& v, float delta, int32_t st,
                                              int32_t n_exit, float t_star, bool& stepped_last) {
-    if (st == 0 || s > t_star) {
+    if (s > t_star) {  // also every axis with no step: its side distance is +inf
         stepped_last = false;
         return;
     }
-    int32_t k = (int32_t)__fdividef(__fsub_rn(t_star, s), delta);
-    k = max(min(k, n_exit - 2), 0);  // add_chain takes k >= 0
+    // t_star - s >= 0, and S(n_exit - 1) > t_star >= S(0) gives n_exit >= 2: k >= 0 for add_chain
+    int32_t k = min((int32_t)__fdividef(__fsub_rn(t_star, s), delta), n_exit - 2);
     float x = add_chain(s, delta, k);  // S(k)
     if (x > t_star) {                  // the estimate overshot: walk up from S(0)
         k = 0;
@@ -377,8 +377,8 @@ __device__ __forceinline__ void advance_axis(float& s, int32_t& v, float delta, 
 // last processed value equals T*.
 //
 // Only the axes that can leave first need their exit value S_a(N_a - 1) exactly: the
-// approximation s + (N-1) * delta is within (N + 2) * 2^-24 of the exact chain relative to its
-// magnitude, so any axis whose approximation exceeds the smallest by more than the sum of both
+// approximation s + (N-1) * delta (one fused multiply-add) is within (N + 2) * 2^-24 of the exact
+// chain relative to its magnitude, so any axis whose approximation exceeds the smallest by more than the sum of both
 // bounds (taken 4x larger here) cannot be the minimum.  Every value compared is computed with
 // real binary32 additions, so the result is bit-identical to iterating the reference loop.
 __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, int32_t& vx,
@@ -386,17 +386,16 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
                                              float dlz, int32_t stx, int32_t sty, int32_t stz,
                                              int32_t nxe, int32_t nye, int32_t nze, bool& mx,
                                              bool& my, bool& mz) {
-    const float ax = stx ? __fadd_rn(sx, __fmul_rn(__int2float_rn(nxe - 1), dlx)) : INFINITY;
-    const float ay = sty ? __fadd_rn(sy, __fmul_rn(__int2float_rn(nye - 1), dly)) : INFINITY;
-    const float az = stz ? __fadd_rn(sz, __fmul_rn(__int2float_rn(nze - 1), dlz)) : INFINITY;
+    const float ax = stx ? __fmaf_rn(__int2float_rn(nxe - 1), dlx, sx) : INFINITY;
+    const float ay = sty ? __fmaf_rn(__int2float_rn(nye - 1), dly, sy) : INFINITY;
+    const float az = stz ? __fmaf_rn(__int2float_rn(nze - 1), dlz, sz) : INFINITY;
     // Candidates: an axis within 2 * amin of the smallest approximation carries at most
     // (Nmax + 2) * 2 * amin * 2^-24 of error, so (Nmax + 2) * amin * 2^-20 bounds the errors of
     // both sides of its comparison with the smallest (with the 4x margin above); axes beyond it
     // cannot leave first.
     const float amin = fminf(fminf(ax, ay), az);
     const int32_t nmax = max(max(nxe, nye), nze);
-    const float lim =
-        __fadd_rn(amin, __fmul_rn(__fmul_rn(__int2float_rn(nmax + 2), amin), 0x1p-20f));
+    const float lim = __fmaf_rn(__int2float_rn(nmax + 2) * 0x1p-20f, amin, amin);
     const bool cx = stx && ax <= lim;
     const bool cy = sty && ay <= lim;
     const bool cz = stz && az <= lim;
