@@ -115,11 +115,12 @@ def test_reference_call_sequence(lib):
     assert L.add_texture(t0.ctypes.data, 16, 16, 16) == -1
 
 
-@pytest.mark.parametrize("load_dist,size", [(3, (320, 240)), (5, (256, 320))])
+@pytest.mark.parametrize("load_dist,size", [(3, (320, 240)), (5, (256, 320)), (4, (203, 117))])
 def test_pager_world_with_instance_culling(lib, monkeypatch, load_dist, size):
     """vtrace's own world shape (src/world.rs:136-190): hundreds of 16^3 terrain chunks around
     the camera, some straddling it, and 121 entities, drawn through the per-tile instance bins;
-    the frame equals the oracle's loop over every instance."""
+    the frame equals the oracle's loop over every instance (203 x 117: warps that straddle the
+    frame's right and bottom edges)."""
     from vtrace_gb300 import workloads
     w, h = size
     world = workloads.pager_world(load_dist=load_dist, width=w, height=h)

@@ -101,19 +101,33 @@ __global__ void __launch_bounds__(256) compat_bin_kernel(const CompatInstance* _
     }
 }
 
-// The instances of tile `tile` in draw order: all of them when there are no bins.
+// The instances of tile `tile` in draw order (all of them when there are no bins), the same
+// sequence for every lane of a warp, whose lanes all lie in one tile and all call next() together:
+// the lanes load the tile's mask words 32 at a time (one word each, one ballot of the non-empty
+// ones), and each non-empty word is broadcast to the warp when its turn comes, so a tile's words
+// cost one load round per 32 instead of one dependent load each.
 struct InstanceCursor {
     const uint32_t* bins;
-    int32_t ninst, words, w, i;
-    uint32_t bits;
+    int32_t ninst, words, base, i, w;
+    uint32_t lane, mine, pending, bits;
     __device__ InstanceCursor(const uint32_t* b, int32_t n, int32_t nw, int32_t tile)
-        : bins(b ? b + (size_t)tile * nw : nullptr), ninst(n), words(nw), w(-1), i(-1), bits(0) {}
+        : bins(b ? b + (size_t)tile * nw : nullptr), ninst(n), words(nw), base(-32), i(-1), w(0),
+          lane(threadIdx.x & 31u), mine(0), pending(0), bits(0) {}
     // next instance index, or -1
     __device__ __forceinline__ int32_t next() {
         if (!bins) return ++i < ninst ? i : -1;
         while (bits == 0) {
-            if (++w >= words) return -1;
-            bits = __ldg(bins + w);
+            if (pending == 0) {
+                base += 32;
+                if (base >= words) return -1;
+                mine = base + (int32_t)lane < words ? __ldg(bins + base + lane) : 0u;
+                pending = __ballot_sync(0xFFFFFFFFu, mine != 0u);
+                continue;
+            }
+            const int32_t j = __ffs(pending) - 1;
+            pending &= pending - 1u;
+            bits = __shfl_sync(0xFFFFFFFFu, mine, j);
+            w = base + j;
         }
         const int32_t b = __ffs(bits) - 1;
         bits &= bits - 1u;
@@ -131,7 +145,10 @@ __global__ void __launch_bounds__(128, 8) compat_kernel(const GridView* __restri
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const int32_t px = (int32_t)(blockIdx.x * 16 + (warp & 1u) * 8u + (lane & 7u));
     const int32_t py = (int32_t)(blockIdx.y * 8 + (warp >> 1) * 4u + (lane >> 3));
-    if (px >= f.width || py >= f.height) return;
+    // a warp's 8 x 4 pixels lie in one binning tile; lanes outside the frame stay to the end,
+    // since the cursor's loads are shared by the warp
+    const bool inside = px < f.width && py < f.height;
+    if (__ballot_sync(0xFFFFFFFFu, inside) == 0u) return;
     const float inv_w = __fdiv_rn(2.0f, __int2float_rn(f.width));
     const float xn = __fsub_rn(__fmul_rn(__fadd_rn(__int2float_rn(px), 0.5f), inv_w), 1.0f);
     const float yn = __fsub_rn(__fmul_rn(__fadd_rn(__int2float_rn(py), 0.5f), inv_w), 1.0f);
@@ -150,6 +167,7 @@ __global__ void __launch_bounds__(128, 8) compat_kernel(const GridView* __restri
     float depth = INFINITY;
     InstanceCursor cur(bins, ninst, words, (int32_t)((blockIdx.y >> 1) * gridDim.x + blockIdx.x));
     for (int32_t i = cur.next(); i >= 0; i = cur.next()) {
+        if (!inside) continue;
         const CompatInstance& I = inst[i];
         if (I.texture < 0) continue;  // draws nothing (only reached without bins)
         const GridView g = views[I.texture];
@@ -210,6 +228,7 @@ __global__ void __launch_bounds__(128, 8) compat_kernel(const GridView* __restri
         ca = tex >> 24;  // alpha: ONE * src + ZERO * dst
         depth = tn;
     }
+    if (!inside) return;
     fb[(size_t)py * f.width + px] = make_uchar4((unsigned char)cr, (unsigned char)cg,
                                                 (unsigned char)cb, (unsigned char)ca);
 }
