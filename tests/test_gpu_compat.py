@@ -150,3 +150,59 @@ def test_pager_world_with_instance_culling(lib, monkeypatch, load_dist, size):
     assert len(diff[0]) == 0, (len(diff[0]), diff[0][:5], diff[1][:5])
     sky = np.array([0xC0, 0xE8, 0xF6, 0xFF], np.uint8)
     assert 0.05 < (fb != sky).any(-1).mean() < 0.99
+
+
+def test_random_affine_instances_in_shuffled_order(lib, monkeypatch):
+    """Overlapping instances with rotations, non-uniform scales and shears (condition numbers from
+    1 to about 4000, so that the per-instance depth bound is both used and switched off), some
+    close to the camera, in shuffled draw order so that nearer and farther cubes alternate: every
+    pixel (blending and the depth test included) equals the oracle's loop over every instance."""
+    rng = np.random.default_rng(31)
+    w, h = 160, 120
+    monkeypatch.setenv("VTRACE_WIDTH", str(w))
+    monkeypatch.setenv("VTRACE_HEIGHT", str(h))
+    texs = []
+    for k in range(6):
+        n = int(rng.integers(6, 20))
+        t = np.where(rng.random((n, n, n)) < 0.35,
+                     vt.gen_palette(k)[rng.integers(1, 256, (n, n, n))] | 0xFF000000, 0)
+        t[rng.random((n, n, n)) < 0.1] &= 0x7FFFFFFF  # half-transparent texels blend
+        texs.append(np.ascontiguousarray(t.astype(np.uint32)))
+    insts = []
+    for i in range(160):
+        M = np.eye(4)
+        A = rng.normal(size=(3, 3))
+        A = np.linalg.qr(A)[0] @ np.diag(rng.uniform(0.3, 3.0, 3))
+        if i % 5 == 0:
+            A = A @ np.array([[1, rng.uniform(-8, 8), 0], [0, 1, 0], [0, 0, 1]])  # shear
+        if i % 17 == 0:
+            A = A @ np.diag([1, 1, rng.uniform(0.002, 0.01)])  # nearly flat: large condition
+        M[:3, :3] = A
+        M[:3, 3] = rng.uniform(-6, 6, 3) + (0.0, 0.0, -8.0 if i % 9 else -1.0)
+        cm = np.ascontiguousarray(M.T, np.float32).reshape(16)
+        cm[15] = struct.unpack("<f", struct.pack("<i", int(rng.integers(0, len(texs)))))[0]
+        insts.append(cm)
+    insts = np.ascontiguousarray(np.stack(insts))
+    P = perspective(math.radians(80.0), w / h, 0.01, 200.0)
+    C = look_at((0.5, 0.8, 4.0), (0.0, 0.0, -8.0), (0.0, 1.0, 0.0))
+    L = lib
+    assert L.entry() == 0
+    try:
+        for t in texs:
+            nz, ny, nx = t.shape
+            assert L.add_texture(t.ctypes.data, nx, ny, nz) >= 0
+        ptr = L.start_update_instances(len(insts))
+        ctypes.memmove(ptr, insts.ctypes.data, insts.nbytes)
+        assert L.end_update_instances(len(insts)) == 0
+        info = vt.RenderTickInfo(P.ctypes.data, C.ctypes.data)
+        ww, hh = ctypes.c_int32(0), ctypes.c_int32(0)
+        assert L.render_tick(ctypes.byref(ww), ctypes.byref(hh), ctypes.byref(info)) == 0
+        fb = np.zeros((h, w, 4), np.uint8)
+        assert L.vt_framebuffer_download(fb.ctypes.data, fb.nbytes) == 0
+    finally:
+        L.cleanup()
+    grids = [po.Grid(texels=t) for t in texs]
+    want = po.compat_render(grids, insts, P.reshape(16), C.reshape(16), w, h)
+    diff = np.nonzero((fb != want).any(-1))
+    assert len(diff[0]) == 0, (len(diff[0]), diff[0][:5], diff[1][:5])
+    assert (fb != np.array([0xC0, 0xE8, 0xF6, 0xFF], np.uint8)).any(-1).mean() > 0.2

@@ -36,7 +36,8 @@ struct CompatInstance {
     int32_t texture;
     int32_t tx0, ty0, tx1, ty1;  // 16 x 16-pixel tiles its pixels can fall in (inclusive; empty
                                  // when tx0 > tx1)
-    int32_t pad[2];
+    float near;  // at most the slab entry parameter tn of any pixel's ray (0: no bound)
+    int32_t pad;
 };
 
 constexpr int32_t kTile = 16;
@@ -170,6 +171,7 @@ __global__ void __launch_bounds__(128, 8) compat_kernel(const GridView* __restri
         if (!inside) continue;
         const CompatInstance& I = inst[i];
         if (I.texture < 0) continue;  // draws nothing (only reached without bins)
+        if (I.near >= depth) continue;  // tn >= near >= depth: fails the depth test below
         const GridView g = views[I.texture];
         float om[3], dm[3];
 #pragma unroll
@@ -372,6 +374,37 @@ static CullFrame cull_frame(const double* dm, const double* cam, int32_t width, 
 
 // Tile rectangle of an instance (model matrix md, column-major; its inverse mi).  Returns false
 // when no pixel can see it.
+// A lower bound of the slab entry parameter tn (the distance along the unit-length pixel ray) of
+// every pixel's ray, for rejecting the instance behind a pixel's depth before its slab test: the
+// camera's distance to the cube in model space over a bound of the inverse's spectral norm
+// (sqrt(|Minv|_1 |Minv|_inf)), less 1%.  The pixel kernel's binary32 tn is within about
+// cond(M) 2^-21 of the exact one relative to its size, so the 1% holds it above the bound while
+// cond(M) (Frobenius) stays below 1024 and the camera is not within 1/256 of the cube; otherwise 0.
+static __host__ __device__ float instance_near(const CullFrame& cf, const double* md,
+                                               const double* mi) {
+    if (!cf.ok) return 0.0f;
+    double d2 = 0.0, fm = 0.0, fi = 0.0, n1 = 0.0, ninf = 0.0;
+    for (int r = 0; r < 3; ++r) {
+        const double om = mi[0 * 4 + r] * cf.cam[0] + mi[1 * 4 + r] * cf.cam[1] +
+                          mi[2 * 4 + r] * cf.cam[2] + mi[3 * 4 + r];
+        const double e = fmax(fabs(om) - 0.5, 0.0);
+        d2 += e * e;
+        double row = 0.0, col = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            fm += md[k * 4 + r] * md[k * 4 + r];
+            fi += mi[k * 4 + r] * mi[k * 4 + r];
+            row += fabs(mi[k * 4 + r]);  // row r of the inverse's linear part
+            col += fabs(mi[r * 4 + k]);  // column r
+        }
+        ninf = fmax(ninf, row);
+        n1 = fmax(n1, col);
+    }
+    const double dist = sqrt(d2), cond = sqrt(fm) * sqrt(fi), n2 = sqrt(n1 * ninf);
+    if (!(dist > 1.0 / 256.0) || !(cond <= 1024.0) || !(n2 > 0.0) || !isfinite(dist)) return 0.0f;
+    const float near = (float)(0.99 * dist / n2);
+    return isfinite(near) ? near : 0.0f;
+}
+
 static __host__ __device__ bool instance_tiles(const CullFrame& cf, const double* md,
                                                const double* mi, int32_t& tx0, int32_t& ty0,
                                                int32_t& tx1, int32_t& ty1) {
@@ -467,7 +500,8 @@ __global__ void __launch_bounds__(128) compat_prepare_kernel(const float* __rest
     ci.texture = -1;
     ci.tx0 = ci.ty0 = 1;  // empty rectangle: in no tile
     ci.tx1 = ci.ty1 = 0;
-    ci.pad[0] = ci.pad[1] = 0;
+    ci.near = 0.0f;
+    ci.pad = 0;
     if (tid >= 0 && (uint32_t)tid < ntex) {
         double md[16], mi[16];
 #pragma unroll
@@ -477,6 +511,7 @@ __global__ void __launch_bounds__(128) compat_prepare_kernel(const float* __rest
             for (int r = 0; r < 3; ++r)
                 for (int k = 0; k < 4; ++k) ci.minv[4 * r + k] = (float)mi[k * 4 + r];
             ci.texture = tid;
+            ci.near = instance_near(cf, md, mi);
             if (!instance_tiles(cf, md, mi, ci.tx0, ci.ty0, ci.tx1, ci.ty1)) {
                 ci.tx0 = ci.ty0 = 1;
                 ci.tx1 = ci.ty1 = 0;
