@@ -548,64 +548,29 @@ __global__ void __launch_bounds__(256) brick_run_kernel(const uint32_t* __restri
     run[b] = packed;
 }
 
-// Long forward boxes read directly off the runs (K x K cells per octant and axis): cheaper than
-// the pyramid below for the few bricks a paging update touches.  Same values.
-__global__ void __launch_bounds__(256) brick_long_direct_kernel(const uint32_t* __restrict__ oct,
-                                                                const uint32_t* __restrict__ run,
-                                                                uint32_t* __restrict__ lng,
-                                                                int32_t bx, int32_t by, int32_t bz,
-                                                                BrickBox box) {
-    BrickCoord c;
-    uint64_t b;
-    if (!box_brick(box, bx, by, c, b)) return;
-    const uint64_t bricks = (uint64_t)bx * by * bz;
-    const int32_t pos[3] = {c.bxi, c.byi, c.bzi}, n[3] = {bx, by, bz};
-    const int64_t stride[3] = {1, (int64_t)bx, (int64_t)bx * by};
-    const uint32_t ow = __ldg(oct + b);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const int e1 = (a + 1) % 3, e2 = (a + 2) % 3;
-        uint32_t packed = 0;
-        for (int o = 0; o < 8; ++o) {
-            const int32_t K = (int32_t)((ow >> (4 * o)) & 15u);
-            int32_t L = K;
-            if (K > 0 && K < (int32_t)kMaxOctantDistance) {
-                const int32_t s1 = (o >> e1) & 1 ? -1 : 1, s2 = (o >> e2) & 1 ? -1 : 1;
-                const uint32_t nib = 4u * (2u * a + ((o >> a) & 1));
-                L = kMaxOctantDistance;
-                for (int32_t i = 0; i < K && L > K; ++i) {
-                    const int32_t p1 = pos[e1] + i * s1;
-                    if (p1 < 0 || p1 >= n[e1]) break;
-                    for (int32_t j = 0; j < K && L > K; ++j) {
-                        const int32_t p2 = pos[e2] + j * s2;
-                        if (p2 < 0 || p2 >= n[e2]) break;
-                        const int64_t cc = (int64_t)b + (int64_t)i * s1 * stride[e1] +
-                                           (int64_t)j * s2 * stride[e2];
-                        L = min(L, (int32_t)((__ldg(run + cc) >> nib) & 15u));
-                    }
-                }
-                L = max(L, K);
-            }
-            packed |= (uint32_t)L << (4 * o);
-        }
-        lng[(uint64_t)a * bricks + b] = packed;
-    }
-}
-
 // Window minima of the runs: level p of axis a holds, for octant o (nibble o), the smallest run
 // along a toward o over the 2^p x 2^p bricks across from the brick toward o (cells beyond the
 // grid count as the cap).  Level 0 repacks the runs per octant; level p + 1 is the minimum of four
-// level-p blocks.  Layout: pyr[(p * 3 + a) * bricks + brick].
+// level-p blocks.  The levels are stored for the bricks of the index window `pw` (the whole
+// lattice for a full build): pyr[(p * 3 + a) * |pw| + local index in pw].
+__device__ __forceinline__ int64_t pyr_index(const BrickBox& pw, int32_t x, int32_t y, int32_t z) {
+    if (x < pw.x0 || y < pw.y0 || z < pw.z0 || x >= pw.x0 + pw.nx || y >= pw.y0 + pw.ny ||
+        z >= pw.z0 + pw.nz)
+        return -1;  // not stored: the windows of a partial pass are nested so that this is not read
+    return (int64_t)(x - pw.x0) + (int64_t)pw.nx * ((int64_t)(y - pw.y0) + (int64_t)pw.ny * (z - pw.z0));
+}
+
 __global__ void __launch_bounds__(256) brick_pyramid_kernel(const uint32_t* __restrict__ run,
                                                             uint32_t* __restrict__ pyr, int32_t p,
                                                             int32_t bx, int32_t by, int32_t bz,
-                                                            BrickBox box) {
+                                                            BrickBox box, BrickBox pw) {
     BrickCoord c;
     uint64_t b;
     if (!box_brick(box, bx, by, c, b)) return;
-    const uint64_t bricks = (uint64_t)bx * by * bz;
+    const uint64_t pn = (uint64_t)pw.nx * pw.ny * pw.nz;
     const int32_t pos[3] = {c.bxi, c.byi, c.bzi}, n[3] = {bx, by, bz};
-    const int64_t stride[3] = {1, (int64_t)bx, (int64_t)bx * by};
+    const int64_t self_i = pyr_index(pw, c.bxi, c.byi, c.bzi);
+    if (self_i < 0) return;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         uint32_t packed = 0;
@@ -616,17 +581,25 @@ __global__ void __launch_bounds__(256) brick_pyramid_kernel(const uint32_t* __re
         } else {
             const int e1 = (a + 1) % 3, e2 = (a + 2) % 3;
             const int32_t h = 1 << (p - 1);
-            const uint32_t* prev = pyr + (uint64_t)((p - 1) * 3 + a) * bricks;
-            const uint32_t self = __ldg(prev + b);
+            const uint32_t* prev = pyr + (uint64_t)((p - 1) * 3 + a) * pn;
+            const uint32_t self = __ldg(prev + self_i);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {  // lateral signs (bit 0: e1 negative, bit 1: e2 negative)
                 const int32_t s1 = (q & 1) ? -1 : 1, s2 = (q & 2) ? -1 : 1;
-                const bool in1 = pos[e1] + h * s1 >= 0 && pos[e1] + h * s1 < n[e1];
-                const bool in2 = pos[e2] + h * s2 >= 0 && pos[e2] + h * s2 < n[e2];
-                const int64_t d1 = (int64_t)h * s1 * stride[e1], d2 = (int64_t)h * s2 * stride[e2];
-                const uint32_t w1 = in1 ? __ldg(prev + b + d1) : 0xFFFFFFFFu;
-                const uint32_t w2 = in2 ? __ldg(prev + b + d2) : 0xFFFFFFFFu;
-                const uint32_t w3 = in1 && in2 ? __ldg(prev + b + d1 + d2) : 0xFFFFFFFFu;
+                int32_t p1[3] = {pos[0], pos[1], pos[2]}, p2[3] = {pos[0], pos[1], pos[2]},
+                        p3[3] = {pos[0], pos[1], pos[2]};
+                p1[e1] += h * s1;
+                p2[e2] += h * s2;
+                p3[e1] += h * s1;
+                p3[e2] += h * s2;
+                const bool in1 = p1[e1] >= 0 && p1[e1] < n[e1];
+                const bool in2 = p2[e2] >= 0 && p2[e2] < n[e2];
+                const int64_t i1 = in1 ? pyr_index(pw, p1[0], p1[1], p1[2]) : -1;
+                const int64_t i2 = in2 ? pyr_index(pw, p2[0], p2[1], p2[2]) : -1;
+                const int64_t i3 = in1 && in2 ? pyr_index(pw, p3[0], p3[1], p3[2]) : -1;
+                const uint32_t w1 = i1 >= 0 ? __ldg(prev + i1) : 0xFFFFFFFFu;
+                const uint32_t w2 = i2 >= 0 ? __ldg(prev + i2) : 0xFFFFFFFFu;
+                const uint32_t w3 = i3 >= 0 ? __ldg(prev + i3) : 0xFFFFFFFFu;
 #pragma unroll
                 for (int o = 0; o < 8; ++o) {
                     if (((o >> e1) & 1) != (q & 1) || ((o >> e2) & 1) != ((q >> 1) & 1)) continue;
@@ -637,7 +610,7 @@ __global__ void __launch_bounds__(256) brick_pyramid_kernel(const uint32_t* __re
                 }
             }
         }
-        pyr[(uint64_t)(p * 3 + a) * bricks + b] = packed;
+        pyr[(uint64_t)(p * 3 + a) * pn + self_i] = packed;
     }
 }
 
@@ -649,13 +622,14 @@ __global__ void __launch_bounds__(256) brick_pyramid_kernel(const uint32_t* __re
 __global__ void __launch_bounds__(256) brick_long_kernel(const uint32_t* __restrict__ oct,
                                                          const uint32_t* __restrict__ pyr,
                                                          uint32_t* __restrict__ lng, int32_t bx,
-                                                         int32_t by, int32_t bz, BrickBox box) {
+                                                         int32_t by, int32_t bz, BrickBox box,
+                                                         BrickBox pw) {
     BrickCoord c;
     uint64_t b;
     if (!box_brick(box, bx, by, c, b)) return;
     const uint64_t bricks = (uint64_t)bx * by * bz;
+    const uint64_t pn = (uint64_t)pw.nx * pw.ny * pw.nz;
     const int32_t pos[3] = {c.bxi, c.byi, c.bzi}, n[3] = {bx, by, bz};
-    const int64_t stride[3] = {1, (int64_t)bx, (int64_t)bx * by};
     const uint32_t ow = __ldg(oct + b);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -668,16 +642,17 @@ __global__ void __launch_bounds__(256) brick_long_kernel(const uint32_t* __restr
                 const int32_t p = 31 - __clz(K);  // 2^p <= K < 2^(p+1), p <= 3
                 const int32_t off = K - (1 << p);
                 const int32_t s1 = (o >> e1) & 1 ? -1 : 1, s2 = (o >> e2) & 1 ? -1 : 1;
-                const uint32_t* lev = pyr + (uint64_t)(p * 3 + a) * bricks;
+                const uint32_t* lev = pyr + (uint64_t)(p * 3 + a) * pn;
                 L = kMaxOctantDistance;
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const int32_t o1 = (k & 1) ? off : 0, o2 = (k & 2) ? off : 0;
-                    const int32_t p1 = pos[e1] + o1 * s1, p2 = pos[e2] + o2 * s2;
-                    if (p1 < 0 || p1 >= n[e1] || p2 < 0 || p2 >= n[e2]) continue;
-                    const int64_t cc = (int64_t)b + (int64_t)o1 * s1 * stride[e1] +
-                                       (int64_t)o2 * s2 * stride[e2];
-                    L = min(L, (int32_t)((__ldg(lev + cc) >> (4 * o)) & 15u));
+                    int32_t q[3] = {pos[0], pos[1], pos[2]};
+                    q[e1] += o1 * s1;
+                    q[e2] += o2 * s2;
+                    if (q[e1] < 0 || q[e1] >= n[e1] || q[e2] < 0 || q[e2] >= n[e2]) continue;
+                    const int64_t cc = pyr_index(pw, q[0], q[1], q[2]);
+                    if (cc >= 0) L = min(L, (int32_t)((__ldg(lev + cc) >> (4 * o)) & 15u));
                 }
                 L = max(L, K);
             }
@@ -719,29 +694,55 @@ cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* 
     return cudaGetLastError();
 }
 
+// Index windows of the long-box passes after a change inside `changed`: long words within 15
+// bricks of it; the pyramid's level 3 within 6 more (the long kernel reads level p up to
+// K - 2^p <= 6 bricks across), level 2 within 4 more, level 1 within 2, level 0 and the runs
+// within 1 (level p + 1 reads level p 2^p bricks across).
+struct LongWindows {
+    BrickBox w, wp[4];
+};
+
+static LongWindows long_windows(const BrickBox& changed, int32_t bx, int32_t by, int32_t bz);
+
+size_t brick_long_scratch_words(const BrickBox* changed, int32_t bx, int32_t by, int32_t bz) {
+    const uint64_t bricks = (uint64_t)bx * by * bz;
+    if (!changed) return (size_t)(13 * bricks);
+    const BrickBox& p0 = long_windows(*changed, bx, by, bz).wp[0];
+    return (size_t)(bricks + 12ull * (uint64_t)p0.nx * p0.ny * p0.nz);
+}
+
 cudaError_t launch_brick_long(const uint32_t* dir, const uint32_t* oct, uint32_t* tmp,
                               uint32_t* lng, int32_t bx, int32_t by, int32_t bz,
                               cudaStream_t stream, const BrickBox* changed) {
-    // tmp: runs (1 word per brick), then the pyramid (12 words per brick).  With a change, long
-    // boxes are recomputed within 15 bricks of it, directly from the runs, which they read up to
-    // 13 bricks across (and the runs are recomputed there).
-    const int32_t R = (int32_t)kMaxOctantDistance;
+    // tmp: runs (1 word per brick), then the pyramid (12 words per brick of its index window)
     const uint64_t bricks = (uint64_t)bx * by * bz;
     uint32_t* run = tmp;
     uint32_t* pyr = tmp + bricks;
+    const BrickBox all = {0, 0, 0, bx, by, bz};
+    LongWindows L;
     if (changed) {
-        const BrickBox w = grow(*changed, R, R, R, bx, by, bz);
-        const BrickBox wr = grow(w, R - 2, R - 2, R - 2, bx, by, bz);
-        brick_run_kernel<<<box_blocks(wr), 256, 0, stream>>>(dir, run, bx, by, bz, wr);
-        brick_long_direct_kernel<<<box_blocks(w), 256, 0, stream>>>(oct, run, lng, bx, by, bz, w);
-        return cudaGetLastError();
+        L = long_windows(*changed, bx, by, bz);
+    } else {
+        L.w = all;
+        for (int p = 0; p < 4; ++p) L.wp[p] = all;
     }
-    const BrickBox w = {0, 0, 0, bx, by, bz};
-    brick_run_kernel<<<box_blocks(w), 256, 0, stream>>>(dir, run, bx, by, bz, w);
+    brick_run_kernel<<<box_blocks(L.wp[0]), 256, 0, stream>>>(dir, run, bx, by, bz, L.wp[0]);
     for (int32_t p = 0; p < 4; ++p)
-        brick_pyramid_kernel<<<box_blocks(w), 256, 0, stream>>>(run, pyr, p, bx, by, bz, w);
-    brick_long_kernel<<<box_blocks(w), 256, 0, stream>>>(oct, pyr, lng, bx, by, bz, w);
+        brick_pyramid_kernel<<<box_blocks(L.wp[p]), 256, 0, stream>>>(run, pyr, p, bx, by, bz,
+                                                                       L.wp[p], L.wp[0]);
+    brick_long_kernel<<<box_blocks(L.w), 256, 0, stream>>>(oct, pyr, lng, bx, by, bz, L.w, L.wp[0]);
     return cudaGetLastError();
+}
+
+static LongWindows long_windows(const BrickBox& changed, int32_t bx, int32_t by, int32_t bz) {
+    const int32_t R = (int32_t)kMaxOctantDistance;
+    LongWindows L;
+    L.w = grow(changed, R, R, R, bx, by, bz);
+    L.wp[3] = grow(L.w, 6, 6, 6, bx, by, bz);
+    L.wp[2] = grow(L.wp[3], 4, 4, 4, bx, by, bz);
+    L.wp[1] = grow(L.wp[2], 2, 2, 2, bx, by, bz);
+    L.wp[0] = grow(L.wp[1], 1, 1, 1, bx, by, bz);
+    return L;
 }
 
 cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,

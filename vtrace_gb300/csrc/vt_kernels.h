@@ -94,11 +94,14 @@ cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* 
                                  cudaStream_t stream, const BrickBox* changed = nullptr);
 
 // Phase 4: Chebyshev distance of every empty brick to the nearest occupied one, into dir.
-// Long forward boxes (3 words per brick, axis-major) from the directory and the octant words;
-// tmp holds 13 words per brick.
+// Long forward boxes (3 words per brick, axis-major) from the directory and the octant words, for
+// every brick or (changed != nullptr) for the bricks a change inside `changed` can affect; tmp
+// holds brick_long_scratch_words() words (13 per brick for a full pass, the runs of every brick
+// and a windowed pyramid after a change).
 cudaError_t launch_brick_long(const uint32_t* dir, const uint32_t* oct, uint32_t* tmp,
                               uint32_t* lng, int32_t bx, int32_t by, int32_t bz,
                               cudaStream_t stream, const BrickBox* changed = nullptr);
+size_t brick_long_scratch_words(const BrickBox* changed, int32_t bx, int32_t by, int32_t bz);
 cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,
                                   int32_t bz, cudaStream_t stream,
                                   const BrickBox* changed = nullptr);

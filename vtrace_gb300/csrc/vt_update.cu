@@ -196,7 +196,9 @@ extern "C" int32_t vt_grid_update(int32_t grid, const void* voxels, uint32_t ord
     const size_t o_old = o_flags + al(K * 4), o_slots = o_old + al(K * 4), o_delta = o_slots + al(K * 4);
     const size_t o_da = o_delta + 256, o_db = o_da + al(g->bricks), o_ty = o_db + al(g->bricks);
     const size_t o_run = o_ty + al(g->bricks * 2);
-    const size_t total = o_run + al(g->bricks * 4);
+    const BrickBox changed = {u.bx0, u.by0, u.bz0, u.kx, u.ky, u.kz};
+    const size_t total = o_run + al(4 * brick_long_scratch_words(&changed, (int32_t)g->bx,
+                                                                  (int32_t)g->by, (int32_t)g->bz));
     char* scr = nullptr;
     cudaError_t e = cudaMallocAsync((void**)&scr, total, st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_grid_update: scratch");
@@ -269,7 +271,6 @@ extern "C" int32_t vt_grid_update(int32_t grid, const void* voxels, uint32_t ord
         BuildScratch bs;
         bs.dist_a = (uint8_t*)(scr + o_da);
         bs.dist_b = (uint8_t*)(scr + o_db);
-        const BrickBox changed = {u.bx0, u.by0, u.bz0, u.kx, u.ky, u.kz};
         if (e == cudaSuccess)
             e = launch_brick_distance(bs, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st,
                                       &changed);
