@@ -1,6 +1,7 @@
 """Large-grid brick builds (more than 512 bricks, built by launches rather than the small-grid
-graph; the words pass stages each occupied brick's voxels for the compaction): the directory, the
-masks and every payload byte equal a brute-force restatement of the layout (lib/memory.c:353-366
+graph; the words pass stages each occupied brick's voxels for the compaction, and the passes along
+x read an occupancy bitmask): the directory with its distances, the masks, every payload byte and
+the octant and long-box words equal brute-force restatements of the layout (lib/memory.c:353-366
 gives the dense x-fastest input), for u8 grids with and without the "index != 0" occupancy
 shortcut, RGBA8 texels, z-fastest chunks and device input, at sizes with partial bricks on every
 axis and rows that are not 8-byte aligned."""
@@ -8,7 +9,7 @@ import numpy as np
 import pytest
 
 import vtrace_gb300 as vt
-from test_gpu_parity import expected_bricks
+from test_gpu_parity import expected_bricks, expected_long, expected_octants
 
 pytestmark = pytest.mark.gpu
 
@@ -47,6 +48,11 @@ def check_layout(g, vox, pal, texels=None):
     if texels is not None:
         got = got.view(np.uint32)[..., 0]
     np.testing.assert_array_equal(got, want)
+    # the empty-box words (octant and long boxes), against the brute-force restatements
+    dims = vox.shape[::-1]
+    oc = g.octants()
+    np.testing.assert_array_equal(oc, expected_octants(d, dims))
+    np.testing.assert_array_equal(g.long_boxes(), expected_long(d, oc, dims))
 
 
 def random_vox(rng, dims, density):

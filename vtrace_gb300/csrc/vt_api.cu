@@ -211,17 +211,23 @@ static cudaError_t build_launches(const void* d_src, uint32_t format, const uint
     if (e == cudaSuccess) e = launch_brick_scan(s, g.bricks, stream);
     if (e == cudaSuccess)
         e = launch_brick_compact(d_src, format, nx, ny, nz, s, g.dir, g.masks, g.payload, stream);
+    // the occupancy words are no longer needed: their scratch (16 words per brick) holds the
+    // occupancy bitmask of the passes along x (words 13 on), the octant passes, and then the
+    // long-box runs and window minima (words 0-12)
+    uint32_t* occ = (uint32_t*)s.words + 13 * g.bricks;
     if (e == cudaSuccess)
-        e = launch_brick_distance(s, g.dir, (int32_t)g.bx, (int32_t)g.by, (int32_t)g.bz, stream);
-    // the occupancy words are no longer needed: their scratch holds the octant passes, and then
-    // the long-box runs and window minima (13 words per brick of the 16 there)
+        e = launch_brick_xmask(g.dir, occ, (int32_t)g.bx, (int32_t)g.by, (int32_t)g.bz, stream);
+    if (e == cudaSuccess)
+        e = launch_brick_distance(s, g.dir, (int32_t)g.bx, (int32_t)g.by, (int32_t)g.bz, stream,
+                                  nullptr, occ);
     if (e == cudaSuccess)
         e = launch_brick_octants(g.dir, (uint8_t*)s.words,
                                  (uint16_t*)((uint8_t*)s.words + ((g.bricks + 255) / 256) * 256),
-                                 g.oct, (int32_t)g.bx, (int32_t)g.by, (int32_t)g.bz, stream);
+                                 g.oct, (int32_t)g.bx, (int32_t)g.by, (int32_t)g.bz, stream,
+                                 nullptr, occ);
     if (e == cudaSuccess)
         e = launch_brick_long(g.dir, g.oct, (uint32_t*)s.words, g.lng, (int32_t)g.bx,
-                              (int32_t)g.by, (int32_t)g.bz, stream);
+                              (int32_t)g.by, (int32_t)g.bz, stream, nullptr, occ);
     return e;
 }
 
@@ -486,15 +492,20 @@ int32_t build_grid(const void* d_src, uint32_t format, const uint32_t* palette_h
         // octant and long-box passes: build_launches' sequence after its scan
         e = launch_brick_compact(d_src, format, (int32_t)nx, (int32_t)ny, (int32_t)nz, s, g->dir,
                                  g->masks, g->payload, stream);
+        uint32_t* occ = (uint32_t*)s.words + 13 * g->bricks;  // as in build_launches
         if (e == cudaSuccess)
-            e = launch_brick_distance(s, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
+            e = launch_brick_xmask(g->dir, occ, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
+        if (e == cudaSuccess)
+            e = launch_brick_distance(s, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz,
+                                      stream, nullptr, occ);
         if (e == cudaSuccess)
             e = launch_brick_octants(g->dir, (uint8_t*)s.words,
                                      (uint16_t*)((uint8_t*)s.words + ((g->bricks + 255) / 256) * 256),
-                                     g->oct, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream);
+                                     g->oct, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, stream,
+                                     nullptr, occ);
         if (e == cudaSuccess)
             e = launch_brick_long(g->dir, g->oct, (uint32_t*)s.words, g->lng, (int32_t)g->bx,
-                                  (int32_t)g->by, (int32_t)g->bz, stream);
+                                  (int32_t)g->by, (int32_t)g->bz, stream, nullptr, occ);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
         if (e != cudaSuccess) { rc = cuda_fail(e, "brick build"); break; }
         g->bytes = g->block_bytes;

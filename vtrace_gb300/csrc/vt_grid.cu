@@ -387,6 +387,54 @@ cudaError_t launch_brick_compact(const void* src, uint32_t format, int32_t nx, i
     return cudaGetLastError();
 }
 
+// Occupancy bitmask of the brick lattice for the passes along x: row (y, z) is occ_words(bx) words,
+// bit x of the row set iff brick (x, y, z) is occupied.  One thread per word.
+__host__ __device__ __forceinline__ int32_t occ_words(int32_t bx) { return (bx + 31) >> 5; }
+
+__global__ void __launch_bounds__(256) brick_xmask_kernel(const uint32_t* __restrict__ dir,
+                                                          uint32_t* __restrict__ occ, int32_t bx,
+                                                          uint64_t words) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= words) return;
+    const int32_t rw = occ_words(bx);
+    const uint64_t row = t / (uint64_t)rw;
+    const int32_t x0 = (int32_t)(t - row * (uint64_t)rw) * 32;
+    const uint32_t* d = dir + row * (uint64_t)bx + x0;
+    const int32_t n = min(32, bx - x0);
+    uint32_t m = 0;
+    for (int32_t k = 0; k < n; ++k) m |= (uint32_t)!brick_empty(__ldg(d + k)) << k;
+    occ[t] = m;
+}
+
+// Steps from brick x of an occupancy row to the nearest occupied brick in direction s (+1 / -1),
+// the brick itself included (0 when occupied), or `cap` (<= 31) when none lies within cap - 1
+// steps; beyond the row counts as empty.  Reads at most two words.
+__device__ __forceinline__ int32_t occ_fwd(const uint32_t* __restrict__ row, int32_t rw, int32_t x,
+                                           int32_t s, int32_t cap) {
+    const int32_t w = x >> 5, b = x & 31;
+    if (s > 0) {
+        uint64_t v = __ldg(row + w);
+        if (w + 1 < rw) v |= (uint64_t)__ldg(row + w + 1) << 32;
+        const uint32_t m = (uint32_t)(v >> b) & ((1u << cap) - 1u);  // bit k: brick x + k
+        return m ? __ffs(m) - 1 : cap;
+    }
+    uint64_t v = (uint64_t)__ldg(row + w) << 32;
+    if (w > 0) v |= __ldg(row + w - 1);
+    const uint32_t m = (uint32_t)((v << (31 - b)) >> 32) & ~((1u << (32 - cap)) - 1u);  // bit 31 - k: brick x - k
+    return m ? __clz(m) : cap;
+}
+
+cudaError_t launch_brick_xmask(const uint32_t* dir, uint32_t* occ, int32_t bx, int32_t by,
+                               int32_t bz, cudaStream_t stream) {
+    const uint64_t words = (uint64_t)occ_words(bx) * by * bz;
+    brick_xmask_kernel<<<(unsigned)((words + 255) / 256), 256, 0, stream>>>(dir, occ, bx, words);
+    return cudaGetLastError();
+}
+
+size_t brick_xmask_words(int32_t bx, int32_t by, int32_t bz) {
+    return (size_t)occ_words(bx) * by * bz;
+}
+
 // Chebyshev (L-infinity) distance, in bricks, from each empty brick to the nearest occupied one,
 // capped at kMaxBrickDistance.  The transform is separable: pass x computes the 1D distance
 // along x; passes y and z take min over the line of max(|offset|, previous pass), which composes
@@ -396,10 +444,18 @@ __global__ void __launch_bounds__(256) brick_distance_kernel(uint32_t* __restric
                                                              const uint8_t* __restrict__ in,
                                                              uint8_t* __restrict__ out,
                                                              int32_t bx, int32_t by, int32_t bz,
-                                                             BrickBox box) {
+                                                             BrickBox box,
+                                                             const uint32_t* __restrict__ occ) {
     BrickCoord c;
     uint64_t b;
     if (!box_brick(box, bx, by, c, b)) return;
+    if (AXIS == 0 && occ) {  // pass x from the occupancy rows
+        const int32_t rw = occ_words(bx);
+        const uint32_t* row = occ + ((uint64_t)c.bzi * by + c.byi) * rw;
+        const int32_t cap = (int32_t)kMaxBrickDistance;
+        out[b] = (uint8_t)min(occ_fwd(row, rw, c.bxi, 1, cap), occ_fwd(row, rw, c.bxi, -1, cap));
+        return;
+    }
     const int32_t pos = AXIS == 0 ? c.bxi : (AXIS == 1 ? c.byi : c.bzi);
     const int32_t n = AXIS == 0 ? bx : (AXIS == 1 ? by : bz);
     const int64_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? (int64_t)bx : (int64_t)bx * by);
@@ -436,10 +492,18 @@ constexpr int kMaxOctantDistance = 15;
 __global__ void __launch_bounds__(256) brick_octant_x_kernel(const uint32_t* __restrict__ dir,
                                                              uint8_t* __restrict__ out,
                                                              int32_t bx, int32_t by,
-                                                             BrickBox box) {
+                                                             BrickBox box,
+                                                             const uint32_t* __restrict__ occ) {
     BrickCoord c;
     uint64_t b;
     if (!box_brick(box, bx, by, c, b)) return;
+    if (occ) {
+        const int32_t rw = occ_words(bx);
+        const uint32_t* row = occ + ((uint64_t)c.bzi * by + c.byi) * rw;
+        const int32_t cap = (int32_t)kMaxOctantDistance;
+        out[b] = (uint8_t)(occ_fwd(row, rw, c.bxi, 1, cap) | (occ_fwd(row, rw, c.bxi, -1, cap) << 4));
+        return;
+    }
     uint32_t packed = 0;
 #pragma unroll
     for (int neg = 0; neg < 2; ++neg) {
@@ -521,15 +585,25 @@ __global__ void __launch_bounds__(256) brick_octant_z_kernel(const uint16_t* __r
 // grid counts as empty.  Nibble 2a + (s < 0).
 __global__ void __launch_bounds__(256) brick_run_kernel(const uint32_t* __restrict__ dir,
                                                         uint32_t* __restrict__ run, int32_t bx,
-                                                        int32_t by, int32_t bz, BrickBox box) {
+                                                        int32_t by, int32_t bz, BrickBox box,
+                                                        const uint32_t* __restrict__ occ) {
     BrickCoord c;
     uint64_t b;
     if (!box_brick(box, bx, by, c, b)) return;
     const int32_t pos[3] = {c.bxi, c.byi, c.bzi}, n[3] = {bx, by, bz};
     const int64_t stride[3] = {1, (int64_t)bx, (int64_t)bx * by};
     uint32_t packed = 0;
+    int a0 = 0;
+    if (occ) {  // axis x from the occupancy rows
+        const int32_t rw = occ_words(bx);
+        const uint32_t* row = occ + ((uint64_t)c.bzi * by + c.byi) * rw;
+        const int32_t cap = (int32_t)kMaxOctantDistance;
+        packed = (uint32_t)occ_fwd(row, rw, c.bxi, 1, cap) | ((uint32_t)occ_fwd(row, rw, c.bxi, -1, cap) << 4);
+        a0 = 1;
+    }
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
+        if (a < a0) continue;
 #pragma unroll
         for (int neg = 0; neg < 2; ++neg) {
             const int32_t sg = neg ? -1 : 1;
@@ -560,6 +634,18 @@ __device__ __forceinline__ int64_t pyr_index(const BrickBox& pw, int32_t x, int3
     return (int64_t)(x - pw.x0) + (int64_t)pw.nx * ((int64_t)(y - pw.y0) + (int64_t)pw.ny * (z - pw.z0));
 }
 
+// WIN: `pw` is a window of the lattice (a partial pass, whose windows are nested so that every
+// neighbour read lies in it; checked all the same); otherwise it is the whole lattice and the local
+// index is the brick index.  Neighbours are addressed by local strides.
+template <bool WIN>
+__device__ __forceinline__ bool pyr_in(const BrickBox& pw, int a, int32_t v) {
+    if (!WIN) return true;
+    const int32_t lo = a == 0 ? pw.x0 : (a == 1 ? pw.y0 : pw.z0);
+    const int32_t n = a == 0 ? pw.nx : (a == 1 ? pw.ny : pw.nz);
+    return v >= lo && v < lo + n;
+}
+
+template <bool WIN>
 __global__ void __launch_bounds__(256) brick_pyramid_kernel(const uint32_t* __restrict__ run,
                                                             uint32_t* __restrict__ pyr, int32_t p,
                                                             int32_t bx, int32_t by, int32_t bz,
@@ -569,7 +655,8 @@ __global__ void __launch_bounds__(256) brick_pyramid_kernel(const uint32_t* __re
     if (!box_brick(box, bx, by, c, b)) return;
     const uint64_t pn = (uint64_t)pw.nx * pw.ny * pw.nz;
     const int32_t pos[3] = {c.bxi, c.byi, c.bzi}, n[3] = {bx, by, bz};
-    const int64_t self_i = pyr_index(pw, c.bxi, c.byi, c.bzi);
+    const int64_t ls[3] = {1, (int64_t)pw.nx, (int64_t)pw.nx * pw.ny};
+    const int64_t self_i = WIN ? pyr_index(pw, c.bxi, c.byi, c.bzi) : (int64_t)b;
     if (self_i < 0) return;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -586,20 +673,13 @@ __global__ void __launch_bounds__(256) brick_pyramid_kernel(const uint32_t* __re
 #pragma unroll
             for (int q = 0; q < 4; ++q) {  // lateral signs (bit 0: e1 negative, bit 1: e2 negative)
                 const int32_t s1 = (q & 1) ? -1 : 1, s2 = (q & 2) ? -1 : 1;
-                int32_t p1[3] = {pos[0], pos[1], pos[2]}, p2[3] = {pos[0], pos[1], pos[2]},
-                        p3[3] = {pos[0], pos[1], pos[2]};
-                p1[e1] += h * s1;
-                p2[e2] += h * s2;
-                p3[e1] += h * s1;
-                p3[e2] += h * s2;
-                const bool in1 = p1[e1] >= 0 && p1[e1] < n[e1];
-                const bool in2 = p2[e2] >= 0 && p2[e2] < n[e2];
-                const int64_t i1 = in1 ? pyr_index(pw, p1[0], p1[1], p1[2]) : -1;
-                const int64_t i2 = in2 ? pyr_index(pw, p2[0], p2[1], p2[2]) : -1;
-                const int64_t i3 = in1 && in2 ? pyr_index(pw, p3[0], p3[1], p3[2]) : -1;
-                const uint32_t w1 = i1 >= 0 ? __ldg(prev + i1) : 0xFFFFFFFFu;
-                const uint32_t w2 = i2 >= 0 ? __ldg(prev + i2) : 0xFFFFFFFFu;
-                const uint32_t w3 = i3 >= 0 ? __ldg(prev + i3) : 0xFFFFFFFFu;
+                const int32_t c1 = pos[e1] + h * s1, c2 = pos[e2] + h * s2;
+                const bool in1 = c1 >= 0 && c1 < n[e1] && pyr_in<WIN>(pw, e1, c1);
+                const bool in2 = c2 >= 0 && c2 < n[e2] && pyr_in<WIN>(pw, e2, c2);
+                const int64_t d1 = (int64_t)h * s1 * ls[e1], d2 = (int64_t)h * s2 * ls[e2];
+                const uint32_t w1 = in1 ? __ldg(prev + self_i + d1) : 0xFFFFFFFFu;
+                const uint32_t w2 = in2 ? __ldg(prev + self_i + d2) : 0xFFFFFFFFu;
+                const uint32_t w3 = in1 && in2 ? __ldg(prev + self_i + d1 + d2) : 0xFFFFFFFFu;
 #pragma unroll
                 for (int o = 0; o < 8; ++o) {
                     if (((o >> e1) & 1) != (q & 1) || ((o >> e2) & 1) != ((q >> 1) & 1)) continue;
@@ -619,6 +699,7 @@ __global__ void __launch_bounds__(256) brick_pyramid_kernel(const uint32_t* __re
 // is empty: the smallest run along a over the box's K x K cross-section, read as the minimum of
 // four overlapping 2^p blocks of the pyramid (2^p <= K < 2^(p+1)).  L >= K since the cube is
 // empty; K = 0 (occupied brick) gives 0 and K at the cap gives the cap.
+template <bool WIN>
 __global__ void __launch_bounds__(256) brick_long_kernel(const uint32_t* __restrict__ oct,
                                                          const uint32_t* __restrict__ pyr,
                                                          uint32_t* __restrict__ lng, int32_t bx,
@@ -630,6 +711,8 @@ __global__ void __launch_bounds__(256) brick_long_kernel(const uint32_t* __restr
     const uint64_t bricks = (uint64_t)bx * by * bz;
     const uint64_t pn = (uint64_t)pw.nx * pw.ny * pw.nz;
     const int32_t pos[3] = {c.bxi, c.byi, c.bzi}, n[3] = {bx, by, bz};
+    const int64_t ls[3] = {1, (int64_t)pw.nx, (int64_t)pw.nx * pw.ny};
+    const int64_t self_i = WIN ? pyr_index(pw, c.bxi, c.byi, c.bzi) : (int64_t)b;
     const uint32_t ow = __ldg(oct + b);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -638,7 +721,7 @@ __global__ void __launch_bounds__(256) brick_long_kernel(const uint32_t* __restr
         for (int o = 0; o < 8; ++o) {
             const int32_t K = (int32_t)((ow >> (4 * o)) & 15u);
             int32_t L = K;
-            if (K > 0 && K < (int32_t)kMaxOctantDistance) {
+            if (K > 0 && K < (int32_t)kMaxOctantDistance && self_i >= 0) {
                 const int32_t p = 31 - __clz(K);  // 2^p <= K < 2^(p+1), p <= 3
                 const int32_t off = K - (1 << p);
                 const int32_t s1 = (o >> e1) & 1 ? -1 : 1, s2 = (o >> e2) & 1 ? -1 : 1;
@@ -647,12 +730,11 @@ __global__ void __launch_bounds__(256) brick_long_kernel(const uint32_t* __restr
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {
                     const int32_t o1 = (k & 1) ? off : 0, o2 = (k & 2) ? off : 0;
-                    int32_t q[3] = {pos[0], pos[1], pos[2]};
-                    q[e1] += o1 * s1;
-                    q[e2] += o2 * s2;
-                    if (q[e1] < 0 || q[e1] >= n[e1] || q[e2] < 0 || q[e2] >= n[e2]) continue;
-                    const int64_t cc = pyr_index(pw, q[0], q[1], q[2]);
-                    if (cc >= 0) L = min(L, (int32_t)((__ldg(lev + cc) >> (4 * o)) & 15u));
+                    const int32_t c1 = pos[e1] + o1 * s1, c2 = pos[e2] + o2 * s2;
+                    if (c1 < 0 || c1 >= n[e1] || c2 < 0 || c2 >= n[e2]) continue;
+                    if (!pyr_in<WIN>(pw, e1, c1) || !pyr_in<WIN>(pw, e2, c2)) continue;
+                    const int64_t cc = self_i + (int64_t)o1 * s1 * ls[e1] + (int64_t)o2 * s2 * ls[e2];
+                    L = min(L, (int32_t)((__ldg(lev + cc) >> (4 * o)) & 15u));
                 }
                 L = max(L, K);
             }
@@ -681,14 +763,15 @@ static BrickBox grow(const BrickBox& b, int32_t gx, int32_t gy, int32_t gz, int3
 
 cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* tmp_y,
                                  uint32_t* oct, int32_t bx, int32_t by, int32_t bz,
-                                 cudaStream_t stream, const BrickBox* changed) {
+                                 cudaStream_t stream, const BrickBox* changed,
+                                 const uint32_t* occ) {
     // pass z at the bricks within reach of a change reads pass y up to 14 bricks away in z, which
     // reads pass x up to 14 away in y
     const int32_t R = (int32_t)kMaxOctantDistance - 1;
     const BrickBox all = {0, 0, 0, bx, by, bz};
     const BrickBox w = changed ? grow(*changed, R, R, R, bx, by, bz) : all;
     const BrickBox wy = grow(w, 0, 0, R, bx, by, bz), wx = grow(w, 0, R, R, bx, by, bz);
-    brick_octant_x_kernel<<<box_blocks(wx), 256, 0, stream>>>(dir, tmp_x, bx, by, wx);
+    brick_octant_x_kernel<<<box_blocks(wx), 256, 0, stream>>>(dir, tmp_x, bx, by, wx, occ);
     brick_octant_y_kernel<<<box_blocks(wy), 256, 0, stream>>>(tmp_x, tmp_y, bx, by, wy);
     brick_octant_z_kernel<<<box_blocks(w), 256, 0, stream>>>(tmp_y, oct, bx, by, bz, w);
     return cudaGetLastError();
@@ -713,7 +796,8 @@ size_t brick_long_scratch_words(const BrickBox* changed, int32_t bx, int32_t by,
 
 cudaError_t launch_brick_long(const uint32_t* dir, const uint32_t* oct, uint32_t* tmp,
                               uint32_t* lng, int32_t bx, int32_t by, int32_t bz,
-                              cudaStream_t stream, const BrickBox* changed) {
+                              cudaStream_t stream, const BrickBox* changed,
+                              const uint32_t* occ) {
     // tmp: runs (1 word per brick), then the pyramid (12 words per brick of its index window)
     const uint64_t bricks = (uint64_t)bx * by * bz;
     uint32_t* run = tmp;
@@ -726,11 +810,19 @@ cudaError_t launch_brick_long(const uint32_t* dir, const uint32_t* oct, uint32_t
         L.w = all;
         for (int p = 0; p < 4; ++p) L.wp[p] = all;
     }
-    brick_run_kernel<<<box_blocks(L.wp[0]), 256, 0, stream>>>(dir, run, bx, by, bz, L.wp[0]);
-    for (int32_t p = 0; p < 4; ++p)
-        brick_pyramid_kernel<<<box_blocks(L.wp[p]), 256, 0, stream>>>(run, pyr, p, bx, by, bz,
-                                                                       L.wp[p], L.wp[0]);
-    brick_long_kernel<<<box_blocks(L.w), 256, 0, stream>>>(oct, pyr, lng, bx, by, bz, L.w, L.wp[0]);
+    brick_run_kernel<<<box_blocks(L.wp[0]), 256, 0, stream>>>(dir, run, bx, by, bz, L.wp[0], occ);
+    for (int32_t p = 0; p < 4; ++p) {
+        if (changed)
+            brick_pyramid_kernel<true><<<box_blocks(L.wp[p]), 256, 0, stream>>>(
+                run, pyr, p, bx, by, bz, L.wp[p], L.wp[0]);
+        else
+            brick_pyramid_kernel<false><<<box_blocks(L.wp[p]), 256, 0, stream>>>(
+                run, pyr, p, bx, by, bz, L.wp[p], L.wp[0]);
+    }
+    if (changed)
+        brick_long_kernel<true><<<box_blocks(L.w), 256, 0, stream>>>(oct, pyr, lng, bx, by, bz, L.w, L.wp[0]);
+    else
+        brick_long_kernel<false><<<box_blocks(L.w), 256, 0, stream>>>(oct, pyr, lng, bx, by, bz, L.w, L.wp[0]);
     return cudaGetLastError();
 }
 
@@ -746,16 +838,17 @@ static LongWindows long_windows(const BrickBox& changed, int32_t bx, int32_t by,
 }
 
 cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,
-                                  int32_t bz, cudaStream_t stream, const BrickBox* changed) {
+                                  int32_t bz, cudaStream_t stream, const BrickBox* changed,
+                                  const uint32_t* occ) {
     // distances change only within kMaxBrickDistance of a change; each pass reads the previous
     // one up to that far along its axis
     const int32_t R = (int32_t)kMaxBrickDistance;
     const BrickBox all = {0, 0, 0, bx, by, bz};
     const BrickBox w = changed ? grow(*changed, R, R, R, bx, by, bz) : all;
     const BrickBox w1 = grow(w, 0, 0, R, bx, by, bz), w0 = grow(w, 0, R, R, bx, by, bz);
-    brick_distance_kernel<0><<<box_blocks(w0), 256, 0, stream>>>(dir, nullptr, s.dist_a, bx, by, bz, w0);
-    brick_distance_kernel<1><<<box_blocks(w1), 256, 0, stream>>>(dir, s.dist_a, s.dist_b, bx, by, bz, w1);
-    brick_distance_kernel<2><<<box_blocks(w), 256, 0, stream>>>(dir, s.dist_b, nullptr, bx, by, bz, w);
+    brick_distance_kernel<0><<<box_blocks(w0), 256, 0, stream>>>(dir, nullptr, s.dist_a, bx, by, bz, w0, occ);
+    brick_distance_kernel<1><<<box_blocks(w1), 256, 0, stream>>>(dir, s.dist_a, s.dist_b, bx, by, bz, w1, nullptr);
+    brick_distance_kernel<2><<<box_blocks(w), 256, 0, stream>>>(dir, s.dist_b, nullptr, bx, by, bz, w, nullptr);
     return cudaGetLastError();
 }
 

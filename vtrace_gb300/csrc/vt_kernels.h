@@ -91,7 +91,14 @@ struct BrickBox {
 // `changed` can affect.
 cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* tmp_y,
                                  uint32_t* oct, int32_t bx, int32_t by, int32_t bz,
-                                 cudaStream_t stream, const BrickBox* changed = nullptr);
+                                 cudaStream_t stream, const BrickBox* changed = nullptr,
+                                 const uint32_t* occ = nullptr);
+// Occupancy bitmask of the directory (brick_xmask_words() words: one bit per brick, rows along x
+// padded to 32 bits), from which the passes along x read their distances when it is given
+// (`occ` of the distance, octant and long-box launches) instead of scanning the directory.
+cudaError_t launch_brick_xmask(const uint32_t* dir, uint32_t* occ, int32_t bx, int32_t by,
+                               int32_t bz, cudaStream_t stream);
+size_t brick_xmask_words(int32_t bx, int32_t by, int32_t bz);
 
 // Phase 4: Chebyshev distance of every empty brick to the nearest occupied one, into dir.
 // Long forward boxes (3 words per brick, axis-major) from the directory and the octant words, for
@@ -100,10 +107,11 @@ cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* 
 // and a windowed pyramid after a change).
 cudaError_t launch_brick_long(const uint32_t* dir, const uint32_t* oct, uint32_t* tmp,
                               uint32_t* lng, int32_t bx, int32_t by, int32_t bz,
-                              cudaStream_t stream, const BrickBox* changed = nullptr);
+                              cudaStream_t stream, const BrickBox* changed = nullptr,
+                              const uint32_t* occ = nullptr);
 size_t brick_long_scratch_words(const BrickBox* changed, int32_t bx, int32_t by, int32_t bz);
 cudaError_t launch_brick_distance(const BuildScratch& s, uint32_t* dir, int32_t bx, int32_t by,
                                   int32_t bz, cudaStream_t stream,
-                                  const BrickBox* changed = nullptr);
+                                  const BrickBox* changed = nullptr, const uint32_t* occ = nullptr);
 
 }  // namespace vt

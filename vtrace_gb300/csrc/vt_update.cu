@@ -197,8 +197,9 @@ extern "C" int32_t vt_grid_update(int32_t grid, const void* voxels, uint32_t ord
     const size_t o_da = o_delta + 256, o_db = o_da + al(g->bricks), o_ty = o_db + al(g->bricks);
     const size_t o_run = o_ty + al(g->bricks * 2);
     const BrickBox changed = {u.bx0, u.by0, u.bz0, u.kx, u.ky, u.kz};
-    const size_t total = o_run + al(4 * brick_long_scratch_words(&changed, (int32_t)g->bx,
+    const size_t o_occ = o_run + al(4 * brick_long_scratch_words(&changed, (int32_t)g->bx,
                                                                   (int32_t)g->by, (int32_t)g->bz));
+    const size_t total = o_occ + al(4 * brick_xmask_words((int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz));
     char* scr = nullptr;
     cudaError_t e = cudaMallocAsync((void**)&scr, total, st);
     if (e != cudaSuccess) return cuda_fail(e, "vt_grid_update: scratch");
@@ -271,15 +272,18 @@ extern "C" int32_t vt_grid_update(int32_t grid, const void* voxels, uint32_t ord
         BuildScratch bs;
         bs.dist_a = (uint8_t*)(scr + o_da);
         bs.dist_b = (uint8_t*)(scr + o_db);
+        uint32_t* occ = (uint32_t*)(scr + o_occ);
+        if (e == cudaSuccess)
+            e = launch_brick_xmask(g->dir, occ, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st);
         if (e == cudaSuccess)
             e = launch_brick_distance(bs, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st,
-                                      &changed);
+                                      &changed, occ);
         if (e == cudaSuccess)
             e = launch_brick_octants(g->dir, (uint8_t*)(scr + o_da), (uint16_t*)(scr + o_ty), g->oct,
-                                     (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st, &changed);
+                                     (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st, &changed, occ);
         if (e == cudaSuccess)
             e = launch_brick_long(g->dir, g->oct, (uint32_t*)(scr + o_run), g->lng, (int32_t)g->bx,
-                                  (int32_t)g->by, (int32_t)g->bz, st, &changed);
+                                  (int32_t)g->by, (int32_t)g->bz, st, &changed, occ);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) { rc = cuda_fail(e, "vt_grid_update: scatter"); break; }
         uint64_t nonempty = 0;
