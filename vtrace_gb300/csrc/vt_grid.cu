@@ -393,17 +393,21 @@ __host__ __device__ __forceinline__ int32_t occ_words(int32_t bx) { return (bx +
 
 __global__ void __launch_bounds__(256) brick_xmask_kernel(const uint32_t* __restrict__ dir,
                                                           uint32_t* __restrict__ occ, int32_t bx,
-                                                          uint64_t words) {
+                                                          int32_t by, int32_t y0, int32_t ny,
+                                                          int32_t z0, uint64_t words) {
+    // words of the rows y0 .. y0 + ny - 1 of the planes z0 ..
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= words) return;
     const int32_t rw = occ_words(bx);
-    const uint64_t row = t / (uint64_t)rw;
-    const int32_t x0 = (int32_t)(t - row * (uint64_t)rw) * 32;
+    const uint64_t r = t / (uint64_t)rw;
+    const uint64_t row = (uint64_t)(z0 + (int32_t)(r / (uint64_t)ny)) * by + y0 + (int32_t)(r % (uint64_t)ny);
+    const int32_t x0 = (int32_t)(t - r * (uint64_t)rw) * 32;
+    const uint64_t w = row * rw + (uint64_t)(x0 >> 5);
     const uint32_t* d = dir + row * (uint64_t)bx + x0;
     const int32_t n = min(32, bx - x0);
     uint32_t m = 0;
     for (int32_t k = 0; k < n; ++k) m |= (uint32_t)!brick_empty(__ldg(d + k)) << k;
-    occ[t] = m;
+    occ[w] = m;
 }
 
 // Steps from brick x of an occupancy row to the nearest occupied brick in direction s (+1 / -1),
@@ -425,9 +429,20 @@ __device__ __forceinline__ int32_t occ_fwd(const uint32_t* __restrict__ row, int
 }
 
 cudaError_t launch_brick_xmask(const uint32_t* dir, uint32_t* occ, int32_t bx, int32_t by,
-                               int32_t bz, cudaStream_t stream) {
-    const uint64_t words = (uint64_t)occ_words(bx) * by * bz;
-    brick_xmask_kernel<<<(unsigned)((words + 255) / 256), 256, 0, stream>>>(dir, occ, bx, words);
+                               int32_t bz, cudaStream_t stream, const BrickBox* changed) {
+    // after a change, the rows the passes along x read: those of the distance pass's window (its
+    // y and z reach, kMaxBrickDistance twice over, covers the octant and long-box windows)
+    int32_t y0 = 0, ny = by, z0 = 0, nz = bz;
+    if (changed) {
+        const int32_t R = 2 * (int32_t)kMaxBrickDistance;
+        y0 = max(changed->y0 - R, 0);
+        z0 = max(changed->z0 - R, 0);
+        ny = min(changed->y0 + changed->ny + R, by) - y0;
+        nz = min(changed->z0 + changed->nz + R, bz) - z0;
+    }
+    const uint64_t words = (uint64_t)occ_words(bx) * ny * nz;
+    brick_xmask_kernel<<<(unsigned)((words + 255) / 256), 256, 0, stream>>>(dir, occ, bx, by, y0,
+                                                                             ny, z0, words);
     return cudaGetLastError();
 }
 

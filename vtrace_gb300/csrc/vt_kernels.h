@@ -95,9 +95,10 @@ cudaError_t launch_brick_octants(const uint32_t* dir, uint8_t* tmp_x, uint16_t* 
                                  const uint32_t* occ = nullptr);
 // Occupancy bitmask of the directory (brick_xmask_words() words: one bit per brick, rows along x
 // padded to 32 bits), from which the passes along x read their distances when it is given
-// (`occ` of the distance, octant and long-box launches) instead of scanning the directory.
+// (`occ` of the distance, octant and long-box launches) instead of scanning the directory; with
+// `changed`, only the rows those passes read after a change inside it.
 cudaError_t launch_brick_xmask(const uint32_t* dir, uint32_t* occ, int32_t bx, int32_t by,
-                               int32_t bz, cudaStream_t stream);
+                               int32_t bz, cudaStream_t stream, const BrickBox* changed = nullptr);
 size_t brick_xmask_words(int32_t bx, int32_t by, int32_t bz);
 
 // Phase 4: Chebyshev distance of every empty brick to the nearest occupied one, into dir.

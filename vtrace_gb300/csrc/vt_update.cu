@@ -274,7 +274,8 @@ extern "C" int32_t vt_grid_update(int32_t grid, const void* voxels, uint32_t ord
         bs.dist_b = (uint8_t*)(scr + o_db);
         uint32_t* occ = (uint32_t*)(scr + o_occ);
         if (e == cudaSuccess)
-            e = launch_brick_xmask(g->dir, occ, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st);
+            e = launch_brick_xmask(g->dir, occ, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st,
+                                   &changed);
         if (e == cudaSuccess)
             e = launch_brick_distance(bs, g->dir, (int32_t)g->bx, (int32_t)g->by, (int32_t)g->bz, st,
                                       &changed, occ);
