@@ -378,9 +378,10 @@ __device__ __forceinline__ void advance_axis(float& s, int32_t& v, float delta, 
 //
 // Only the axes that can leave first need their exit value S_a(N_a - 1) exactly: the
 // approximation s + (N-1) * delta (one fused multiply-add) is within (N + 2) * 2^-24 of the exact
-// chain relative to its magnitude, so any axis whose approximation exceeds the smallest by more than the sum of both
-// bounds (taken 4x larger here) cannot be the minimum.  Every value compared is computed with
-// real binary32 additions, so the result is bit-identical to iterating the reference loop.
+// chain relative to its magnitude, so any axis whose approximation exceeds the smallest by more
+// than the sum of both bounds (taken 4x larger here) cannot be the minimum.  Every value compared
+// is computed with real binary32 additions, so the result is bit-identical to iterating the
+// reference loop.
 __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, int32_t& vx,
                                              int32_t& vy, int32_t& vz, float dlx, float dly,
                                              float dlz, int32_t stx, int32_t sty, int32_t stz,

@@ -270,7 +270,10 @@ __global__ void __launch_bounds__(256) render_persistent_kernel(
 constexpr int kUnitWait = 4;
 
 // n_dev: nullptr, or the device-side ray count (at most n), read at the start (ray queues whose
-// length the host does not know).
+// length the host does not know).  Held to 48 registers (a few bytes of spills) so that five
+// blocks fit an SM instead of four: the short rays of dense grids wait on their mask and directory
+// loads, and the fifth block hides more of that (16.7M cave rays 2.29 -> 2.17 ms; six blocks at
+// 40 registers spill more and lose).
 __global__ void __launch_bounds__(256, 5) trace_rays_persistent_kernel(
     GridView g, const float2* __restrict__ rays, uint64_t n, uint4* __restrict__ out,
     unsigned long long* __restrict__ counter, uint32_t refill_min,
