@@ -453,6 +453,16 @@ int32_t vt_serve_start(const vt_serve_config* cfg, int32_t* service_out);
  * the life of the service: the cache rebuilds evicted scenes from it). */
 int32_t vt_serve_add_scene(int32_t service, const uint8_t* voxels, const uint32_t* palette,
                            uint32_t nx, uint32_t ny, uint32_t nz, int32_t* scene_out);
+/* Chunk paging into the scene cache (src/gen/pager.rs:52-78): the caller has changed the voxels of
+ * the box (x0, y0, z0) + (w, h, d) of the scene's registered array; if the scene is resident, the
+ * box is written into its grid in place (vt_grid_update), else the next build reads the array.
+ * Pieces of the scene admitted after the call returns render the change (ones admitted while the
+ * caller was changing the array, before the call, may render either state); the call waits until
+ * the scene's pieces in flight have retired, and holds back new ones meanwhile (requests behind
+ * them in arrival order wait too).  The grid's slot arrays may grow, past the budget for a
+ * moment.  VT_EINVAL for an empty box or one outside the scene. */
+int32_t vt_serve_update_scene(int32_t service, int32_t scene, uint32_t x0, uint32_t y0,
+                              uint32_t z0, uint32_t w, uint32_t h, uint32_t d);
 /* Queue a request (width * height * spp below 2^32, else VT_ELIMIT). */
 int32_t vt_serve_submit(int32_t service, const vt_serve_request* req, uint64_t* request_id);
 /* Wait up to timeout_us for a request: VT_OK (image written; the request is released),

@@ -356,3 +356,74 @@ def test_protocol_errors(torch):
     finally:
         svc.stop()
     assert vt.lib().vt_serve_poll(service_id, 1, 0, None) == -4  # the stopped service is gone
+
+
+def test_scene_updates_page_chunks_into_the_cache(torch):
+    """vt_serve_update_scene (the pager's chunk uploads, src/gen/pager.rs:52-78, into the scene
+    cache): boxes written into a resident scene, the first a solid block at its centre and the
+    rest from another thread while requests of the scene are in flight, and into a scene never
+    built (twice over one box); afterwards every request's image equals the oracle's of the
+    updated array, and the centre block changed the oracle's image of the first view."""
+    import threading
+    scenes, views = small_world(8)
+    rng = np.random.default_rng(17)
+    svc = vt.Service(max_inflight=2)
+    try:
+        sids = [svc.add_scene(s["voxels"].copy(), s["palette"]) for s in scenes]
+        arrays = [svc._keep[sid][0] for sid in sids]
+        v0 = next(v for v in views if v["scene"] == 0)
+        buf = pinned(torch, v0["camera"])
+        svc.wait(svc.submit(sids[0], v0["camera"], buf, v0["spp"], v0["seed"], v0["view_id"],
+                            v0["light"]))
+        original = dict(scenes[0], voxels=arrays[0].copy())
+        svc.update_scene(sids[0], (16, 16, 16), np.full((32, 32, 32), 7, np.uint8))
+
+        def chunk(arr):
+            nz, ny, nx = arr.shape
+            d, h, w = (int(rng.integers(4, 20)) for _ in range(3))
+            org = (int(rng.integers(0, nx - w)), int(rng.integers(0, ny - h)), int(rng.integers(0, nz - d)))
+            box = np.where(rng.random((d, h, w)) < 0.5, rng.integers(1, 256, (d, h, w)), 0)
+            return org, box.astype(np.uint8)
+
+        # resident scene 0, while its requests run on the dispatcher
+        bufs = [pinned(torch, v0["camera"]) for _ in range(6)]
+        rids = [svc.submit(sids[0], v0["camera"], b, v0["spp"], v0["seed"], v0["view_id"],
+                           v0["light"]) for b in bufs]
+        errors = []
+
+        def pager():
+            try:
+                for _ in range(5):
+                    org, box = chunk(arrays[0])
+                    svc.update_scene(sids[0], org, box)
+            except Exception as e:  # reported below
+                errors.append(e)
+
+        th = threading.Thread(target=pager)
+        th.start()
+        th.join()
+        for r in rids:
+            svc.wait(r)
+        assert not errors, errors
+        # a scene never built yet, and one updated twice over the same box
+        org, box = chunk(arrays[1])
+        svc.update_scene(sids[1], org, box)
+        svc.update_scene(sids[1], org, box)
+        for v in views:
+            b = pinned(torch, v["camera"])
+            svc.wait(svc.submit(sids[v["scene"]], v["camera"], b, v["spp"], v["seed"],
+                                v["view_id"], v["light"]))
+            img = b.numpy().reshape(v["camera"].height, v["camera"].width, 4)
+            updated = dict(scenes[v["scene"]], voxels=arrays[v["scene"]])
+            np.testing.assert_array_equal(img, oracle_image(updated, v),
+                                          err_msg="view %d" % v["view_id"])
+            if v is v0:
+                assert not np.array_equal(img, oracle_image(original, v)), "update not visible"
+        with pytest.raises(vt.VtError):
+            vt.check(vt.lib().vt_serve_update_scene(svc.id, sids[0], 0, 0, 0, 0, 4, 4))
+        with pytest.raises(vt.VtError):
+            vt.check(vt.lib().vt_serve_update_scene(svc.id, sids[0], 60, 0, 0, 8, 4, 4))
+        with pytest.raises(vt.VtError):
+            vt.check(vt.lib().vt_serve_update_scene(svc.id, 99, 0, 0, 0, 1, 1, 1))
+    finally:
+        svc.stop()

@@ -220,6 +220,7 @@ SIGNATURES = [
     ("vt_serve_default_config", _i32, [ctypes.POINTER(ServeConfig)]),
     ("vt_serve_start", _i32, [ctypes.POINTER(ServeConfig), ctypes.POINTER(ctypes.c_int32)]),
     ("vt_serve_add_scene", _i32, [_i32, _vp, _vp, _u32, _u32, _u32, ctypes.POINTER(ctypes.c_int32)]),
+    ("vt_serve_update_scene", _i32, [_i32, _i32, _u32, _u32, _u32, _u32, _u32, _u32]),
     ("vt_serve_submit", _i32, [_i32, ctypes.POINTER(ServeRequest), ctypes.POINTER(ctypes.c_uint64)]),
     ("vt_serve_poll", _i32, [_i32, _u64, _u32, ctypes.POINTER(ServeTiming)]),
     ("vt_serve_get_stats", _i32, [_i32, ctypes.POINTER(ServeStats)]),
@@ -674,17 +675,29 @@ class Service:
         sid = ctypes.c_int32(-1)
         check(lib().vt_serve_start(ctypes.byref(cfg), ctypes.byref(sid)))
         self.id = sid.value
-        self._keep = []
+        self._keep = {}
 
     def add_scene(self, voxels, palette):
+        """Registers a [z, y, x] u8 scene; the service reads this array (kept here) for its
+        builds."""
         voxels = np.ascontiguousarray(voxels, np.uint8)
         palette = np.ascontiguousarray(palette, np.uint32)
-        self._keep.append((voxels, palette))
         nz, ny, nx = voxels.shape
         out = ctypes.c_int32(-1)
         check(lib().vt_serve_add_scene(self.id, voxels.ctypes.data, palette.ctypes.data, nx, ny,
                                        nz, ctypes.byref(out)))
+        self._keep[out.value] = (voxels, palette)
         return out.value
+
+    def update_scene(self, scene, origin, voxels):
+        """Writes a [d, h, w] u8 box at origin (x0, y0, z0) into the scene's registered array and
+        into its resident grid (vt_serve_update_scene)."""
+        arr = self._keep[scene][0]
+        box = np.asarray(voxels, np.uint8)
+        d, h, w = box.shape
+        x0, y0, z0 = origin
+        arr[z0:z0 + d, y0:y0 + h, x0:x0 + w] = box
+        check(lib().vt_serve_update_scene(self.id, scene, x0, y0, z0, w, h, d))
 
     def submit(self, scene, camera, out_rgba, spp=1, seed=0, view_id=0, light=None):
         if out_rgba is not None and not isinstance(out_rgba, int) and \

@@ -669,7 +669,7 @@ void vt_shutdown(void) {
 
 const char* vt_last_error(void) { return g_last_error.c_str(); }
 
-uint32_t vt_version(void) { return (1u << 16) | 2u; }
+uint32_t vt_version(void) { return (1u << 16) | 3u; }
 
 void* vt_get_stream(void) {
     if (ensure_init()) return nullptr;

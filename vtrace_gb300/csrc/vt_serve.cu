@@ -93,6 +93,7 @@ struct ServeScene {
     int32_t grid = -1;
     int32_t refs = 0;  // in-flight and packed pieces
     bool loading = false;
+    bool updating = false;  // a vt_serve_update_scene is writing its grid: no piece is admitted
     uint64_t last_use = 0;
     uint64_t bytes = 0;
 };
@@ -294,6 +295,9 @@ bool Service::pack(Slot& slot, std::unique_lock<std::mutex>& lk) {
                 continue;
             }
         }
+        // a scene being updated admits no piece until the update is written: the head of the
+        // line keeps its place
+        if (scenes[q.r.scene]->updating) break;
         // (admit_scene may release the lock while it builds a grid; only this thread pops
         // `pending`, so its front is still `pc` afterwards)
         const int32_t rc = admit_scene(lk, q.r.scene);
@@ -434,6 +438,7 @@ void Service::retire(Slot& slot, int32_t error) {
     slot.extra_bytes = 0;
     slot.pieces.clear();
     slot.busy = false;
+    cv_done.notify_all();  // scene updates wait for their scene's pieces to retire
 }
 
 void Service::run() {
@@ -588,6 +593,47 @@ int32_t vt_serve_add_scene(int32_t service, const uint8_t* voxels, const uint32_
     s->scenes.push_back(std::move(sc));
     *scene_out = (int32_t)s->scenes.size() - 1;
     return VT_OK;
+}
+
+int32_t vt_serve_update_scene(int32_t service, int32_t scene, uint32_t x0, uint32_t y0,
+                              uint32_t z0, uint32_t w, uint32_t h, uint32_t d) {
+    std::shared_ptr<Service> s = lookup_service(service);
+    if (!s) return fail(VT_ENOTFOUND, "vt_serve_update_scene: unknown service");
+    std::unique_lock<std::mutex> lk(s->mu);
+    if (scene < 0 || (size_t)scene >= s->scenes.size())
+        return fail(VT_ENOTFOUND, "vt_serve_update_scene: unknown scene");
+    ServeScene& sc = *s->scenes[scene];
+    if (w == 0 || h == 0 || d == 0 || (uint64_t)x0 + w > sc.nx || (uint64_t)y0 + h > sc.ny ||
+        (uint64_t)z0 + d > sc.nz)
+        return fail(VT_EINVAL, "vt_serve_update_scene: empty box or box outside the scene");
+    // one update of a scene at a time; then no new piece of it is admitted, and the update waits
+    // for the pieces in flight (and a build in progress) to end
+    while (sc.updating) s->cv_done.wait(lk);
+    sc.updating = true;
+    while (sc.refs > 0 || sc.loading) s->cv_done.wait(lk);
+    int32_t rc = VT_OK;
+    const int32_t g = sc.grid;
+    if (g >= 0) {  // resident: write the box into the grid (an evicted scene is rebuilt from the
+                   // caller's array, which already holds the change)
+        lk.unlock();
+        std::vector<uint8_t> box((size_t)w * h * d);
+        for (uint32_t z = 0; z < d; ++z)
+            for (uint32_t y = 0; y < h; ++y)
+                memcpy(box.data() + ((size_t)z * h + y) * w,
+                       sc.voxels + (((size_t)(z0 + z) * sc.ny + (y0 + y)) * sc.nx + x0), w);
+        rc = vt_grid_update(g, box.data(), VT_ORDER_X_FASTEST, x0, y0, z0, w, h, d);
+        vt_grid_info info;
+        const bool known = vt_grid_get_info(g, &info) == VT_OK;
+        lk.lock();
+        if (known) {  // the slot arrays may have grown
+            s->resident_bytes += info.device_bytes - sc.bytes;
+            sc.bytes = info.device_bytes;
+        }
+    }
+    sc.updating = false;
+    s->cv_done.notify_all();
+    s->cv.notify_one();
+    return rc;
 }
 
 int32_t vt_serve_submit(int32_t service, const vt_serve_request* req, uint64_t* request_id) {
