@@ -244,6 +244,7 @@ int32_t Service::admit_scene(std::unique_lock<std::mutex>& lk, int32_t scene) {
     const bool ok = g >= 0 && vt_grid_get_info(g, &info) == VT_OK;
     lk.lock();
     s.loading = false;
+    cv_done.notify_all();  // a scene update may be waiting for the build to end
     resident_bytes -= need;
     if (!ok) return g < 0 ? g : VT_ECUDA;
     s.grid = g;
