@@ -215,7 +215,7 @@ bool Service::evict_for(uint64_t need) {
     while (used() + need > cfg.hbm_budget_bytes) {
         ServeScene* victim = nullptr;
         for (auto& s : scenes)
-            if (s->grid >= 0 && s->refs == 0 && !s->loading &&
+            if (s->grid >= 0 && s->refs == 0 && !s->loading && !s->updating &&
                 (!victim || s->last_use < victim->last_use))
                 victim = s.get();
         if (!victim) return false;
