@@ -427,3 +427,54 @@ def test_scene_updates_page_chunks_into_the_cache(torch):
             vt.check(vt.lib().vt_serve_update_scene(svc.id, 99, 0, 0, 0, 1, 1, 1))
     finally:
         svc.stop()
+
+
+def test_scene_updates_while_the_cache_evicts(torch):
+    """Room for one scene at a time: requests alternating between two scenes evict each in turn
+    while another thread pages boxes into the first; no update lands in a grid being evicted or
+    rebuilt, and the final images equal the oracle's of the updated arrays."""
+    import threading
+    scenes, views = small_world(8)
+    scenes, views = scenes[:2], [v for v in views if v["scene"] < 2]
+    bound = max(grid_bound(s["n"]) for s in scenes)
+    cap = 160 * 120 * 4
+    svc = vt.Service(hbm_budget_bytes=bound + 1024 + cap * 20, max_inflight=1,
+                     max_samples_per_launch=cap)
+    rng = np.random.default_rng(5)
+    try:
+        sids = [svc.add_scene(s["voxels"].copy(), s["palette"]) for s in scenes]
+        arrays = [svc._keep[sid][0] for sid in sids]
+        errors, done = [], threading.Event()
+
+        def pager():
+            try:
+                n = arrays[0].shape[0]
+                while not done.is_set():
+                    org = tuple(int(x) for x in rng.integers(0, n - 8, 3))
+                    box = np.where(rng.random((8, 8, 8)) < 0.5, rng.integers(1, 256, (8, 8, 8)), 0)
+                    svc.update_scene(sids[0], org, box.astype(np.uint8))
+            except Exception as e:
+                errors.append(e)
+
+        th = threading.Thread(target=pager)
+        th.start()
+        try:
+            for _ in range(3):
+                for v in views:
+                    svc.wait(svc.submit(sids[v["scene"]], v["camera"], pinned(torch, v["camera"]),
+                                        v["spp"], v["seed"], v["view_id"], v["light"]))
+        finally:
+            done.set()
+            th.join()
+        assert not errors, errors
+        assert svc.stats()["evictions"] > 0
+        for v in views:
+            b = pinned(torch, v["camera"])
+            svc.wait(svc.submit(sids[v["scene"]], v["camera"], b, v["spp"], v["seed"],
+                                v["view_id"], v["light"]))
+            img = b.numpy().reshape(v["camera"].height, v["camera"].width, 4)
+            updated = dict(scenes[v["scene"]], voxels=arrays[v["scene"]])
+            np.testing.assert_array_equal(img, oracle_image(updated, v),
+                                          err_msg="view %d" % v["view_id"])
+    finally:
+        svc.stop()
