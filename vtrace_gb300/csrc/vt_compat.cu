@@ -422,7 +422,7 @@ static __host__ __device__ bool instance_tiles(const CullFrame& cf, const double
         for (int k = 0; k < 3; ++k) fro += mi[k * 4 + r] * mi[k * 4 + r];
     }
     if (!(d2 > 0.0) || !isfinite(d2) || !(fro > 0.0) || !isfinite(fro)) return true;
-    const double eps = 0.5 * sqrt(d2) / sqrt(fro) / cf.len_max;
+    const double eps = 0.5 * sqrt(d2 / fro) / cf.len_max;
     // corners in q space
     double q[8][3];
     for (int k = 0; k < 8; ++k) {
@@ -437,7 +437,7 @@ static __host__ __device__ bool instance_tiles(const CullFrame& cf, const double
     double xmin = INFINITY, xmax = -INFINITY, ymin = INFINITY, ymax = -INFINITY;
     int used = 0;
     auto take = [&](const double* p) {
-        const double xn = p[0] / p[2], yn = p[1] / p[2];
+        const double r = 1.0 / p[2], xn = p[0] * r, yn = p[1] * r;
         xmin = fmin(xmin, xn);
         xmax = fmax(xmax, xn);
         ymin = fmin(ymin, yn);
