@@ -365,6 +365,50 @@ __device__ __forceinline__ void advance_axis(float& s, int32_t& v, float delta, 
     stepped_last = x == t_star;
 }
 
+// Number of additions for an axis that cannot leave the box first: the estimate
+// floor((amin - s) / delta) of its events after S(0) up to `amin` (the smallest approximate exit),
+// at most n_exit - 2; 0 when its first event is already past it (also the axes with no step, whose
+// side distance is +inf).  Only a speed hint: finish_axis checks the prefix exactly.  A margin of
+// one addition below the estimate (so that the prefix never passes T*) measured 2% slower frames
+// than settling the rare overshoot from S(0).
+__device__ __forceinline__ int32_t prefix_count(float s, float delta, int32_t n_exit, float amin) {
+    if (s > amin) return 0;
+    return max(min((int32_t)__fdividef(__fsub_rn(amin, s), delta), n_exit - 2), 0);
+}
+
+// State of one axis after the crossing, from h = S(k) (its one chain): a candidate whose exit value
+// is the minimum steps out of the box; any other axis walks up exactly from its prefix to its last
+// event at or before t_star.  A candidate that does not leave first, or a prefix past t_star (an
+// event of this axis between T* and amin, or the estimate's rounding), is settled from S(0) by
+// advance_axis.
+__device__ __forceinline__ void finish_axis(float& s, int32_t& v, float h, int32_t k, bool cand,
+                                            float delta, int32_t st, int32_t n_exit, float t_star,
+                                            bool& stepped_last) {
+    if (cand) {
+        if (h == t_star) {
+            s = __fadd_rn(h, delta);
+            v += st * n_exit;
+            stepped_last = true;
+            return;
+        }
+    } else if (h <= t_star) {
+        float x = h, y = __fadd_rn(h, delta);
+        while (y <= t_star && k + 1 < n_exit) {
+            x = y;
+            y = __fadd_rn(y, delta);
+            ++k;
+        }
+        s = y;
+        v += st * (k + 1);
+        stepped_last = x == t_star;
+        return;
+    } else if (k == 0) {  // h = S(0) > t_star: no event in the crossing
+        stepped_last = false;
+        return;
+    }
+    advance_axis(s, v, delta, st, n_exit, t_star, stepped_last);
+}
+
 // Crossing of an empty box of voxels by the reference DDA, computed per axis.
 //
 // In trace.frag's loop each axis a advances on the iterations where its side distance is the
@@ -379,7 +423,11 @@ __device__ __forceinline__ void advance_axis(float& s, int32_t& v, float delta, 
 // Only the axes that can leave first need their exit value S_a(N_a - 1) exactly: the
 // approximation s + (N-1) * delta (one fused multiply-add) is within (N + 2) * 2^-24 of the exact
 // chain relative to its magnitude, so any axis whose approximation exceeds the smallest by more
-// than the sum of both bounds (taken 4x larger here) cannot be the minimum.  Every value compared
+// than the sum of both bounds (taken 4x larger here) cannot be the minimum.  Each axis runs one
+// chain of additions, so a warp whose lanes leave their boxes along different axes runs three
+// chains rather than one per axis and role (4% faster frames than exit chains followed by
+// separate advances): the candidates to their exit value, the others to the prefix of their
+// estimated count, from which finish_axis walks up once T* is known.  Every value compared
 // is computed with real binary32 additions, so the result is bit-identical to iterating the
 // reference loop.
 __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, int32_t& vx,
@@ -400,31 +448,16 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
     const bool cx = stx && ax <= lim;
     const bool cy = sty && ay <= lim;
     const bool cz = stz && az <= lim;
-    const float tx = cx ? add_chain(sx, dlx, nxe - 1) : INFINITY;
-    const float ty = cy ? add_chain(sy, dly, nye - 1) : INFINITY;
-    const float tz = cz ? add_chain(sz, dlz, nze - 1) : INFINITY;
-    const float ts = fminf(fminf(tx, ty), tz);
-    if (cx && tx == ts) {
-        sx = __fadd_rn(tx, dlx);
-        vx += stx * nxe;
-        mx = true;
-    } else {
-        advance_axis(sx, vx, dlx, stx, nxe, ts, mx);
-    }
-    if (cy && ty == ts) {
-        sy = __fadd_rn(ty, dly);
-        vy += sty * nye;
-        my = true;
-    } else {
-        advance_axis(sy, vy, dly, sty, nye, ts, my);
-    }
-    if (cz && tz == ts) {
-        sz = __fadd_rn(tz, dlz);
-        vz += stz * nze;
-        mz = true;
-    } else {
-        advance_axis(sz, vz, dlz, stz, nze, ts, mz);
-    }
+    const int32_t kx = cx ? nxe - 1 : prefix_count(sx, dlx, nxe, amin);
+    const int32_t ky = cy ? nye - 1 : prefix_count(sy, dly, nye, amin);
+    const int32_t kz = cz ? nze - 1 : prefix_count(sz, dlz, nze, amin);
+    const float hx = add_chain(sx, dlx, kx);
+    const float hy = add_chain(sy, dly, ky);
+    const float hz = add_chain(sz, dlz, kz);
+    const float ts = fminf(fminf(cx ? hx : INFINITY, cy ? hy : INFINITY), cz ? hz : INFINITY);
+    finish_axis(sx, vx, hx, kx, cx, dlx, stx, nxe, ts, mx);
+    finish_axis(sy, vy, hy, ky, cy, dly, sty, nye, ts, my);
+    finish_axis(sz, vz, hz, kz, cz, dlz, stz, nze, ts, mz);
 }
 
 // Moves along one axis from voxel v (in brick bi) to the far face of a box reaching r bricks
