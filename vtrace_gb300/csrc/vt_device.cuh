@@ -435,9 +435,11 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
                                              float dlz, int32_t stx, int32_t sty, int32_t stz,
                                              int32_t nxe, int32_t nye, int32_t nze, bool& mx,
                                              bool& my, bool& mz) {
-    const float ax = stx ? __fmaf_rn(__int2float_rn(nxe - 1), dlx, sx) : INFINITY;
-    const float ay = sty ? __fmaf_rn(__int2float_rn(nye - 1), dly, sy) : INFINITY;
-    const float az = stz ? __fmaf_rn(__int2float_rn(nze - 1), dlz, sz) : INFINITY;
+    // An axis with no step (N = 0, side and delta +inf) gives NaN here, which fminf and the
+    // candidate comparison below pass over.
+    const float ax = __fmaf_rn(__int2float_rn(nxe - 1), dlx, sx);
+    const float ay = __fmaf_rn(__int2float_rn(nye - 1), dly, sy);
+    const float az = __fmaf_rn(__int2float_rn(nze - 1), dlz, sz);
     // Candidates: an axis within 2 * amin of the smallest approximation carries at most
     // (Nmax + 2) * 2 * amin * 2^-24 of error, so (Nmax + 2) * amin * 2^-20 bounds the errors of
     // both sides of its comparison with the smallest (with the 4x margin above); axes beyond it
@@ -445,9 +447,9 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
     const float amin = fminf(fminf(ax, ay), az);
     const int32_t nmax = max(max(nxe, nye), nze);
     const float lim = __fmaf_rn(__int2float_rn(nmax + 2) * 0x1p-20f, amin, amin);
-    const bool cx = stx && ax <= lim;
-    const bool cy = sty && ay <= lim;
-    const bool cz = stz && az <= lim;
+    const bool cx = ax <= lim;
+    const bool cy = ay <= lim;
+    const bool cz = az <= lim;
     const int32_t kx = cx ? nxe - 1 : prefix_count(sx, dlx, nxe, amin);
     const int32_t ky = cy ? nye - 1 : prefix_count(sy, dly, nye, amin);
     const int32_t kz = cz ? nze - 1 : prefix_count(sz, dlz, nze, amin);
