@@ -149,6 +149,19 @@ def roofline(algo_bytes, ms, kernel, **extra):
     return out
 
 
+def phase_shares(prof):
+    """Shares of the frame's warp time by ray kind and traversal phase (vt_render_phases)."""
+    total = sum(sum(prof[k].values()) for k in ("camera", "shadow"))
+    out = {k: {ph: round(v / total, 4) for ph, v in prof[k].items()} for k in ("camera", "shadow")}
+    out["passes"] = prof["passes"]
+    out["warps"] = prof["warps"]
+    out["note"] = ("share of warp residency per phase (SM clock read at warp-synchronous points "
+                   "of an instrumented build of the default 8x4-tile launch): load latency "
+                   "included, which other warps hide in this issue-bound kernel, so not a "
+                   "share of issue slots")
+    return out
+
+
 def stats_bytes(st, records, io_per_ray=0):
     """Algorithmic bytes of a launch from its traversal counters: 4 B per brick directory entry
     visited, 64 B per occupied brick's mask entered, 5 B per hit (payload byte + palette entry),
@@ -426,6 +439,7 @@ def run_ours(args):
     # the frame's distinct footprint
     stats = vt.render_stats(grid, cam, light, d_hits)
     fp = vt.render_footprint(grid, cam, light, d_hits)
+    phases = phase_shares(vt.render_phases(grid, cam, light, d_hits))
     unique_bytes = (4 * fp["bricks"] + 64 * fp["nonempty_bricks"] + 512 * fp["hit_bricks"] +
                     16 * npx)
     rays_per_frame = stats["rays"]
@@ -528,6 +542,7 @@ def run_ours(args):
             issue=issue),
         "clocks": clocks,
         "grid_info": grid.info(),
+        "phase_profile": phases,
     }
     if tuning:
         tuning["render"]["installed"] = vt.get_tuning(vt.KERNEL_RENDER)

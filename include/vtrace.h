@@ -314,6 +314,28 @@ typedef struct vt_footprint {
 } vt_footprint;
 int32_t vt_render_footprint(int32_t grid, const vt_camera* camera, const vt_light* light,
                             vt_hit* d_hits, vt_footprint* out);
+/* Warp-time phase profile of one vt_render frame (a separate, slower build of the render kernel,
+ * default 8x4-pixel warp tiles in 128-thread blocks; same records as vt_render).  At each
+ * warp-synchronous point of the traversal the warp reads the SM clock and charges the cycles since
+ * its previous point to a phase: its residency in each phase, load latency included (in an
+ * issue-bound launch other warps issue meanwhile), not issue slots.  The clock reads add about a
+ * third to the frame time. */
+#define VT_PHASE_SETUP 0        /* ray set-up up to the first traversal pass (raygen or shadow
+                                   origin, slab, DDA set-up; a warp with no pass charges its tail) */
+#define VT_PHASE_LOOP 1         /* traversal loop top: inside test, directory load, kind ballot */
+#define VT_PHASE_WALK 2         /* walks through occupied bricks */
+#define VT_PHASE_CROSS_BOX 3    /* empty-box crossing: box, exit approximations, prefix estimates */
+#define VT_PHASE_CROSS_CHAINS 4 /* empty-box crossing: chains of binary32 additions */
+#define VT_PHASE_CROSS_FINISH 5 /* empty-box crossing: prefix walk-ups, exits, settles */
+#define VT_PHASE_TAIL 6         /* hit record; after the shadow ray also shading and the store */
+#define VT_PHASES 7
+typedef struct vt_phase_profile {
+    uint64_t warp_cycles[2][VT_PHASES]; /* [0 camera rays, 1 shadow rays][VT_PHASE_*] */
+    uint64_t passes[2][2];              /* [camera, shadow][0 walk, 1 crossing] traversal passes */
+    uint64_t warps;                     /* warps of the launch */
+} vt_phase_profile;
+int32_t vt_render_phases(int32_t grid, const vt_camera* camera, const vt_light* light,
+                         vt_hit* d_hits, vt_phase_profile* out);
 int32_t vt_trace_rays_stats(int32_t grid, const vt_ray* d_rays, uint64_t n, vt_hit* d_hits,
                             vt_trace_stats* stats);
 

@@ -153,6 +153,14 @@ class Footprint(ctypes.Structure):
                 ("hit_bricks", ctypes.c_uint64), ("reserved", ctypes.c_uint64)]
 
 
+PHASES = ("setup", "loop", "walk", "cross_box", "cross_chains", "cross_finish", "tail")
+
+
+class PhaseProfile(ctypes.Structure):
+    _fields_ = [("warp_cycles", (ctypes.c_uint64 * len(PHASES)) * 2),
+                ("passes", (ctypes.c_uint64 * 2) * 2), ("warps", ctypes.c_uint64)]
+
+
 class VoxInfo(ctypes.Structure):
     _fields_ = [("version", ctypes.c_uint32), ("models", ctypes.c_uint32),
                 ("has_palette", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
@@ -206,6 +214,8 @@ SIGNATURES = [
                                ctypes.POINTER(TraceStats)]),
     ("vt_render_footprint", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp,
                                    ctypes.POINTER(Footprint)]),
+    ("vt_render_phases", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(Light), _vp,
+                                ctypes.POINTER(PhaseProfile)]),
     ("vt_trace_rays_stats", _i32, [_i32, _vp, _u64, _vp, ctypes.POINTER(TraceStats)]),
     ("vt_path_trace", _i32, [_i32, ctypes.POINTER(Camera), ctypes.POINTER(PathParams), _vp, _vp,
                              _vp]),
@@ -590,6 +600,22 @@ def render_footprint(grid, camera, light, d_hits):
                                     ctypes.byref(light) if light is not None else None,
                                     _ptr(d_hits), ctypes.byref(fp)))
     return {"bricks": fp.bricks, "nonempty_bricks": fp.nonempty_bricks, "hit_bricks": fp.hit_bricks}
+
+
+def render_phases(grid, camera, light, d_hits):
+    """Warp-time phase profile of one frame (vt_render_phases; same records in `d_hits` as
+    render): {"camera": {phase: warp cycles}, "shadow": {...}, "passes": {"camera_walk",
+    "camera_cross", "shadow_walk", "shadow_cross"}, "warps": n}, phases as in PHASES."""
+    pp = PhaseProfile()
+    check(lib().vt_render_phases(grid.id, ctypes.byref(camera),
+                                 ctypes.byref(light) if light is not None else None,
+                                 _ptr(d_hits), ctypes.byref(pp)))
+    out = {kind: {ph: int(pp.warp_cycles[k][i]) for i, ph in enumerate(PHASES)}
+           for k, kind in enumerate(("camera", "shadow"))}
+    out["passes"] = {"camera_walk": int(pp.passes[0][0]), "camera_cross": int(pp.passes[0][1]),
+                     "shadow_walk": int(pp.passes[1][0]), "shadow_cross": int(pp.passes[1][1])}
+    out["warps"] = int(pp.warps)
+    return out
 
 
 def render_stats(grid, camera, light, d_hits):

@@ -1063,6 +1063,37 @@ int32_t vt_render_footprint(int32_t grid, const vt_camera* camera, const vt_ligh
     return VT_OK;
 }
 
+int32_t vt_render_phases(int32_t grid, const vt_camera* camera, const vt_light* light,
+                         vt_hit* d_hits, vt_phase_profile* out) {
+    Grid* g = lookup_grid(grid);
+    if (!g) return fail(VT_ENOTFOUND, "vt_render_phases: unknown grid");
+    int32_t rc = check_camera(camera);
+    if (rc) return rc;
+    if (!out || !d_hits || ((uintptr_t)d_hits & 15u)) return fail(VT_EINVAL, "vt_render_phases: bad buffer");
+    const unsigned words = phase_profile_words();
+    unsigned long long* dt = nullptr;
+    cudaStream_t st = state().stream;
+    if (cudaMalloc(&dt, words * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(VT_ENOMEM, "cudaMalloc(phase totals)");
+    }
+    std::vector<unsigned long long> h(words);
+    cudaError_t e = cudaMemsetAsync(dt, 0, words * sizeof(unsigned long long), st);
+    if (e == cudaSuccess)
+        e = launch_render_phases(g->view(), *camera, light_view(light), (uint4*)d_hits, dt, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h.data(), dt, words * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dt);
+    if (e != cudaSuccess) return cuda_fail(e, "vt_render_phases");
+    for (int k = 0; k < 2; ++k) {
+        for (int p = 0; p < VT_PHASES; ++p) out->warp_cycles[k][p] = h[k * VT_PHASES + p];
+        for (int j = 0; j < 2; ++j) out->passes[k][j] = h[2 * VT_PHASES + 2 * k + j];
+    }
+    out->warps = h[2 * VT_PHASES + 4];
+    return VT_OK;
+}
+
 int32_t vt_render_host(int32_t grid, const vt_camera* camera, const vt_light* light,
                        vt_hit* hits) {
     Grid* g = lookup_grid(grid);

@@ -18,6 +18,19 @@
 
 #include "vtrace.h"
 
+// Hooks of the warp-time phase profile (vt_render_phases): they compile to nothing unless the
+// translation unit defines VT_PHASE_CLOCKS together with vt::phase_mark, vt::phase_pass and
+// vt::phase_kind (vt_phase.cu), so every other kernel is built without them.
+#ifdef VT_PHASE_CLOCKS
+#define VT_PHASE_MARK(mask, phase) phase_mark((mask), (phase))
+#define VT_PHASE_PASS(mask, walk) phase_pass((mask), (walk))
+#define VT_PHASE_KIND(mask, kind) phase_kind((mask), (kind))
+#else
+#define VT_PHASE_MARK(mask, phase) ((void)0)
+#define VT_PHASE_PASS(mask, walk) ((void)0)
+#define VT_PHASE_KIND(mask, kind) ((void)0)
+#endif
+
 namespace vt {
 
 constexpr uint32_t kEmptyBit = 0x80000000u;
@@ -453,10 +466,12 @@ __device__ __forceinline__ void cross_region(float& sx, float& sy, float& sz, in
     const int32_t kx = cx ? nxe - 1 : prefix_count(sx, dlx, nxe, amin);
     const int32_t ky = cy ? nye - 1 : prefix_count(sy, dly, nye, amin);
     const int32_t kz = cz ? nze - 1 : prefix_count(sz, dlz, nze, amin);
+    VT_PHASE_MARK(__activemask(), VT_PHASE_CROSS_BOX);
     const float hx = add_chain(sx, dlx, kx);
     const float hy = add_chain(sy, dly, ky);
     const float hz = add_chain(sz, dlz, kz);
     const float ts = fminf(fminf(cx ? hx : INFINITY, cy ? hy : INFINITY), cz ? hz : INFINITY);
+    VT_PHASE_MARK(__activemask(), VT_PHASE_CROSS_CHAINS);
     finish_axis(sx, vx, hx, kx, cx, dlx, stx, nxe, ts, mx);
     finish_axis(sy, vy, hy, ky, cy, dly, sty, nye, ts, my);
     finish_axis(sz, vz, hz, kz, cz, dlz, stz, nze, ts, mz);
@@ -564,11 +579,13 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
             // waits end.
             const bool walk = !brick_empty(e);
             const uint32_t act = __activemask();
+            VT_PHASE_MARK(act, VT_PHASE_LOOP);
             const uint32_t wb = __ballot_sync(act, walk), cb = act & ~wb;
             bool run_walk = __popc(wb) >= __popc(cb);
             if (run_walk ? (cb && pend_c) : (wb && pend_w)) run_walk = !run_walk;
             pend_w = !run_walk && wb;
             pend_c = run_walk && cb;
+            VT_PHASE_PASS(act, run_walk);
             if (walk != run_walk) continue;
         }
         --guard;
@@ -594,6 +611,7 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
             vx = (bxi << 3) + lx;
             vy = (byi << 3) + ly;
             vz = (bzi << 3) + lz;
+            VT_PHASE_MARK(__activemask(), VT_PHASE_WALK);
             if (hit) break;
         } else {
             const uint32_t ow = octant_word(g, bidx);
@@ -603,6 +621,7 @@ __device__ __forceinline__ void dda_skip(const GridView& g, float px, float py, 
                         nye, nze);
             cross_region(sx, sy, sz, vx, vy, vz, dlx, dly, dlz, stx, sty, stz, nxe, nye, nze, mx,
                          my, mz);
+            VT_PHASE_MARK(__activemask(), VT_PHASE_CROSS_FINISH);
         }
     }
     (void)max_steps;
@@ -888,6 +907,49 @@ __device__ __forceinline__ HitRec shade_ray(const GridView& g, const LightView& 
     }
     h.w3 = shade_rgba(h.w3, ndl, vis, L.ambient);
     h.w1 |= extra << 24;
+    return h;
+}
+
+// One pixel of vt_render (the body of render_kernel): camera ray, shading and shadow ray, with the
+// warp (lanes `vmask`) re-converged between the camera rays and the shadow rays.  Same record as
+// shade_ray.
+template <bool STATS>
+__device__ __forceinline__ HitRec render_pixel(const GridView& g, const vt_camera& cam,
+                                               const LightView& light, uint32_t px, uint32_t py,
+                                               uint32_t vmask, Tally<STATS>& tl) {
+    float o[3], d[3];
+    raygen(cam, px, py, 0.5f, 0.5f, o, d);
+    HitRec h = trace_ray<STATS>(g, o, d, tl);
+    // The warp's shadow rays start together: lanes reaching theirs at different times would run
+    // them as separate groups (a third of the lanes per traversal pass).
+    __syncwarp(vmask);
+    VT_PHASE_MARK(vmask, VT_PHASE_TAIL);
+    VT_PHASE_KIND(vmask, 1);
+    const uint32_t flags = h.w1 >> 24;
+    float ndl = 0.0f;
+    if (!(flags & VT_HIT_FLAG_HIT)) {
+        h.w3 = VT_SKY_RGBA;
+    } else {
+        tl.hit();
+        if (light.enabled && face_lit(h, light, ndl)) {
+            float vis = 1.0f;
+            uint32_t extra = 0;
+            if (ndl > 0.0f && light.shadows) {
+                float so[3];
+                shadow_origin(h, o, d, so);
+                const float ld[3] = {light.dx, light.dy, light.dz};
+                const HitRec s = trace_ray<STATS>(g, so, ld, tl);
+                tl.shadow();
+                extra |= VT_HIT_FLAG_SHADOW_RAY;
+                if ((s.w1 >> 24) & VT_HIT_FLAG_HIT) {
+                    vis = 0.0f;
+                    extra |= VT_HIT_FLAG_SHADOWED;
+                }
+            }
+            h.w3 = shade_rgba(h.w3, ndl, vis, light.ambient);
+            h.w1 |= extra << 24;
+        }
+    }
     return h;
 }
 

@@ -44,6 +44,11 @@ cudaError_t launch_trace_rays_persistent(const GridView& g, const vt_ray* rays, 
 cudaError_t launch_render(const GridView& g, const vt_camera& cam, const LightView& light,
                           uint4* out, Counters* counters, cudaStream_t stream, uint32_t row0 = 0,
                           uint32_t row1 = 0, const TraceTuning* tune = nullptr);
+// Warp-time phase profile of one frame (vt_phase.cu): `totals` holds phase_profile_words() words,
+// zeroed, and receives per kind and phase the warp cycles, then the passes, then the warp count.
+unsigned phase_profile_words();
+cudaError_t launch_render_phases(const GridView& g, const vt_camera& cam, const LightView& light,
+                                 uint4* out, unsigned long long* totals, cudaStream_t stream);
 // n_dev as for launch_trace_rays_persistent: the device-side ray count (at most n), or nullptr.
 cudaError_t launch_trace_rays(const GridView& g, const vt_ray* rays, uint64_t n, uint4* out,
                               Counters* counters, cudaStream_t stream,

@@ -58,38 +58,7 @@ __global__ void __launch_bounds__(256) render_kernel(GridView g, vt_camera cam, 
     if (px >= cam.width || py >= row1) return;
     Tally<STATS> tl;
     tl.bind(counters, g.bricks);
-    float o[3], d[3];
-    raygen(cam, px, py, 0.5f, 0.5f, o, d);
-    HitRec h = trace_ray<STATS>(g, o, d, tl);
-    // The warp's shadow rays start together: lanes reaching theirs at different times would run
-    // them as separate groups (a third of the lanes per traversal pass).  The shading is
-    // shade_ray's, written out here around the re-convergence.
-    __syncwarp(vmask);
-    const uint32_t flags = h.w1 >> 24;
-    float ndl = 0.0f;
-    if (!(flags & VT_HIT_FLAG_HIT)) {
-        h.w3 = VT_SKY_RGBA;
-    } else {
-        tl.hit();
-        if (light.enabled && face_lit(h, light, ndl)) {
-            float vis = 1.0f;
-            uint32_t extra = 0;
-            if (ndl > 0.0f && light.shadows) {
-                float so[3];
-                shadow_origin(h, o, d, so);
-                const float ld[3] = {light.dx, light.dy, light.dz};
-                const HitRec s = trace_ray<STATS>(g, so, ld, tl);
-                tl.shadow();
-                extra |= VT_HIT_FLAG_SHADOW_RAY;
-                if ((s.w1 >> 24) & VT_HIT_FLAG_HIT) {
-                    vis = 0.0f;
-                    extra |= VT_HIT_FLAG_SHADOWED;
-                }
-            }
-            h.w3 = shade_rgba(h.w3, ndl, vis, light.ambient);
-            h.w1 |= extra << 24;
-        }
-    }
+    const HitRec h = render_pixel<STATS>(g, cam, light, px, py, vmask, tl);
     out[(size_t)py * cam.width + px] = make_uint4(h.w0, h.w1, h.w2, h.w3);
     tl.flush(counters);
 }
